@@ -1,0 +1,650 @@
+// ORACLE — test infrastructure only.  Only tests/, __graft_entry__.smoke() and
+// bench.py's CPU-baseline leg may load this library, and only as the checker
+// or the timed CPU baseline.  It is never part of the product path.
+//
+// CPU restatement (C++, FP64, OpenMP where the reference uses OpenMP) of the
+// reference's linRotCartSph_NoQuad Hv path, written from its behaviour:
+//
+//   inputs     HvInputFile tokens       HvCalc/NoQuadOnTheFly/linRotCartSphHvFullVPrepRoutines.cpp:246-348
+//              cage .xyz                potentialCalc/Alavi/SPCE/SPCE_AH2_EngRoutines.cpp:5-108
+//              IsoHarmOsc input          potentialCalc/IsotropicHarmonicOscillatorPotential/IsoHarmOsc_Routines.cpp:34-79
+//   tables     genIndices_lm             HvCalc/linRotCartSphHvRoutines.cpp:24-68
+//              gauleg                    HvCalc/linRotCartSphHvRoutines.cpp:219-255
+//              normAssocLegendrePoly     HvCalc/linRotCartSphHvRoutines.cpp:293-403
+//              tesseralTrigTerm          HvCalc/linRotCartSphHvRoutines.cpp:405-434
+//              gaussChebyshev            HvCalc/linRotCartSphHvRoutines.cpp:450-463
+//              cartKinGrid               HvCalc/linRotCartSphHvRoutines.cpp:484-517
+//              rotKinEng                 HvCalc/linRotCartSphHvRoutines.cpp:522-538
+//              QuadraturePrep            HvCalc/linRotCartSphHvRoutines.cpp:1480-1532
+//              TesseralPrep              HvCalc/linRotCartSphHvRoutines.cpp:1534-1735
+//   potential  Alavi_SiteSite_Eng_contGrid potentialCalc/Alavi/AlaviGeneric/Alavi_ContGrid_H2_Routines.cpp:6-147
+//              Q_SPCE_Eng / LJ_SPCE_Eng_Fast potentialCalc/Alavi/SPCE/SPCE_AH2_EngRoutines.cpp:110-178
+//              CoulombEng / LJEngFast    potentialCalc/CommonRoutines/energyRoutines.cpp:5-54
+//              rotMat3D                  librarySources/matVecClasses/rotmat.cpp:6-32
+//              IsoHarmOscEng             potentialCalc/IsotropicHarmonicOscillatorPotential/IsoHarmOsc_Routines.cpp:6-31
+//   V blocks   calc_Vlmlpmp_NoQuad_ContGrid HvCalc/NoQuadOnTheFly/ContinuousAngularGrid/linRotCartSphHvContGridRoutines.cpp:7-152
+//              calc_Vlmlpmp_NoQuad       HvCalc/NoQuadOnTheFly/linRotCartSphHvFullVPrepRoutines.cpp:7-227
+//              calcSym                   HvCalc/NoQuadOnTheFly/linRotCartSphHvFullVPrepRoutines.cpp:530-573
+//   Hv         Tv_5D_oneCompositeIndex   HvCalc/linRotCartSphHvRoutines.cpp:1807-1969
+//              Vv_5D_oneCompositeIndex_NoQuad HvCalc/NoQuadOnTheFly/linRotCartSphHvFullVPrepRoutines.cpp:675-734
+//              Hv_5D_oneCompositeIndex_NoQuad / Hv_linRotCartSph_NoQuad  same file :736-822
+//   Lanczos    loop 1                    headLoop/LanczosCode/lanczosEigenValuesVectors.cpp:170-242
+//              lancbis                   headLoop/LanczosCode/supportingRoutines/lancbis.cpp:5-105 (tail in cw_tail.cpp)
+//              lanczosvectors + loop 2   headLoop/LanczosCode/lanczosEigenValuesVectors.cpp:329-469, 509-561
+//
+// Arithmetic is evaluated in the same order as the reference so that, with
+// the same inputs, results agree to the last bit or nearly so (the reference
+// is compiled with -O3 and OpenMP; this file with -ffp-contract=off).
+// Reference paths here are relative to Hv-calculators/linRotor/cartSphBasis/
+// unless they start with headLoop/.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cstdint>
+#include <cfloat>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+#include <chrono>
+#include <omp.h>
+
+extern "C" {
+void bisec_(double*, double*, double*, int*, double*, int*, double*, int*, double*, double*, int*);
+void isoev_(double*, int*, int*);
+void inverr_(double*, double*, double*, double*, double*, int*, double*, int*, double*, int*);
+void trivec_(double*, double*, double*, double*, double*, int*, double*, int*, double*, double*);
+}
+
+namespace {
+
+// headLoop/InterfaceCode/lanczosUnits.h:5-14
+const double kPI = 3.141592653589793;
+const double kK = 138.9354846111096;
+const double kHBAR = 0.0635077857002;
+const double kNmPerAng = 0.1;
+// potentialCalc/Alavi/AlaviGeneric/Alavi_Parameters.h:5-10
+const double kQ_H2_H = 0.4932, kQ_H2_CM = -0.9864, kH2_H1_Z = 0.03707;
+// potentialCalc/Alavi/SPCE/SPCE_AH2_EngRoutines.h:17-38
+const double kQ_H_SPCE = 0.4238, kQ_O_SPCE = -0.8476;
+const double kO_SPCE[3] = {0.0, 0.0, 0.006461408220};
+const double kH1_SPCE[3] = {-8.164965810E-2, 0.0, -0.05127361870};
+const double kH2_SPCE[3] = {8.164965810E-2, 0.0, -0.05127361870};
+const double kA_LJ = 1.364e-06, kB_LJ = 1.533e-3;
+
+std::string g_err;
+
+struct HvInput {
+  int nx, ny, nz, l_max, theta_points, phi_points, pnx, pny, pnz;
+  double x_max, y_max, z_max, px_max, py_max, pz_max;
+  double total_mass, rot_const, ceiling;
+  std::string geometry, title, quad_study, sym;
+};
+
+bool read_hv_input(const char* path, HvInput* h) {
+  std::ifstream f(path);
+  if (!f.is_open()) { g_err = std::string("cannot open HvInputFile ") + path; return false; }
+  std::string line, junk;
+  std::getline(f, line);
+  std::getline(f, line);
+  f >> junk >> h->nx >> junk >> h->x_max >> junk >> h->ny >> junk >> h->y_max >> junk >> h->nz >> junk >>
+      h->z_max >> junk >> h->l_max >> junk >> h->theta_points >> junk >> h->phi_points >> junk >> h->pnx >>
+      junk >> h->px_max >> junk >> h->pny >> junk >> h->py_max >> junk >> h->pnz >> junk >> h->pz_max >>
+      junk >> h->total_mass >> junk >> h->rot_const >> junk >> h->geometry >> junk >> h->title >> junk >>
+      h->ceiling >> junk >> h->quad_study >> junk >> h->sym;
+  if (!f) { g_err = "truncated HvInputFile"; return false; }
+  return true;
+}
+
+struct Cage {
+  std::vector<double> pos;   // [atom][3] nm
+  std::vector<double> q;     // charge
+  std::vector<int> is_o;     // LJ site
+};
+
+// getSPCEatoms: rotate the SPC/E body frame with the ZY'Z'' Euler angles and
+// translate by the centre of mass (Angstrom -> nm).
+bool read_cage(const std::string& path, Cage* c) {
+  std::ifstream f(path);
+  if (!f.is_open()) { g_err = "cannot open geometry " + path; return false; }
+  int nmol;
+  std::string line;
+  f >> nmol;
+  std::getline(f, line);
+  std::getline(f, line);
+  for (int i = 0; i < nmol; ++i) {
+    std::string name;
+    double cm[3], ea[3];
+    f >> name >> cm[0] >> ea[0] >> cm[1] >> ea[1] >> cm[2] >> ea[2];
+    if (!f) { g_err = "truncated geometry file"; return false; }
+    double cp = cos(ea[0]), sp = sin(ea[0]), ct = cos(ea[1]), st = sin(ea[1]), cx = cos(ea[2]), sx = sin(ea[2]);
+    double R[3][3] = {{(cp * ct * cx) - (sp * sx), (-1 * cp * ct * sx) - (sp * cx), cp * st},
+                      {(sp * ct * cx) + (cp * sx), (-1 * sp * ct * sx) + (cp * cx), sp * st},
+                      {-1 * st * cx, st * sx, ct}};
+    const double* local[3] = {kO_SPCE, kH1_SPCE, kH2_SPCE};
+    const double qs[3] = {kQ_O_SPCE, kQ_H_SPCE, kQ_H_SPCE};
+    for (int a = 0; a < 3; ++a) {
+      for (int r = 0; r < 3; ++r) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s += R[r][k] * local[a][k];
+        c->pos.push_back(s + kNmPerAng * cm[r]);
+      }
+      c->q.push_back(qs[a]);
+      c->is_o.push_back(a == 0);
+    }
+  }
+  return true;
+}
+
+inline double coulomb_sum(const double* p, double qsite, const Cage& c) {
+  double e = 0;
+  size_t na = c.q.size();
+  for (size_t i = 0; i < na; ++i) {
+    double d0 = c.pos[3 * i] - p[0], d1 = c.pos[3 * i + 1] - p[1], d2 = c.pos[3 * i + 2] - p[2];
+    double s = 0.;
+    s += d0 * d0;
+    s += d1 * d1;
+    s += d2 * d2;
+    e += kK * qsite * c.q[i] / sqrt(s);
+  }
+  return e;
+}
+
+inline double lj_sum(const double* p, const Cage& c) {
+  double e = 0;
+  size_t na = c.q.size();
+  for (size_t i = 0; i < na; ++i) {
+    if (!c.is_o[i]) continue;
+    double d0 = c.pos[3 * i] - p[0], d1 = c.pos[3 * i + 1] - p[1], d2 = c.pos[3 * i + 2] - p[2];
+    double s = 0.;
+    s += d0 * d0;
+    s += d1 * d1;
+    s += d2 * d2;
+    double r = sqrt(s);
+    e += (kA_LJ / pow(r, 12)) - (kB_LJ / pow(r, 6));
+  }
+  return e;
+}
+
+double factorial(int n) {
+  double f = 1.0;
+  for (int i = 2; i <= n; ++i) f *= double(i);
+  return f;
+}
+
+struct Model {
+  HvInput in;
+  int potential_kind = 0;  // 0 Alavi SPC/E continuous grid, 1 IsoHarmOsc, 2 synthetic blocks
+  double iso_factor = 0, iso_ceil = 0;
+  int nn = 0;              // (l_max+1)^2
+  std::vector<int> ql, qm; // n -> l, m
+  std::vector<double> xgrid, ygrid, zgrid, Tx, Ty, Tz, rot, sym;
+  std::vector<double> gl_x, gl_w, gc_x, gc_w, theta, phi, phi2;
+  // tesseral factors: L[n][a], S1[m+lmax][b] (phi), S2 (2pi - phi)
+  std::vector<double> L, S1, S2;
+  std::vector<double> V1, V2;  // [(i*ny+j)*nz+k][a][b]
+  std::vector<double> Vb;      // [(i*ny+j)*nz+k][n][n']
+  Cage cage;
+};
+
+void cart_kin_grid(double xmax, int n, double mass, std::vector<double>* T, std::vector<double>* g) {
+  double dx = xmax / double(n - 1);
+  T->assign((size_t)n * n, 0.0);
+  g->assign(n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double t = (kHBAR * kHBAR) / (2.0 * mass * dx * dx) * pow(-1.0, (i + 1) - (j + 1));
+      if (i == j) t *= (kPI * kPI) / 3.0;
+      else t *= 2.0 / double(((i + 1) - (j + 1)) * ((i + 1) - (j + 1)));
+      (*T)[(size_t)i * n + j] = t;
+    }
+  for (int i = 0; i < n; ++i) (*g)[i] = double(i) * dx - xmax / 2.0;
+}
+
+void gauleg(double x1, double x2, double* x, double* w, int n) {
+  int m = (n + 1) / 2;
+  double xm = 0.5 * (x2 + x1), xl = 0.5 * (x2 - x1);
+  for (int i = 1; i <= m; i++) {
+    double z = cos(M_PI * ((double)i - 0.25) / ((double)n + 0.5)), z1, pp, p1, p2, p3;
+    do {
+      p1 = 1.0;
+      p2 = 0.0;
+      for (int j = 1; j <= n; j++) {
+        p3 = p2;
+        p2 = p1;
+        p1 = ((2.0 * (double)j - 1.0) * z * p2 - ((double)j - 1.0) * p3) / (double)j;
+      }
+      pp = (double)n * (z * p1 - p2) / (z * z - 1.0);
+      z1 = z;
+      z = z1 - p1 / pp;
+    } while (fabs(z - z1) > DBL_EPSILON);
+    x[i - 1] = xm - xl * z;
+    x[n - i] = xm + xl * z;
+    w[i - 1] = 2.0 * xl / ((1.0 - z * z) * pp * pp);
+    w[n - i] = w[i - 1];
+  }
+}
+
+// normalised associated Legendre values for every n at cos(theta) = x
+void norm_assoc_legendre(const Model& M, double x, double* out) {
+  int lmax = M.in.l_max;
+  std::vector<double> P((size_t)(lmax + 1) * (lmax + 1), 0.0);
+  auto at = [&](int l, int m) -> double& { return P[(size_t)l * (lmax + 1) + m]; };
+  double rf = sqrt(1.0 - x * x);
+  at(0, 0) = 1.0;
+  for (int l = 1; l <= lmax; l++) at(l, l) = (2.0 * double(l) - 1.0) * at(l - 1, l - 1) * rf;
+  for (int m = 0; m <= lmax - 1; m++)
+    for (int l = m; l <= lmax - 1; l++) {
+      double ld = l, md = m;
+      double prev = ((l - 1) < m) ? 0.0 : at(l - 1, m);
+      at(l + 1, m) = (((2.0 * ld + 1.0) * x * at(l, m)) - ((ld + md) * prev)) / (ld - md + 1.0);
+    }
+  for (int l = 0; l <= lmax; l++) {
+    double phase = 1.0;
+    for (int m = 0; m <= l; m++) {
+      double nf = factorial(l - m) * (2.0 * double(l) + 1.0) / (2.0 * factorial(l + m));
+      at(l, m) *= phase * sqrt(nf);
+      phase *= -1.0;
+    }
+  }
+  for (int n = 0; n < M.nn; ++n) out[n] = at(M.ql[n], std::abs(M.qm[n]));
+}
+
+double trig_term(int m, double phi) {
+  double s = 1.0 / sqrt(kPI);
+  if (m == 0) return s / sqrt(2.0);
+  if (m > 0) return s * cos(double(m) * phi);
+  return s * sin(double(-m) * phi);
+}
+
+void build_tables(Model& M) {
+  HvInput& in = M.in;
+  cart_kin_grid(in.x_max, in.nx, in.total_mass, &M.Tx, &M.xgrid);
+  cart_kin_grid(in.y_max, in.ny, in.total_mass, &M.Ty, &M.ygrid);
+  cart_kin_grid(in.z_max, in.nz, in.total_mass, &M.Tz, &M.zgrid);
+  int lmax = in.l_max;
+  M.nn = (lmax + 1) * (lmax + 1);
+  for (int m = -lmax; m <= lmax; m++)
+    for (int l = std::abs(m); l <= lmax; l++) { M.ql.push_back(l); M.qm.push_back(m); }
+  M.rot.resize(M.nn);
+  for (int n = 0; n < M.nn; ++n) { double l = M.ql[n]; M.rot[n] = in.rot_const * l * (l + 1.0); }
+  M.sym.resize(M.nn);
+  for (int n = 0; n < M.nn; ++n) {
+    int l = M.ql[n];
+    if (in.sym == "All") M.sym[n] = 1.0;
+    else if (in.sym == "Even") M.sym[n] = (l % 2 == 0) ? 1.0 : 0.0;
+    else M.sym[n] = (l % 2 == 1) ? 1.0 : 0.0;
+  }
+  int na = in.theta_points, nb = in.phi_points;
+  M.gl_x.resize(na); M.gl_w.resize(na);
+  gauleg(-1.0, 1.0, M.gl_x.data(), M.gl_w.data(), na);
+  M.gc_x.resize(nb); M.gc_w.resize(nb);
+  for (int i = 0; i < nb; i++) {
+    M.gc_x[i] = cos(kPI * (2.0 * double(i + 1) - 1.0) / (2.0 * double(nb)));
+    M.gc_w[i] = kPI / double(nb);
+  }
+  M.theta.resize(na); M.phi.resize(nb); M.phi2.resize(nb);
+  for (int a = 0; a < na; a++) M.theta[a] = acos(M.gl_x[a]);
+  for (int b = 0; b < nb; b++) { M.phi[b] = acos(M.gc_x[b]); M.phi2[b] = 2 * kPI - acos(M.gc_x[b]); }
+  M.L.assign((size_t)M.nn * na, 0.0);
+  std::vector<double> tmp(M.nn);
+  for (int a = 0; a < na; a++) {
+    norm_assoc_legendre(M, M.gl_x[a], tmp.data());
+    for (int n = 0; n < M.nn; ++n) M.L[(size_t)n * na + a] = tmp[n];
+  }
+  int nm = 2 * lmax + 1;
+  M.S1.assign((size_t)nm * nb, 0.0);
+  M.S2.assign((size_t)nm * nb, 0.0);
+  for (int b = 0; b < nb; b++)
+    for (int m = -lmax; m <= lmax; m++) {
+      M.S1[(size_t)(m + lmax) * nb + b] = trig_term(m, acos(M.gc_x[b]));
+      M.S2[(size_t)(m + lmax) * nb + b] = trig_term(m, 2.0 * kPI - acos(M.gc_x[b]));
+    }
+}
+
+void build_potential_alavi(Model& M, int nthreads) {
+  HvInput& in = M.in;
+  int ni = in.nx, nj = in.ny, nk = in.nz, na = in.theta_points, nb = in.phi_points;
+  size_t np = (size_t)ni * nj * nk;
+  M.V1.assign(np * na * nb, 0.0);
+  M.V2.assign(np * na * nb, 0.0);
+  std::vector<double> cmpot(np);
+  std::vector<double> h1((size_t)na * nb * 3), h2((size_t)na * nb * 3);
+  for (int a = 0; a < na; a++)
+    for (int b = 0; b < nb; b++) {
+      size_t o = ((size_t)a * nb + b) * 3;
+      h1[o] = kH2_H1_Z * sin(M.theta[a]) * M.gc_x[b];
+      h1[o + 1] = kH2_H1_Z * sin(M.theta[a]) * sin(M.phi[b]);
+      h1[o + 2] = kH2_H1_Z * M.gl_x[a];
+      h2[o] = h1[o];
+      h2[o + 1] = -1.0 * h1[o + 1];
+      h2[o + 2] = h1[o + 2];
+    }
+  double ceil_v = in.ceiling;
+#pragma omp parallel for schedule(guided) num_threads(nthreads)
+  for (long p = 0; p < (long)np; ++p) {
+    int i = p / ((size_t)nj * nk), j = (p / nk) % nj, k = p % nk;
+    double g[3] = {M.xgrid[i], M.ygrid[j], M.zgrid[k]};
+    double c = coulomb_sum(g, kQ_H2_CM, M.cage);
+    c += lj_sum(g, M.cage);
+    cmpot[p] = c;
+  }
+#pragma omp parallel for schedule(guided) collapse(3) num_threads(nthreads)
+  for (long p = 0; p < (long)np; ++p)
+    for (int a = 0; a < na; a++)
+      for (int b = 0; b < nb; b++) {
+        int i = p / ((size_t)nj * nk), j = (p / nk) % nj, k = p % nk;
+        double g[3] = {M.xgrid[i], M.ygrid[j], M.zgrid[k]};
+        for (int half = 0; half < 2; ++half) {
+          const double* h = (half ? h2.data() : h1.data()) + ((size_t)a * nb + b) * 3;
+          double p1[3] = {g[0] + h[0], g[1] + h[1], g[2] + h[2]};
+          double p2[3] = {g[0] - h[0], g[1] - h[1], g[2] - h[2]};
+          double v = coulomb_sum(p1, kQ_H2_H, M.cage);
+          v += coulomb_sum(p2, kQ_H2_H, M.cage);
+          v += cmpot[p];
+          if (v >= ceil_v) v = ceil_v;
+          (half ? M.V2 : M.V1)[((size_t)p * na + a) * nb + b] = v;
+        }
+      }
+}
+
+// calc_Vlmlpmp_NoQuad with IsoHarmOscEng: V = 0.5 m w^2 |r|^2, clipped first by
+// the oscillator's own ceiling (|V| > |c| -> c) and then by the HvInputFile
+// ceiling (V >= c -> c).
+void build_potential_iso(Model& M) {
+  HvInput& in = M.in;
+  int ni = in.nx, nj = in.ny, nk = in.nz, na = in.theta_points, nb = in.phi_points;
+  size_t np = (size_t)ni * nj * nk;
+  M.V1.assign(np * na * nb, 0.0);
+  M.V2.assign(np * na * nb, 0.0);
+  for (int i = 0; i < ni; ++i)
+    for (int j = 0; j < nj; ++j)
+      for (int k = 0; k < nk; ++k) {
+        double x = M.xgrid[i], y = M.ygrid[j], z = M.zgrid[k];
+        double d2 = 0.;
+        d2 += x * x;
+        d2 += y * y;
+        d2 += z * z;
+        double v = M.iso_factor * d2;
+        if (fabs(v) > fabs(M.iso_ceil)) v = M.iso_ceil;
+        if (v >= in.ceiling) v = in.ceiling;
+        size_t p = ((size_t)i * nj + j) * nk + k;
+        for (int a = 0; a < na; ++a)
+          for (int b = 0; b < nb; ++b) {
+            M.V1[(p * na + a) * nb + b] = v;
+            M.V2[(p * na + a) * nb + b] = v;
+          }
+      }
+}
+
+void build_vblocks(Model& M, int nthreads) {
+  HvInput& in = M.in;
+  int ni = in.nx, nj = in.ny, nk = in.nz, na = in.theta_points, nb = in.phi_points, nn = M.nn;
+  int lmax = in.l_max;
+  size_t np = (size_t)ni * nj * nk;
+  std::vector<double> hf((size_t)nn * nn * na * nb), hf2((size_t)nn * nn * na * nb);
+  for (int n = 0; n < nn; n++)
+    for (int q = 0; q < nn; q++)
+      for (int a = 0; a < na; a++)
+        for (int b = 0; b < nb; b++) {
+          size_t o = (((size_t)n * nn + q) * na + a) * nb + b;
+          int m = M.qm[n], mp = M.qm[q];
+          hf[o] = M.gl_w[a] * M.gc_w[b] * M.L[(size_t)n * na + a] * M.S1[(size_t)(m + lmax) * nb + b] *
+                  M.L[(size_t)q * na + a] * M.S1[(size_t)(mp + lmax) * nb + b];
+          hf2[o] = M.gl_w[a] * M.gc_w[b] * M.L[(size_t)n * na + a] * M.S2[(size_t)(m + lmax) * nb + b] *
+                   M.L[(size_t)q * na + a] * M.S2[(size_t)(mp + lmax) * nb + b];
+        }
+  M.Vb.assign(np * nn * nn, 0.0);
+#pragma omp parallel for schedule(guided) collapse(3) num_threads(nthreads)
+  for (long p = 0; p < (long)np; ++p)
+    for (int n = 0; n < nn; n++)
+      for (int q = 0; q < nn; q++) {
+        double s = 0.0;
+        const double* h1 = &hf[((size_t)n * nn + q) * na * nb];
+        const double* h2 = &hf2[((size_t)n * nn + q) * na * nb];
+        const double* v1 = &M.V1[(size_t)p * na * nb];
+        const double* v2 = &M.V2[(size_t)p * na * nb];
+        for (int ab = 0; ab < na * nb; ++ab) s += h1[ab] * v1[ab] + h2[ab] * v2[ab];
+        M.Vb[((size_t)p * nn + n) * nn + q] = s;
+      }
+}
+
+// uec += S (T + V) vec in the reference layout ((n*nz+k)*ny+j)*nx+i.
+void hv(const Model& M, const double* v, double* uec, int nthreads) {
+  const HvInput& in = M.in;
+  const int ni = in.nx, nj = in.ny, nk = in.nz, nn = M.nn;
+  const size_t N = (size_t)ni * nj * nk, D = N * nn;
+  std::vector<double> t(D);
+  // Kinetic: each axis is a serial dense line contraction (Mv_5D, reference
+  // loops with the OpenMP pragmas commented out), summed as
+  // rot + (Tz + (Ty + Tx)).
+  for (int n = 0; n < nn; n++)
+    for (int k = 0; k < nk; k++)
+      for (int j = 0; j < nj; j++)
+        for (int i = 0; i < ni; i++) {
+          const size_t base = ((size_t)n * nk + k) * nj;
+          double tx = 0.0, ty = 0.0, tz = 0.0;
+          for (int q = 0; q < ni; q++) tx += M.Tx[(size_t)i * ni + q] * v[(base + j) * ni + q];
+          for (int q = 0; q < nj; q++) ty += M.Ty[(size_t)j * nj + q] * v[(base + q) * ni + i];
+          for (int q = 0; q < nk; q++) tz += M.Tz[(size_t)k * nk + q] * v[((((size_t)n * nk + q) * nj) + j) * ni + i];
+          const size_t p = (base + j) * ni + i;
+          t[p] = M.rot[n] * v[p] + (tz + (ty + tx));
+        }
+  // Potential: per grid point an nn x nn block times the local coefficients.
+#pragma omp parallel for schedule(guided) collapse(3) num_threads(nthreads)
+  for (int i = 0; i < ni; i++)
+    for (int j = 0; j < nj; j++)
+      for (int k = 0; k < nk; k++) {
+        const size_t pb = ((size_t)i * nj + j) * nk + k;
+        const size_t pv = ((size_t)k * nj + j) * ni + i;
+        for (int n = 0; n < nn; n++) {
+          double s = 0.0;
+          const double* blk = &M.Vb[(pb * nn + n) * nn];
+          for (int q = 0; q < nn; q++) s += blk[q] * v[(size_t)q * N + pv];
+          const size_t o = (size_t)n * N + pv;
+          double h = t[o] + s;
+          h *= M.sym[n];
+          uec[o] += h;
+        }
+      }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* orc_last_error() { return g_err.c_str(); }
+
+// calculator: "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE" or
+// "linRotCartSph_NoQuad_IsoHarmOsc".  extra_input: IsoHarmOsc parameter file.
+void* orc_create(const char* calculator, const char* hv_input, const char* extra_input, int nthreads) {
+  Model* M = new Model();
+  if (!read_hv_input(hv_input, &M->in)) { delete M; return nullptr; }
+  std::string calc(calculator);
+  build_tables(*M);
+  if (calc == "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE") {
+    if (!read_cage(M->in.geometry, &M->cage)) { delete M; return nullptr; }
+    M->potential_kind = 0;
+    build_potential_alavi(*M, nthreads);
+  } else if (calc == "linRotCartSph_NoQuad_IsoHarmOsc") {
+    std::ifstream f(extra_input ? extra_input : "");
+    if (!f.is_open()) { g_err = "cannot open IsoHarmOsc input"; delete M; return nullptr; }
+    std::string line, junk;
+    double mass, freq, ceil_v;
+    std::getline(f, line);
+    std::getline(f, line);
+    f >> junk >> mass >> junk >> freq >> junk >> ceil_v;
+    M->iso_factor = 0.5 * mass * freq * freq;
+    M->iso_ceil = ceil_v;
+    M->potential_kind = 1;
+    build_potential_iso(*M);
+  } else {
+    g_err = "unknown calculator " + calc;
+    delete M;
+    return nullptr;
+  }
+  build_vblocks(*M, nthreads);
+  return M;
+}
+
+// Timing-only model at production sizes: the Hv cost does not depend on the
+// potential values, so the blocks are filled with a cheap deterministic
+// symmetric pattern instead of running the potential and block assembly.
+void* orc_create_synthetic(int nx, int ny, int nz, int l_max, double x_max, double mass, double rot_const,
+                           const char* sym) {
+  Model* M = new Model();
+  HvInput& in = M->in;
+  in.nx = nx; in.ny = ny; in.nz = nz; in.l_max = l_max;
+  in.x_max = in.y_max = in.z_max = x_max;
+  in.theta_points = 2; in.phi_points = 2;
+  in.total_mass = mass; in.rot_const = rot_const; in.sym = sym; in.ceiling = 18.0;
+  build_tables(*M);
+  M->potential_kind = 2;
+  size_t np = (size_t)nx * ny * nz, nn = M->nn;
+  M->Vb.assign(np * nn * nn, 0.0);
+#pragma omp parallel for
+  for (long p = 0; p < (long)np; ++p)
+    for (size_t n = 0; n < nn; ++n)
+      for (size_t q = 0; q < nn; ++q)
+        M->Vb[((size_t)p * nn + n) * nn + q] = 1e-3 * double((p + n + q) % 17) - 8e-3;
+  return M;
+}
+
+void orc_destroy(void* h) { delete static_cast<Model*>(h); }
+
+long orc_basis_size(void* h) {
+  Model* M = static_cast<Model*>(h);
+  return (long)M->in.nx * M->in.ny * M->in.nz * M->nn;
+}
+int orc_nn(void* h) { return static_cast<Model*>(h)->nn; }
+
+void orc_hv(void* h, const double* vec, double* uec, int nthreads) {
+  hv(*static_cast<Model*>(h), vec, uec, nthreads);
+}
+
+// Potential grid halves V(x,y,z,theta_a,phi_b) and V(..,2pi-phi_b), point index
+// (i*ny+j)*nz+k slowest.
+long orc_vgrid_size(void* h) { Model* M = static_cast<Model*>(h); return (long)M->V1.size(); }
+void orc_vgrid(void* h, double* v1, double* v2) {
+  Model* M = static_cast<Model*>(h);
+  std::memcpy(v1, M->V1.data(), M->V1.size() * sizeof(double));
+  std::memcpy(v2, M->V2.data(), M->V2.size() * sizeof(double));
+}
+long orc_vblock_size(void* h) { return (long)static_cast<Model*>(h)->Vb.size(); }
+void orc_vblocks(void* h, double* out) {
+  Model* M = static_cast<Model*>(h);
+  std::memcpy(out, M->Vb.data(), M->Vb.size() * sizeof(double));
+}
+// Tables for unit tests: kinetic matrix of one axis, GL/GC nodes, tesseral L.
+void orc_tables(void* h, double* Tx, double* gl_x, double* gl_w, double* gc_x, double* L, double* S1, double* S2) {
+  Model* M = static_cast<Model*>(h);
+  std::memcpy(Tx, M->Tx.data(), M->Tx.size() * sizeof(double));
+  std::memcpy(gl_x, M->gl_x.data(), M->gl_x.size() * sizeof(double));
+  std::memcpy(gl_w, M->gl_w.data(), M->gl_w.size() * sizeof(double));
+  std::memcpy(gc_x, M->gc_x.data(), M->gc_x.size() * sizeof(double));
+  std::memcpy(L, M->L.data(), M->L.size() * sizeof(double));
+  std::memcpy(S1, M->S1.data(), M->S1.size() * sizeof(double));
+  std::memcpy(S2, M->S2.data(), M->S2.size() * sizeof(double));
+}
+
+// Lanczos loop 1 of the reference driver.  v0 == NULL selects the uniform
+// start vector 1/sqrt(D).  alpha[niter], beta[niter+1], beta2[niter+1] (index
+// 0 unused, zero).  Returns seconds spent.
+double orc_lanczos(void* h, int niter, const double* v0, double* alpha, double* beta, double* beta2, int nthreads) {
+  Model* M = static_cast<Model*>(h);
+  const long D = orc_basis_size(h);
+  std::vector<double> r(D, 0.0), v(D), u(D, 0.0);
+  for (long i = 0; i < D; ++i) v[i] = v0 ? v0[i] : 1. / sqrt((double)D);
+  beta[0] = 0.0;
+  beta2[0] = 0.0;
+  auto t0 = std::chrono::steady_clock::now();
+  for (int j = 1; j <= niter; ++j) {
+    for (long i = 0; i < D; ++i) u[i] = 0.;
+    hv(*M, v.data(), u.data(), nthreads);
+    for (long i = 0; i < D; ++i) r[i] += u[i];
+    double a = 0.;
+    for (long i = 0; i < D; ++i) a += v[i] * r[i];
+    alpha[j - 1] = a;
+    for (long i = 0; i < D; ++i) r[i] -= (a * v[i]);
+    double b2 = 0.;
+    for (long i = 0; i < D; ++i) b2 += r[i] * r[i];
+    beta2[j] = b2;
+    double b = sqrt(b2);
+    beta[j] = b;
+    for (long i = 0; i < D; ++i) r[i] = (1. / b) * r[i];
+    for (long i = 0; i < D; ++i) v[i] = (-b) * v[i];
+    for (long i = 0; i < D; ++i) { u[i] = v[i]; v[i] = r[i]; r[i] = u[i]; }
+  }
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// lancbis (lancbis.cpp:5-105): good eigenvalues in (emin, emax] with
+// inverse-iteration error estimates; returns ngood.  eval/err need niter slots.
+int orc_lancbis(int niter, const double* alpha, const double* beta, const double* beta2, double emin, double emax,
+                double* eval, double* err) {
+  std::vector<double> la(alpha, alpha + niter), lb(beta, beta + niter + 1), lb2(beta2, beta2 + niter + 1);
+  std::vector<double> ql(niter, 0.0), wrk2(2 * niter, 0.0);
+  std::vector<int> mp2(niter, 0);
+  int ndis = 0, nit = niter;
+  bisec_(la.data(), lb.data(), lb2.data(), &nit, ql.data(), mp2.data(), wrk2.data(), &nit, &emin, &emax, &ndis);
+  std::vector<double> vs(ql.begin(), ql.begin() + ndis);
+  std::vector<int> mp(mp2.begin(), mp2.begin() + ndis);
+  if (ndis > 1) isoev_(vs.data(), mp.data(), &ndis);
+  std::vector<double> w1(niter, 0.0), w2(niter + 1, 0.0), w3(niter, 0.0), e(niter > ndis ? niter : ndis, 0.0);
+  if (ndis > 0) inverr_(la.data(), lb.data(), w1.data(), w2.data(), w3.data(), &nit, vs.data(), mp.data(), e.data(), &ndis);
+  int ii = 0;
+  for (int i = 0; i < ndis; ++i)
+    if (mp[i] != 0) { eval[ii] = vs[i]; err[ii] = e[i]; ++ii; }
+  return ii;
+}
+
+// lanczosvectors (lanczosEigenValuesVectors.cpp:509-561): Tm eigenvectors,
+// column-major evtr[niter x ngood].
+void orc_trivec(int niter, const double* alpha, const double* beta, const double* beta2, const double* eval, int ngood,
+                double* evtr) {
+  std::vector<double> la(alpha, alpha + niter), lb(niter + 1), lb2(niter + 1), le(eval, eval + ngood);
+  lb[0] = 0.;
+  lb2[0] = 0.;
+  for (int j = 1; j <= niter; ++j) { lb[j] = beta[j]; lb2[j] = beta2[j]; }
+  std::vector<double> w1(niter, 0.0), w2(niter, 0.0), mamin(ngood, 0.0);
+  std::vector<double> ev((size_t)niter * ngood, 0.0);
+  int nit = niter, ng = ngood;
+  trivec_(la.data(), lb.data(), lb2.data(), w1.data(), w2.data(), &nit, le.data(), &ng, ev.data(), mamin.data());
+  std::memcpy(evtr, ev.data(), ev.size() * sizeof(double));
+}
+
+// Lanczos loop 2 with Ritz accumulation (lanczosEigenValuesVectors.cpp:371-469):
+// ritz[n*D + row] = sum_j evtr[j,n] v_j[row], skipping terms once the
+// cumulative squared coefficient reaches 1 - 1e-16.
+void orc_ritz(void* h, int niter, const double* evtr, int ngood, double* ritz, int nthreads) {
+  Model* M = static_cast<Model*>(h);
+  const long D = orc_basis_size(h);
+  std::vector<double> r(D, 0.0), v(D), u(D, 0.0), cum(ngood, 0.0);
+  for (long i = 0; i < D; ++i) v[i] = 1. / sqrt((double)D);
+  for (long i = 0; i < D * (long)ngood; ++i) ritz[i] = 0.;
+  for (int j = 1; j <= niter; ++j) {
+    for (int n = 0; n < ngood; ++n) {
+      double c = evtr[(size_t)n * niter + (j - 1)];
+      cum[n] += pow(c, 2.);
+      for (long row = 0; row < D; ++row) {
+        double coeff = c * v[row];
+        if (cum[n] < (1. - 1.e-16)) ritz[row + D * n] += coeff;
+      }
+    }
+    for (long i = 0; i < D; ++i) u[i] = 0.;
+    hv(*M, v.data(), u.data(), nthreads);
+    for (long i = 0; i < D; ++i) r[i] += u[i];
+    double a = 0.;
+    for (long i = 0; i < D; ++i) a += v[i] * r[i];
+    for (long i = 0; i < D; ++i) r[i] -= (a * v[i]);
+    double b2 = 0.;
+    for (long i = 0; i < D; ++i) b2 += r[i] * r[i];
+    double b = sqrt(b2);
+    for (long i = 0; i < D; ++i) r[i] = (1. / b) * r[i];
+    for (long i = 0; i < D; ++i) v[i] = (-b) * v[i];
+    for (long i = 0; i < D; ++i) { u[i] = v[i]; v[i] = r[i]; r[i] = u[i]; }
+  }
+}
+
+}  // extern "C"
