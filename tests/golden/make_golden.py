@@ -1,0 +1,141 @@
+"""Generate the committed golden fixtures from the reference itself.
+
+Run in a container that has the reference tree (default /root/reference) and
+has built it with `make -C oracle ref`.  Every fixture below comes from the
+UNMODIFIED reference (oracle/_ref/libref_hv.so for single Hv applications,
+oracle/_ref/ref_lanczos for whole Lanczos runs) or is copied verbatim from the
+reference's own stored runs (Compilation/SmallBasisTest2_*), so that the tests
+can pin the oracle restatement and the GPU path where the reference tree is
+absent.
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+"""
+import ctypes as C
+import glob
+import importlib.util
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF_LIB = os.path.join(REPO, "oracle", "_ref", "libref_hv.so")
+REF_BIN = os.path.join(REPO, "oracle", "_ref", "ref_lanczos")
+
+_spec = importlib.util.spec_from_file_location(
+    "bsl_inputs", os.path.join(REPO, "boundstate-lanczos_gb300", "inputs.py"))
+inputs = importlib.util.module_from_spec(_spec)
+_spec.loader.exec_module(inputs)
+
+CONTGRID = "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE"
+ISO = "linRotCartSph_NoQuad_IsoHarmOsc"
+
+# name: (calculator, n, x_max, l_max, theta, phi, sym, geometry, niter, hv_full, iso)
+CASES = {
+    # the stored 2013-09-03 10^3 l3 runs (inputs identical to the reference's own)
+    "cage11_n10_l3_all": (CONTGRID, 10, 0.4, 3, 10, 10, "All", "cage11.xyz", 300, True, None),
+    # odd parity (ortho) with a synthetic cage
+    "seed1_n6_l3_odd": (CONTGRID, 6, 0.08, 3, 8, 7, "Odd", "cage_seed1.xyz", 200, True, None),
+    # even parity (para) with the CPU-workload angular grid
+    "seed0_n5_l4_even": (CONTGRID, 5, 0.08, 4, 12, 12, "Even", "cage_seed0.xyz", 200, True, None),
+    # isotropic harmonic oscillator (analytic check), orientation independent
+    "iso_n20_l2_all": (ISO, 20, 0.3, 2, 4, 4, "All", "NULL", 300, True, (2.015650064, 24.1, 100.0)),
+    # the CPU workload itself: 15^3 even l<=4 12 x 24, cage seed 0, 600 iterations
+    "cpu_workload": (CONTGRID, 15, 0.08, 4, 12, 12, "Even", "cage_seed0.xyz", 600, False, None),
+}
+
+
+def ref_hv(calc, hv_path, extra):
+    lib = C.CDLL(REF_LIB)
+    lib.ref_hv_setup.restype = C.c_long
+    D = lib.ref_hv_setup(calc.encode(), hv_path.encode(), extra.encode() if extra else None)
+    P = C.POINTER(C.c_double)
+    rng = np.random.default_rng(20131903)
+    v = rng.standard_normal(D)
+    u = np.zeros(D)
+    lib.ref_hv(v.ctypes.data_as(P), u.ctypes.data_as(P))
+    return D, u
+
+
+def run_ref_lanczos(case_dir, calc, extra):
+    tmp = tempfile.mkdtemp()
+    for f in os.listdir(case_dir):
+        shutil.copy(os.path.join(case_dir, f), tmp)
+    lz = os.path.join(tmp, "lanczos_input.txt")
+    txt = open(lz).read().replace("OutputDirectoryPath= ./", "OutputDirectoryPath= %s/out_" % tmp)
+    open(lz, "w").write(txt)
+    args = [REF_BIN, "lanczos_input.txt", "hv_input.txt"] + (["iso_input.txt"] if extra else [])
+    log = subprocess.run(args, cwd=tmp, capture_output=True, text=True, check=True).stdout
+    ab = [l.split() for l in log.splitlines() if re.match(r"^\d+ \S+ \S+$", l)]
+    alpha = np.array([float(x[1]) for x in ab])
+    beta = np.array([float(x[2]) for x in ab])
+    bs = glob.glob(os.path.join(tmp, "out_*", "boundstates.txt"))[0]
+    shutil.copy(bs, os.path.join(case_dir, "ref_boundstates.txt"))
+    shutil.rmtree(tmp)
+    return alpha, beta
+
+
+def main():
+    shutil.copy(os.path.join(REF, "Compilation", "sII_smallCage11_CM_EA_ZYZ.xyz"), os.path.join(HERE, "cage11.xyz"))
+    for seed in (0, 1):
+        inputs.write_cage_xyz(os.path.join(HERE, "cage_seed%d.xyz" % seed), inputs.dodecahedral_cage(seed))
+    manifest = {}
+    for name, (calc, n, xm, lmax, th, ph, sym, geo, niter, full, iso) in CASES.items():
+        d = os.path.join(HERE, name)
+        os.makedirs(d, exist_ok=True)
+        if geo != "NULL":
+            shutil.copy(os.path.join(HERE, geo), os.path.join(d, geo))
+        if calc == CONTGRID and name.startswith("cage11"):
+            vals = inputs.hv_fields(n, xm, lmax, th, ph, geo, "SmallBasisTest2", sym, rot_const=0.7096487130193394)
+        else:
+            vals = inputs.hv_fields(n, xm, lmax, th, ph, geo, name, sym)
+        if iso:
+            vals[16] = 0.709652722117881
+            vals[19] = 100.0
+        inputs.write_hv_input(os.path.join(d, "hv_input.txt"), vals)
+        inputs.write_lanczos_input(os.path.join(d, "lanczos_input.txt"), niter, calc)
+        extra = None
+        if iso:
+            inputs.write_isoharmosc_input(os.path.join(d, "iso_input.txt"), *iso)
+            extra = "iso_input.txt"
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            D, u = ref_hv(calc, "hv_input.txt", extra)
+        finally:
+            os.chdir(cwd)
+        rec = {"calculator": calc, "basis_size": int(D), "niter": niter, "hv_seed": 20131903,
+               "hv_norm": float(np.linalg.norm(u)), "hv_sum": float(u.sum())}
+        if full:
+            np.save(os.path.join(d, "ref_hv.npy"), u)
+        else:
+            idx = np.arange(0, D, max(1, D // 4096))
+            np.savez(os.path.join(d, "ref_hv_sample.npz"), idx=idx, val=u[idx])
+        alpha, beta = run_ref_lanczos(d, calc, extra)
+        np.savez(os.path.join(d, "ref_alpha_beta.npz"), alpha=alpha, beta=beta)
+        manifest[name] = rec
+        print(name, rec)
+    # the reference's own stored 2013 runs that the final tree reproduces
+    stored = {}
+    for run in ("SmallBasisTest2_2013-09-03_18_36_00", "SmallBasisTest2_2013-09-03_19_06_47"):
+        lines = open(os.path.join(REF, "Compilation", run, "boundstates.txt")).read().split("\n")[4:]
+        vals = [[float(x) for x in l.split()[1:3]] for l in lines if l.strip()]
+        niter = int(re.search(r"numberOfIterations= (\d+)",
+                              open(os.path.join(REF, "Compilation", run,
+                                                "LanczosInputFileTobySmallBasisTest2.txt")).read()).group(1))
+        stored[run] = {"niter": niter, "levels": vals}
+    with open(os.path.join(HERE, "stored_2013_runs.json"), "w") as f:
+        json.dump(stored, f, indent=0)
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
