@@ -1,0 +1,337 @@
+"""Lanczos iterations per second on the 54^3 odd-l<=5 40x70 workload.
+
+One step = one Lanczos iteration (H v with the sinc-DVR kinetic, rotor and
+potential blocks, then the alpha/beta recurrence) over the packed odd-l block
+of the 54^3 x (l<=5) basis of H2 in a 20-water SPC/E dodecahedral cage (seed
+1), 40 Gauss-Legendre theta x 70 uniform phi nodes.  The inputs are synthetic
+(generated cage, no external data).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Default arm: the mixed-precision GPU path timed with CUDA events on the
+library's stream (value), the same metric end to end through the C ABI with
+host buffers (e2e), the FP64 GPU path, the level accuracy of the mixed path
+against the FP64 path at the same iteration count, per-kernel times and the
+roofline of the dominant kernel, and the CPU baseline (oracle restatement of
+the reference's Hv and loop on the host cores, bounded sample).
+--impl reference: only the CPU implementation, on the same workload.
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "boundstate-lanczos_gb300")
+ORACLE_LIB = os.path.join(REPO, "oracle", "_build", "liboracle.so")
+METRIC = "Lanczos iter/s at 54³·l≤5 (mixed vs FP64 GPU) at ≤1e-3 cm⁻¹ level error"
+UNIT = "iter/s"
+KJ_TO_CM = 83.5935
+
+
+def _load(name, path):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload_files(tmp):
+    inputs = _load("bsl_inputs", os.path.join(PKG, "inputs.py"))
+    cfg = inputs.CONFIG_METRIC
+    cage = os.path.join(tmp, "cage_seed%d.xyz" % cfg["cage_seed"])
+    inputs.write_cage_xyz(cage, inputs.dodecahedral_cage(cfg["cage_seed"]))
+    hv = os.path.join(tmp, "hv_input.txt")
+    inputs.write_hv_input(hv, inputs.hv_fields(cfg["n"], cfg["x_max"], cfg["l_max"], cfg["theta_points"],
+                                               cfg["phi_points"], cage, "metric_54_odd_l5", cfg["sym"]))
+    return cfg, hv
+
+
+def config_record(cfg, D=None, Df=None, precision="mixed"):
+    rec = {"workload": "H2 in SPC/E dodecahedral cage (seed %d): %d^3 sinc-DVR grid over +-0.4 A, %s l<=%d, "
+                       "%d theta x %d phi" % (cfg["cage_seed"], cfg["n"], cfg["sym"].lower(), cfg["l_max"],
+                                              cfg["theta_points"], 2 * cfg["phi_points"]),
+           "grid": cfg["n"], "l_max": cfg["l_max"], "symmetry": cfg["sym"], "theta_points": cfg["theta_points"],
+           "phi_nodes": 2 * cfg["phi_points"], "precision": precision,
+           "l2": "working set larger than L2 (potential blocks alone 145 MB FP32) - no flush needed"}
+    if D is not None:
+        rec["basis_packed"] = int(D)
+        rec["basis_reference"] = int(Df)
+    return rec
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the oracle restatement of the reference's Hv and Lanczos loop
+# (serial kinetic, OpenMP potential blocks), on the same basis sizes with
+# synthetic block values (the cost does not depend on the values).
+# --------------------------------------------------------------------------
+def cpu_baseline(cfg, budget_s=15.0):
+    if not os.path.exists(ORACLE_LIB):
+        subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "port"], check=True, capture_output=True)
+    L = C.CDLL(ORACLE_LIB)
+    L.orc_create_synthetic.restype = C.c_void_p
+    L.orc_create_synthetic.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                       C.c_char_p]
+    L.orc_basis_size.restype = C.c_long
+    L.orc_basis_size.argtypes = [C.c_void_p]
+    P = C.POINTER(C.c_double)
+    L.orc_lanczos.restype = C.c_double
+    L.orc_lanczos.argtypes = [C.c_void_p, C.c_int, P, P, P, P, C.c_int]
+    L.orc_destroy.argtypes = [C.c_void_p]
+    cores = os.cpu_count() or 1
+    h = C.c_void_p(L.orc_create_synthetic(cfg["n"], cfg["n"], cfg["n"], cfg["l_max"], cfg["x_max"], 2.01588,
+                                          0.709648713, cfg["sym"].encode()))
+    D = L.orc_basis_size(h)
+
+    def run(n):
+        a, b, b2 = np.zeros(n), np.zeros(n + 1), np.zeros(n + 1)
+        return L.orc_lanczos(h, n, None, a.ctypes.data_as(P), b.ctypes.data_as(P), b2.ctypes.data_as(P), cores)
+
+    t1 = run(1)
+    n = int(max(2, min(30, budget_s / max(t1, 1e-3))))
+    t = run(n)
+    L.orc_destroy(h)
+    return {"value": n / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d Lanczos iterations of the reference algorithm (oracle restatement: serial sinc-DVR "
+                      "kinetic, OpenMP potential blocks, serial recurrence) on the %d-function reference basis "
+                      "(%d^3 x (l_max+1)^2 with parity mask), %.1f s" % (n, D, cfg["n"], t),
+            "seconds": t, "iterations": n, "basis_reference": D}
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+        except Exception:
+            rows = []
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def stage_bytes(cfg, D, N, nn, mixed):
+    """Algorithmic bytes per launch of each stage of one Lanczos iteration."""
+    ntri = nn * (nn + 1) // 2
+    vb = ntri * N * (4 if mixed else 8)
+    return [2 * D * 8,              # kinetic x/y: read v, write u_kin
+            3 * D * 8,              # kinetic z: read v, read+write u_kin
+            vb + 4 * D * 8,         # potential apply: blocks, v, u_kin, r (read+write)
+            3 * (D + 1) * 8,        # r -= alpha v, beta^2: read v, r; write r
+            4 * (D + 1) * 8]        # v <- r/beta, r <- -beta v: read 2, write 2
+
+
+def levels_of(bsl, a, b, b2, count):
+    ev, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3)
+    return ev
+
+
+def stable_levels(bsl, a, b, b2, drop=200, tol=1e-9):
+    ev, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3)
+    n = len(a) - drop
+    ev2, _ = bsl.good_eigenvalues(a[:n], b[:n + 1], b2[:n + 1], -1.0e3, 1.0e3)
+    return np.array([e for e in ev if len(ev2) and np.min(np.abs(ev2 - e)) <= tol])
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--accuracy-iters", type=int, default=10000)
+    ap.add_argument("--fp64-steps", type=int, default=200)
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    tmp = tempfile.mkdtemp()
+    cfg, hv_path = workload_files(tmp)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(cfg, budget_s=max(5.0, args.cpu_budget))
+        line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": cb["iterations"],
+                "warmup": 1, "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (generated cage; block values synthetic)",
+                "config": config_record(cfg, precision="fp64"), "impl": "reference",
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    bsl = _load("boundstate_lanczos_gb300", os.path.join(PKG, "__init__.py"))
+    t0 = time.perf_counter()
+    h = bsl.Hamiltonian(hv_path, "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE", precision="mixed", device=local)
+    prep_s = time.perf_counter() - t0
+    D, Df, nn = h.packed_size, h.basis_size, h.nn
+    N = D // nn
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # ---- device-resident mixed path (value) ----
+    h.lanczos(max(3, args.warmup))
+    barrier()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        h.lanczos(args.steps)
+        barrier()
+        wall = time.perf_counter() - t0
+    ms_event = h.last_ms_per_iter()
+    ms_step = ms_event
+    if dist is not None:
+        t = torch.tensor([ms_step], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * 1000.0 / ms_step
+
+    # ---- per-kernel times (CUDA events around each launch on the library stream) ----
+    stage_ms = np.zeros(5)
+    names = (C.c_char_p * 5)()
+    bsl.lib().bsl_stage_times.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_void_p]
+    rc = bsl.lib().bsl_stage_times(h.handle, 200, stage_ms.ctypes.data_as(C.POINTER(C.c_double)), names)
+    stage_names = [n.decode() for n in names] if rc == 0 else []
+    sb = stage_bytes(cfg, D, N, nn, True)
+    peak, peak_src = measured_peak_hbm()
+    dom = int(np.argmax(stage_ms))
+    achieved = sb[dom] / (stage_ms[dom] * 1e-3) / 1e9
+    it_bytes = sum(sb)
+
+    # ---- end to end through the C ABI with host buffers (pinned) ----
+    vec = torch.empty(Df, dtype=torch.float64, pin_memory=True).numpy()
+    rvec = torch.empty(Df, dtype=torch.float64, pin_memory=True).numpy()
+    vec[:] = 1.0 / math.sqrt(Df)
+    rvec[:] = 0.0
+    for _ in range(3):
+        h.step_host(vec, rvec)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        h.step_host(vec, rvec)
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * args.e2e_steps / e2e_s
+
+    # ---- FP64 GPU path ----
+    h.set_precision("fp64")
+    h.lanczos(3)
+    h.lanczos(args.fp64_steps)
+    fp64_ms = h.last_ms_per_iter()
+    fp64_stage = np.zeros(5)
+    bsl.lib().bsl_stage_times(h.handle, 20, fp64_stage.ctypes.data_as(C.POINTER(C.c_double)), None)
+
+    # ---- level accuracy: mixed vs FP64 at the same iteration count ----
+    acc = {}
+    if args.accuracy_iters > 0 and rank == 0:
+        n_it = args.accuracy_iters
+        a64, b64, b264 = h.lanczos(n_it, start="normal", seed=0)
+        h.set_precision("mixed")
+        am, bm, bm2 = h.lanczos(n_it, start="normal", seed=0)
+        ref_levels = np.sort(stable_levels(bsl, a64, b64, b264))[:cfg["levels"]]
+        evm, _ = bsl.good_eigenvalues(am, bm, bm2, -1.0e3, 1.0e3)
+        dev = np.array([np.min(np.abs(evm - e)) for e in ref_levels]) * KJ_TO_CM if len(evm) else np.array([])
+        acc = {"iterations": n_it, "levels_compared": int(len(ref_levels)),
+               "max_abs_dE_cm-1": float(dev.max()) if len(dev) else None,
+               "lowest_levels_kJ_mol": [float(x) for x in ref_levels[:5]], "start": "normal seed 0"}
+    h.close()
+
+    cb = cpu_baseline(cfg, budget_s=args.cpu_budget) if rank == 0 else None
+    clocks = clk.summary()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (generated SPC/E cage, seed 1)",
+        "config": config_record(cfg, D, Df),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * Df * 8, "d2h_bytes_per_step": 2 * Df * 8,
+                "path": "bsl_lanczos_step_host: reference loop body with host (pinned) vec/rvec in the reference "
+                        "layout, H2D + Hv + recurrence + D2H per step"},
+        "roofline": {"bound": "hbm", "kernel": stage_names[dom] if stage_names else None,
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_src + " (of measured)",
+                     "algorithmic_bytes_per_launch": sb[dom], "ms_per_launch": float(stage_ms[dom])},
+        "iteration_roofline": {"bytes_per_iteration": it_bytes,
+                               "achieved_GBs": it_bytes / (ms_step * 1e-3) / 1e9 / world,
+                               "frac": it_bytes / (ms_step * 1e-3) / 1e9 / world / peak},
+        "stages_ms": dict(zip(stage_names, [float(x) for x in stage_ms])),
+        "fp64": {"value": 1000.0 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
+                 "stages_ms": [float(x) for x in fp64_stage], "speedup_mixed_vs_fp64": fp64_ms / (ms_step)},
+        "accuracy": acc,
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "clocks": clocks, "gpu_launches": 5 * args.steps, "prep_seconds": prep_s,
+        "wall_ms_per_step": 1000.0 * wall / args.steps,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

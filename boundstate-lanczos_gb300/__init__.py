@@ -1,0 +1,247 @@
+"""Python mirror of the reference's HvCalculator plugin interface over the C ABI.
+
+The reference registers an HvCalculator by name and hands its Lanczos driver
+an (HvPrep, Hv) function-pointer pair plus opaque storage
+(headLoop/InterfaceCode/interface.cpp:3-250).  `hv_interface_setup(name)`
+returns the same pair for the GB300 calculators, bound to libbsl_gb300.so
+through ctypes; `Hamiltonian` exposes the device-resident extras (the Lanczos
+loop on the GPU, packed-layout applications, Ritz vectors).
+
+The library must have been built (build.py); there is no CPU fallback: a
+missing library raises immediately.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbsl_gb300.so")
+
+OK, ERR_INPUT, ERR_CUDA, ERR_STATE, ERR_BREAKDOWN, ERR_UNSUPPORTED, ERR_NOMEM = range(7)
+SYM = {"All": 0, "Even": 1, "Odd": 2}
+POT_ALAVI_SPCE, POT_ISOHARMOSC = 0, 1
+PREC = {"fp64": 0, "mixed": 1}
+START = {"uniform": 0, "normal": 1}
+CALCULATORS = {
+    "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE": POT_ALAVI_SPCE,
+    "linRotCartSph_NoQuad_IsoHarmOsc": POT_ISOHARMOSC,
+    "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE_GB300": POT_ALAVI_SPCE,
+    "linRotCartSph_NoQuad_IsoHarmOsc_GB300": POT_ISOHARMOSC,
+}
+
+
+class BslError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("bsl error %d: %s" % (code, msg))
+        self.code = code
+
+
+class HvParams(C.Structure):
+    """Mirror of bsl_hv_params (include/bsl.h)."""
+    _fields_ = [("nx", C.c_int), ("x_max", C.c_double), ("ny", C.c_int), ("y_max", C.c_double),
+                ("nz", C.c_int), ("z_max", C.c_double), ("l_max", C.c_int), ("theta_points", C.c_int),
+                ("phi_points", C.c_int), ("pnx", C.c_int), ("px_max", C.c_double), ("pny", C.c_int),
+                ("py_max", C.c_double), ("pnz", C.c_int), ("pz_max", C.c_double), ("total_mass", C.c_double),
+                ("rotational_constant", C.c_double), ("geometry_filename", C.c_char * 1024),
+                ("simulation_title", C.c_char * 256), ("ceiling_potential", C.c_double),
+                ("quadrature_study", C.c_int), ("symmetry", C.c_int), ("potential", C.c_int),
+                ("iso_mass", C.c_double), ("iso_frequency", C.c_double), ("iso_ceiling", C.c_double),
+                ("precision", C.c_int), ("device", C.c_int)]
+
+
+_lib = None
+_P = C.POINTER(C.c_double)
+
+
+def lib():
+    """Load libbsl_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libbsl_gb300.so is not built: run boundstate-lanczos_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+    L.bsl_last_error.restype = C.c_char_p
+    L.bsl_basis_size.restype = C.c_longlong
+    L.bsl_packed_size.restype = C.c_longlong
+    L.bsl_vgrid_size.restype = C.c_longlong
+    L.bsl_vblock_size.restype = C.c_longlong
+    L.bsl_stream.restype = C.c_void_p
+    L.bsl_hv_prep.argtypes = [C.POINTER(HvParams), C.POINTER(C.c_void_p)]
+    for name in ("bsl_basis_size", "bsl_packed_size", "bsl_packed_nn", "bsl_vgrid_size", "bsl_vblock_size",
+                 "bsl_stream", "bsl_destroy"):
+        getattr(L, name).argtypes = [C.c_void_p]
+    L.bsl_hv_apply.argtypes = [C.c_void_p, _P, _P]
+    L.bsl_hv_apply_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.bsl_set_precision.argtypes = [C.c_void_p, C.c_int]
+    L.bsl_lanczos_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong, _P, _P, _P]
+    L.bsl_lanczos_step_host.argtypes = [C.c_void_p, _P, _P, _P, _P, _P]
+    L.bsl_good_eigenvalues.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_int)]
+    L.bsl_tm_eigenvectors.argtypes = [C.c_int, _P, _P, _P, _P, C.c_int, _P]
+    L.bsl_ritz_vectors.argtypes = [C.c_void_p, C.c_int, _P, C.c_int, _P]
+    L.bsl_last_run_ms_per_iter.argtypes = [C.c_void_p, _P]
+    L.bsl_copy_vgrid.argtypes = [C.c_void_p, _P, _P]
+    L.bsl_copy_vblocks.argtypes = [C.c_void_p, _P]
+    L.bsl_parse_hv_input.argtypes = [C.c_char_p, C.POINTER(HvParams)]
+    L.bsl_parse_isoharmosc_input.argtypes = [C.c_char_p, C.POINTER(HvParams)]
+    L.bsl_calculator_potential.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != OK:
+        raise BslError(rc, lib().bsl_last_error().decode())
+
+
+def _ptr(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_P)
+
+
+def parse_hv_input(path):
+    p = HvParams()
+    _check(lib().bsl_parse_hv_input(path.encode(), C.byref(p)))
+    return p
+
+
+def good_eigenvalues(alpha, beta, beta2, emin=-10.0, emax=10.0):
+    """Cullum-Willoughby good eigenvalues in (emin, emax] and error estimates."""
+    alpha, beta, beta2 = (np.ascontiguousarray(x, dtype=np.float64) for x in (alpha, beta, beta2))
+    niter = len(alpha)
+    ev = np.zeros(niter)
+    er = np.zeros(niter)
+    ng = C.c_int(0)
+    _check(lib().bsl_good_eigenvalues(niter, _ptr(alpha), _ptr(beta), _ptr(beta2), emin, emax, _ptr(ev), _ptr(er),
+                                      C.byref(ng)))
+    return ev[:ng.value].copy(), er[:ng.value].copy()
+
+
+def tm_eigenvectors(alpha, beta, beta2, evals):
+    alpha, beta, beta2, evals = (np.ascontiguousarray(x, dtype=np.float64) for x in (alpha, beta, beta2, evals))
+    niter, ngood = len(alpha), len(evals)
+    out = np.zeros(niter * ngood)
+    _check(lib().bsl_tm_eigenvectors(niter, _ptr(alpha), _ptr(beta), _ptr(beta2), _ptr(evals), ngood, _ptr(out)))
+    return out.reshape(ngood, niter)  # row n = column n of the column-major evtr
+
+
+class Hamiltonian:
+    """A prepared H on one GPU (the reference's HvPrep result)."""
+
+    def __init__(self, hv_input, calculator="linRotCartSph_NoQuad_ContGrid_Alavi_SPCE", extra_input=None,
+                 precision="fp64", device=0, params=None):
+        L = lib()
+        p = params if params is not None else parse_hv_input(hv_input)
+        pot = C.c_int(0)
+        _check(L.bsl_calculator_potential(calculator.encode(), C.byref(pot)))
+        p.potential = pot.value
+        if p.potential == POT_ISOHARMOSC:
+            _check(L.bsl_parse_isoharmosc_input(extra_input.encode(), C.byref(p)))
+        p.precision = PREC[precision]
+        p.device = device
+        self.params = p
+        h = C.c_void_p()
+        _check(L.bsl_hv_prep(C.byref(p), C.byref(h)))
+        self._h = h
+        self.basis_size = L.bsl_basis_size(h)
+        self.packed_size = L.bsl_packed_size(h)
+        self.nn = L.bsl_packed_nn(h)
+
+    def close(self):
+        if self._h:
+            lib().bsl_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_precision(self, precision):
+        _check(lib().bsl_set_precision(self._h, PREC[precision]))
+
+    def hv(self, vec, uec):
+        """uec += H vec (host arrays, reference layout)."""
+        _check(lib().bsl_hv_apply(self._h, _ptr(vec), _ptr(uec)))
+
+    def hv_device(self, d_v, d_u, stream=0):
+        """u = H v on device pointers in the packed layout."""
+        _check(lib().bsl_hv_apply_device(self._h, C.c_void_p(d_v), C.c_void_p(d_u), C.c_void_p(stream)))
+
+    def stream(self):
+        return lib().bsl_stream(self._h)
+
+    def lanczos(self, niter, start="uniform", seed=0):
+        a = np.zeros(niter)
+        b = np.zeros(niter + 1)
+        b2 = np.zeros(niter + 1)
+        _check(lib().bsl_lanczos_run(self._h, niter, START[start], seed, _ptr(a), _ptr(b), _ptr(b2)))
+        return a, b, b2
+
+    def last_ms_per_iter(self):
+        x = np.zeros(1)
+        _check(lib().bsl_last_run_ms_per_iter(self._h, _ptr(x)))
+        return float(x[0])
+
+    def step_host(self, vec, rvec):
+        """One reference loop-body iteration on host state; returns alpha, beta, beta2."""
+        out = np.zeros(3)
+        o = out.ctypes.data
+        _check(lib().bsl_lanczos_step_host(self._h, _ptr(vec), _ptr(rvec), C.cast(o, _P), C.cast(o + 8, _P),
+                                           C.cast(o + 16, _P)))
+        return out[0], out[1], out[2]
+
+    def ritz(self, niter, evtr_rows):
+        """Ritz vectors (reference layout), evtr_rows[n] = T_m eigenvector n."""
+        ng = evtr_rows.shape[0]
+        ev = np.ascontiguousarray(evtr_rows, dtype=np.float64).reshape(-1)
+        out = np.zeros(ng * self.basis_size)
+        _check(lib().bsl_ritz_vectors(self._h, niter, _ptr(ev), ng, _ptr(out)))
+        return out.reshape(ng, self.basis_size)
+
+    def vgrid(self):
+        n = lib().bsl_vgrid_size(self._h)
+        a, b = np.zeros(n), np.zeros(n)
+        _check(lib().bsl_copy_vgrid(self._h, _ptr(a), _ptr(b)))
+        return a, b
+
+    def vblocks(self):
+        out = np.zeros(lib().bsl_vblock_size(self._h))
+        _check(lib().bsl_copy_vblocks(self._h, _ptr(out)))
+        return out
+
+
+class _Storage:
+    def __init__(self, calculator):
+        self.calculator = calculator
+        self.h = None
+        self.total_basis_size = None
+
+
+def hv_interface_setup(calculator):
+    """Mirror of HvInterfaceSetup (interface.cpp:3): returns (storage, HvPrep, Hv).
+
+    HvPrep(argv, storage) reads argv[2] (HvInputFile) and argv[3] (oscillator
+    file) like the reference; Hv(argv, storage, vec, uec) accumulates
+    uec += H vec.  Unknown names raise, where the reference prints and exits.
+    """
+    if calculator not in CALCULATORS:
+        raise BslError(ERR_INPUT, "HvCalculator '%s' not recognized." % calculator)
+    st = _Storage(calculator)
+
+    def hv_prep(argv, storage, precision=os.environ.get("BSL_PRECISION", "fp64")):
+        extra = argv[3] if len(argv) > 3 else None
+        storage.h = Hamiltonian(argv[2], calculator, extra_input=extra, precision=precision)
+        storage.total_basis_size = storage.h.basis_size
+        return storage.total_basis_size
+
+    def hv(argv, storage, vec, uec):
+        storage.h.hv(vec, uec)
+
+    return st, hv_prep, hv

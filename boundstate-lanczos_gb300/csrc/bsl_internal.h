@@ -1,0 +1,136 @@
+// Internal declarations shared by the host translation units and the CUDA
+// kernels of the boundstate-lanczos GB300 library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "bsl.h"
+
+namespace bsl {
+
+// Physical constants in the reference's unit system (nm, ps, amu, kJ/mol),
+// headLoop/InterfaceCode/lanczosUnits.h:5-14.
+constexpr double kPi = 3.141592653589793;
+constexpr double kCoulombK = 138.9354846111096;
+constexpr double kHbar = 0.0635077857002;
+constexpr double kNmPerAngstrom = 0.1;
+
+// Largest packed (l,m) block with a register-resident potential kernel.
+constexpr int kMaxNN = 36;
+
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* where);
+
+#define BSL_CUDA(call)                                        \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return ::bsl::cuda_fail(_e, #call); \
+  } while (0)
+
+// Host-side basis and quadrature tables (all FP64).
+struct Tables {
+  int nx = 0, ny = 0, nz = 0;
+  long long npts = 0;          // nx*ny*nz
+  int lmax = 0, nn_full = 0;   // (lmax+1)^2
+  int nn = 0;                  // functions kept by the symmetry block
+  int na = 0, nb = 0;          // theta nodes, phi nodes per half
+  std::vector<int> l_of, m_of; // full composite index -> l, m
+  std::vector<int> full_of;    // packed index -> full index
+  std::vector<double> xg, yg, zg;       // grids
+  std::vector<double> tx, ty, tz;       // kinetic matrices, row-major [i*n + i']
+  std::vector<double> rot;              // rotor energies B l(l+1), packed
+  std::vector<double> gl_x, gl_w;       // Gauss-Legendre nodes in cos(theta), weights
+  std::vector<double> gc_x, gc_w;       // cos(phi_b), weights pi/nb
+  std::vector<double> theta, phi, phi2; // acos values, 2pi - phi
+  std::vector<double> leg;              // [s][a] normalised associated Legendre, packed
+  std::vector<double> trig1, trig2;     // [m+lmax][b] trig factor at phi_b and 2pi-phi_b
+};
+
+// Water cage: atom positions (nm), charges, LJ flag (oxygen).
+struct Cage {
+  std::vector<double> xyz;  // [atom][3]
+  std::vector<double> q;
+  std::vector<int> is_o;
+};
+
+int build_tables(const bsl_hv_params& p, Tables* t);
+int read_cage(const std::string& path, Cage* c);
+
+// Device-resident state of one prepared Hamiltonian.
+struct DeviceState {
+  cudaStream_t stream = nullptr;
+  // kinetic matrices: FP64 and the FP32 hi/lo split (T = hi + lo + O(2^-48))
+  double *tx = nullptr, *ty = nullptr, *tz = nullptr;
+  float *tx_hi = nullptr, *tx_lo = nullptr, *ty_hi = nullptr, *ty_lo = nullptr, *tz_hi = nullptr,
+        *tz_lo = nullptr;
+  double* rot = nullptr;  // [nn]
+  // potential grid V(p, a, b) for phi_b and 2pi - phi_b, p in vector order
+  double *v1 = nullptr, *v2 = nullptr;
+  // potential blocks, packed upper triangle t = (s, s') with s <= s', [t][p]
+  double* vb64 = nullptr;
+  float* vb32 = nullptr;
+  // Lanczos work vectors (packed layout) and reduction scratch
+  double *vec = nullptr, *rvec = nullptr, *ukin = nullptr;
+  double* partials = nullptr;  // one double per reduction block
+  unsigned int* counter = nullptr;
+  double* scalars = nullptr;   // [0] alpha_j, [1] beta_j, [2] beta2_j, [3] 1/beta_j
+  int* status = nullptr;       // non-zero after a breakdown
+  double* hist = nullptr;      // alpha/beta/beta2 history [3][niter+1]
+  int hist_cap = 0;
+  // host-layout staging
+  double *ref_vec = nullptr, *ref_out = nullptr;  // full reference layout
+  int* full_of = nullptr;                          // packed -> full index
+  double* ritz = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int red_blocks = 0;
+};
+
+}  // namespace bsl
+
+struct bsl_handle {
+  bsl_hv_params p;
+  bsl::Tables t;
+  bsl::Cage cage;
+  bsl::DeviceState d;
+  int precision = BSL_PREC_FP64;
+  double last_ms_per_iter = 0.0;
+};
+
+namespace bsl {
+
+// ---- kernel launchers (bsl_kernels.cu) -----------------------------------
+int dev_potential_alavi(bsl_handle* h);
+int dev_potential_iso(bsl_handle* h);
+int dev_vblocks(bsl_handle* h);
+int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s);
+// One Lanczos iteration on the packed state (vec, rvec) with the device
+// iteration index j (1-based) used to store alpha/beta history.
+int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s);
+int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_t* ev);
+const char* dev_stage_name(bsl_handle* h, int i);
+int dev_fill_start(bsl_handle* h, int start, unsigned long long seed, cudaStream_t s);
+int dev_gather_packed(bsl_handle* h, const double* full, double* packed, cudaStream_t s);
+int dev_scatter_full(bsl_handle* h, const double* packed, double* full_accum, cudaStream_t s);
+int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, int ngood, double* ritz,
+                        cudaStream_t s);
+
+// potential-block apply (bsl_vapply_f32.cu / bsl_vapply_f64.cu)
+int launch_vapply_f32(const float* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
+                      const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
+                      double* scalars, double* hist, int j, long long dpk);
+int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
+                      const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
+                      double* scalars, double* hist, int j, long long dpk);
+
+// ---- Cullum-Willoughby tail (bsl_tail.cpp) --------------------------------
+int cw_good_eigenvalues(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
+                        double emax, double* eval, double* err, int* ngood);
+int cw_tm_eigenvectors(int niter, const double* alpha, const double* beta, const double* beta2,
+                       const double* eval, int ngood, double* evtr);
+
+}  // namespace bsl

@@ -1,0 +1,680 @@
+// CUDA kernels (sm_103a) of the boundstate-lanczos GB300 library.
+//
+//   potential grid     V(x,y,z,theta,phi) for the Alavi H2 model in an SPC/E cage
+//                      (reference: potentialCalc/Alavi/AlaviGeneric/Alavi_ContGrid_H2_Routines.cpp:6-147)
+//                      or the isotropic oscillator (IsoHarmOsc_Routines.cpp:6-31), FP64
+//   potential blocks   <lm|V|l'm'>(x,y,z) by the angular quadrature, sum-factorised over phi
+//                      (reference: HvCalc/NoQuadOnTheFly/ContinuousAngularGrid/linRotCartSphHvContGridRoutines.cpp:7-152)
+//   kinetic            sinc-DVR contractions along x, y (one plane per CTA) and z
+//                      (reference: HvCalc/linRotCartSphHvRoutines.cpp:1807-1969)
+//   potential apply    per-point symmetric block times the local (l,m) coefficients, fused
+//                      with the rotor diagonal and the first Lanczos update and dot product
+//                      (reference: HvCalc/NoQuadOnTheFly/linRotCartSphHvFullVPrepRoutines.cpp:675-796)
+//   Lanczos            fused axpy/dot/norm kernels with deterministic last-block reductions
+//                      (reference: headLoop/LanczosCode/lanczosEigenValuesVectors.cpp:191-238)
+//
+// Vectors use the packed layout: element (s, p) at s*N + p with p = (k*ny + j)*nx + i.
+// Potential blocks use [t][p] with t enumerating s <= s' row by row, so that
+// consecutive threads (consecutive p) read consecutive addresses.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "bsl_device.cuh"
+
+namespace bsl {
+namespace {
+
+
+// ---------------------------------------------------------------------------
+// potential grid (FP64, no contraction: the reference evaluates each product
+// and sum separately)
+// ---------------------------------------------------------------------------
+struct AtomSet {
+  const double* xyz;  // [natoms][3]
+  const double* q;
+  const int* is_o;
+  int n;
+};
+
+constexpr double kQ_H2_H = 0.4932, kQ_H2_CM = -0.9864;   // Alavi_Parameters.h:5-6
+constexpr double kA_LJ = 1.364e-06, kB_LJ = 1.533e-3;    // SPCE_AH2_EngRoutines.h:37-38
+constexpr int kMaxAtoms = 512;
+
+__device__ __forceinline__ double dist(const double* a, double x, double y, double z) {
+  const double d0 = __dsub_rn(a[0], x), d1 = __dsub_rn(a[1], y), d2 = __dsub_rn(a[2], z);
+  double s = __dmul_rn(d0, d0);
+  s = __dadd_rn(s, __dmul_rn(d1, d1));
+  s = __dadd_rn(s, __dmul_rn(d2, d2));
+  return __dsqrt_rn(s);
+}
+
+__device__ __forceinline__ double coulomb(const double* sxyz, const double* sq, int n, double qsite, double x,
+                                          double y, double z) {
+  double e = 0.0;
+  const double kq = __dmul_rn(kCoulombK, qsite);
+  for (int i = 0; i < n; ++i) e = __dadd_rn(e, __ddiv_rn(__dmul_rn(kq, sq[i]), dist(sxyz + 3 * i, x, y, z)));
+  return e;
+}
+
+__global__ void k_potential_cm(AtomSet atoms, const double* xg, const double* yg, const double* zg, int nx, int ny,
+                               long long npts, double* cm) {
+  __shared__ double sxyz[3 * kMaxAtoms], sq[kMaxAtoms];
+  __shared__ int so[kMaxAtoms];
+  for (int i = threadIdx.x; i < atoms.n; i += blockDim.x) {
+    sxyz[3 * i] = atoms.xyz[3 * i];
+    sxyz[3 * i + 1] = atoms.xyz[3 * i + 1];
+    sxyz[3 * i + 2] = atoms.xyz[3 * i + 2];
+    sq[i] = atoms.q[i];
+    so[i] = atoms.is_o[i];
+  }
+  __syncthreads();
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  const int i = (int)(p % nx), j = (int)((p / nx) % ny), k = (int)(p / ((long long)nx * ny));
+  const double x = xg[i], y = yg[j], z = zg[k];
+  double e = coulomb(sxyz, sq, atoms.n, kQ_H2_CM, x, y, z);
+  double lj = 0.0;
+  for (int a = 0; a < atoms.n; ++a) {
+    if (!so[a]) continue;
+    const double r = dist(sxyz + 3 * a, x, y, z);
+    lj = __dadd_rn(lj, __dsub_rn(__ddiv_rn(kA_LJ, pow(r, 12.0)), __ddiv_rn(kB_LJ, pow(r, 6.0))));
+  }
+  cm[p] = __dadd_rn(e, lj);
+}
+
+// one thread per (point, theta_a, phi_b): both phi halves
+__global__ void k_potential_alavi(AtomSet atoms, const double* xg, const double* yg, const double* zg, int nx, int ny,
+                                  long long npts, int nab, const double* hdir, const double* cm, double ceiling,
+                                  double* v1, double* v2) {
+  __shared__ double sxyz[3 * kMaxAtoms], sq[kMaxAtoms];
+  for (int i = threadIdx.x; i < atoms.n; i += blockDim.x) {
+    sxyz[3 * i] = atoms.xyz[3 * i];
+    sxyz[3 * i + 1] = atoms.xyz[3 * i + 1];
+    sxyz[3 * i + 2] = atoms.xyz[3 * i + 2];
+    sq[i] = atoms.q[i];
+  }
+  __syncthreads();
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npts * nab) return;
+  const long long p = t / nab;
+  const int ab = (int)(t % nab);
+  const int i = (int)(p % nx), j = (int)((p / nx) % ny), k = (int)(p / ((long long)nx * ny));
+  const double x = xg[i], y = yg[j], z = zg[k];
+  const double hx = hdir[3 * ab], hy = hdir[3 * ab + 1], hz = hdir[3 * ab + 2];
+  const double c = cm[p];
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    const double hyh = half ? -1.0 * hy : hy;
+    double v = coulomb(sxyz, sq, atoms.n, kQ_H2_H, __dadd_rn(x, hx), __dadd_rn(y, hyh), __dadd_rn(z, hz));
+    v = __dadd_rn(v, coulomb(sxyz, sq, atoms.n, kQ_H2_H, __dsub_rn(x, hx), __dsub_rn(y, hyh), __dsub_rn(z, hz)));
+    v = __dadd_rn(v, c);
+    if (v >= ceiling) v = ceiling;
+    (half ? v2 : v1)[t] = v;
+  }
+}
+
+__global__ void k_potential_iso(const double* xg, const double* yg, const double* zg, int nx, int ny, long long npts,
+                                int nab, double factor, double iso_ceiling, double ceiling, double* v1, double* v2) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npts * nab) return;
+  const long long p = t / nab;
+  const int i = (int)(p % nx), j = (int)((p / nx) % ny), k = (int)(p / ((long long)nx * ny));
+  const double x = xg[i], y = yg[j], z = zg[k];
+  double d2 = __dmul_rn(x, x);
+  d2 = __dadd_rn(d2, __dmul_rn(y, y));
+  d2 = __dadd_rn(d2, __dmul_rn(z, z));
+  double v = __dmul_rn(factor, d2);
+  if (fabs(v) > fabs(iso_ceiling)) v = iso_ceiling;
+  if (v >= ceiling) v = ceiling;
+  v1[t] = v;
+  v2[t] = v;
+}
+
+// ---------------------------------------------------------------------------
+// potential blocks: one CTA per grid point.
+//   F[a][m,m'] = sum_b w_b (T1_m(b) T1_m'(b) V1(a,b) + T2_m(b) T2_m'(b) V2(a,b))
+//   B[s,s']   = sum_a w_a L_s(a) L_s'(a) F[a][m_s, m_s']
+// ---------------------------------------------------------------------------
+struct BlockTables {
+  const double* trig1;  // [nm][nb]
+  const double* trig2;
+  const double* leg;    // [nn][na]
+  const double* wa;     // [na]
+  const double* wb;     // [nb]
+  const int2* mpair;    // [nmtri] (mi, mj), mi <= mj
+  const int2* spair;    // [ntri] (s, s')
+  const int* fidx;      // [ntri] index into the mpair list of (m_s, m_s') sorted
+  int na, nb, nm, nmtri, nn, ntri;
+};
+
+__global__ void k_vblocks(BlockTables bt, const double* v1, const double* v2, long long npts, double* vb64,
+                          float* vb32) {
+  extern __shared__ double smem[];
+  const int na = bt.na, nb = bt.nb, nab = na * nb;
+  double* sV1 = smem;
+  double* sV2 = sV1 + nab;
+  double* sT1 = sV2 + nab;
+  double* sT2 = sT1 + bt.nm * nb;
+  double* sL = sT2 + bt.nm * nb;
+  double* sF = sL + bt.nn * na;
+  const long long p = blockIdx.x;
+  for (int e = threadIdx.x; e < nab; e += blockDim.x) {
+    sV1[e] = v1[p * nab + e];
+    sV2[e] = v2[p * nab + e];
+  }
+  for (int e = threadIdx.x; e < bt.nm * nb; e += blockDim.x) {
+    const int b = e % nb;
+    sT1[e] = bt.trig1[e] * sqrt(bt.wb[b]);
+    sT2[e] = bt.trig2[e] * sqrt(bt.wb[b]);
+  }
+  for (int e = threadIdx.x; e < bt.nn * na; e += blockDim.x) sL[e] = bt.leg[e];
+  __syncthreads();
+  for (int e = threadIdx.x; e < na * bt.nmtri; e += blockDim.x) {
+    const int a = e / bt.nmtri;
+    const int2 mm = bt.mpair[e % bt.nmtri];
+    const double* t1a = sT1 + mm.x * nb;
+    const double* t1b = sT1 + mm.y * nb;
+    const double* t2a = sT2 + mm.x * nb;
+    const double* t2b = sT2 + mm.y * nb;
+    const double* va = sV1 + a * nb;
+    const double* vb = sV2 + a * nb;
+    double f = 0.0;
+    for (int b = 0; b < nb; ++b) f += t1a[b] * t1b[b] * va[b] + t2a[b] * t2b[b] * vb[b];
+    sF[e] = f;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < bt.ntri; t += blockDim.x) {
+    const int2 ss = bt.spair[t];
+    const int fi = bt.fidx[t];
+    const double* la = sL + ss.x * na;
+    const double* lb = sL + ss.y * na;
+    double acc = 0.0;
+    for (int a = 0; a < na; ++a) acc += bt.wa[a] * la[a] * lb[a] * sF[a * bt.nmtri + fi];
+    vb64[(long long)t * npts + p] = acc;
+    vb32[(long long)t * npts + p] = (float)acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// kinetic
+// ---------------------------------------------------------------------------
+// x and y contractions of one (s, k) plane; out = Tx.v + Ty.v (overwrites)
+__global__ void k_kin_xy_f64(const double* __restrict__ vec, double* __restrict__ out, const double* __restrict__ tx,
+                             const double* __restrict__ ty, int nx, int ny, int nz) {
+  extern __shared__ double plane[];
+  const int k = blockIdx.x, s = blockIdx.y;
+  const long long base = ((long long)s * nz + k) * ny * nx;
+  const int np = nx * ny;
+  for (int e = threadIdx.x; e < np; e += blockDim.x) plane[e] = vec[base + e];
+  __syncthreads();
+  for (int e = threadIdx.x; e < np; e += blockDim.x) {
+    const int j = e / nx, i = e - j * nx;
+    const double* tr = tx + (long long)i * nx;
+    const double* row = plane + j * nx;
+    double ax = 0.0;
+    for (int q = 0; q < nx; ++q) ax += __ldg(tr + q) * row[q];
+    const double* tc = ty + (long long)j * ny;
+    double ay = 0.0;
+    for (int q = 0; q < ny; ++q) ay += __ldg(tc + q) * plane[q * nx + i];
+    out[base + e] = ay + ax;
+  }
+}
+
+// z contraction of one (s, j) plane, added: out += Tz.v
+__global__ void k_kin_z_f64(const double* __restrict__ vec, double* __restrict__ out, const double* __restrict__ tz,
+                            int nx, int ny, int nz) {
+  extern __shared__ double plane[];  // [k][i]
+  const int j = blockIdx.x, s = blockIdx.y;
+  const long long sb = (long long)s * nz * ny * nx;
+  const int np = nx * nz;
+  for (int e = threadIdx.x; e < np; e += blockDim.x) {
+    const int k = e / nx, i = e - k * nx;
+    plane[e] = vec[sb + ((long long)k * ny + j) * nx + i];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < np; e += blockDim.x) {
+    const int k = e / nx, i = e - k * nx;
+    const double* tr = tz + (long long)k * nz;
+    double az = 0.0;
+    for (int q = 0; q < nz; ++q) az += __ldg(tr + q) * plane[q * nx + i];
+    const long long o = sb + ((long long)k * ny + j) * nx + i;
+    out[o] = az + out[o];
+  }
+}
+
+// Mixed precision: v rounded to FP32, each coefficient matrix split as
+// T = hi + lo (FP32 each).  hi.v and lo.v accumulate in FP32 separately and
+// are combined in FP64, so the FP32 rounding of the coefficients does not
+// reach the result and only the (random) rounding of v and of the sums does.
+__global__ void k_kin_xy_mixed(const double* __restrict__ vec, double* __restrict__ out,
+                               const float* __restrict__ txh, const float* __restrict__ txl,
+                               const float* __restrict__ tyh, const float* __restrict__ tyl, int nx, int ny, int nz) {
+  extern __shared__ float fplane[];
+  const int k = blockIdx.x, s = blockIdx.y;
+  const long long base = ((long long)s * nz + k) * ny * nx;
+  const int np = nx * ny;
+  for (int e = threadIdx.x; e < np; e += blockDim.x) fplane[e] = (float)vec[base + e];
+  __syncthreads();
+  for (int e = threadIdx.x; e < np; e += blockDim.x) {
+    const int j = e / nx, i = e - j * nx;
+    const float* row = fplane + j * nx;
+    const float* th = txh + (long long)i * nx;
+    const float* tl = txl + (long long)i * nx;
+    float xh = 0.f, xl = 0.f;
+    for (int q = 0; q < nx; ++q) {
+      const float pv = row[q];
+      xh = fmaf(__ldg(th + q), pv, xh);
+      xl = fmaf(__ldg(tl + q), pv, xl);
+    }
+    const float* uh = tyh + (long long)j * ny;
+    const float* ul = tyl + (long long)j * ny;
+    float yh = 0.f, yl = 0.f;
+    for (int q = 0; q < ny; ++q) {
+      const float pv = fplane[q * nx + i];
+      yh = fmaf(__ldg(uh + q), pv, yh);
+      yl = fmaf(__ldg(ul + q), pv, yl);
+    }
+    out[base + e] = ((double)yh + (double)yl) + ((double)xh + (double)xl);
+  }
+}
+
+__global__ void k_kin_z_mixed(const double* __restrict__ vec, double* __restrict__ out,
+                              const float* __restrict__ tzh, const float* __restrict__ tzl, int nx, int ny, int nz) {
+  extern __shared__ float fplane[];
+  const int j = blockIdx.x, s = blockIdx.y;
+  const long long sb = (long long)s * nz * ny * nx;
+  const int np = nx * nz;
+  for (int e = threadIdx.x; e < np; e += blockDim.x) {
+    const int k = e / nx, i = e - k * nx;
+    fplane[e] = (float)vec[sb + ((long long)k * ny + j) * nx + i];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < np; e += blockDim.x) {
+    const int k = e / nx, i = e - k * nx;
+    const float* th = tzh + (long long)k * nz;
+    const float* tl = tzl + (long long)k * nz;
+    float zh = 0.f, zl = 0.f;
+    for (int q = 0; q < nz; ++q) {
+      const float pv = fplane[q * nx + i];
+      zh = fmaf(__ldg(th + q), pv, zh);
+      zl = fmaf(__ldg(tl + q), pv, zl);
+    }
+    const long long o = sb + ((long long)k * ny + j) * nx + i;
+    out[o] = ((double)zh + (double)zl) + out[o];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Lanczos vector kernels over L entries (packed block plus the extra
+// coordinate, or the whole reference layout)
+// ---------------------------------------------------------------------------
+// alpha = v . r
+__global__ void k_dot_alpha(const double* __restrict__ v, const double* __restrict__ r, long long L, double* partials,
+                            unsigned int* counter, double* scalars, double* hist, int j) {
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x)
+    acc += v[i] * r[i];
+  double total;
+  if (reduce_grid(acc, partials, counter, &total) && threadIdx.x == 0) {
+    scalars[0] = total;
+    hist[j - 1] = total;
+  }
+}
+
+// r -= alpha v ; beta^2 = r . r ; beta = sqrt(beta^2)
+__global__ void k_update_beta(const double* __restrict__ v, double* __restrict__ r, long long L, double* partials,
+                              unsigned int* counter, double* scalars, double* hist, int hist_stride, int j,
+                              int* status) {
+  const double alpha = scalars[0];
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x) {
+    const double x = r[i] - alpha * v[i];
+    r[i] = x;
+    acc += x * x;
+  }
+  double total;
+  if (reduce_grid(acc, partials, counter, &total) && threadIdx.x == 0) {
+    const double b = sqrt(total);
+    scalars[1] = b;
+    scalars[2] = total;
+    scalars[3] = 1. / b;
+    hist[hist_stride + j] = b;
+    hist[2 * hist_stride + j] = total;
+    if (!(b > 0.0) || !isfinite(b) || !isfinite(alpha)) {
+      if (status[0] == 0) status[1] = j;
+      status[0] = 1;
+    }
+  }
+}
+
+// v_{j+1} = r / beta ; r_{j+1} = -beta v_j  (the reference's scale-then-swap)
+__global__ void k_normalize_swap(double* __restrict__ v, double* __restrict__ r, long long L,
+                                 const double* __restrict__ scalars) {
+  const double b = scalars[1], inv = scalars[3];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x) {
+    const double vi = v[i];
+    v[i] = inv * r[i];
+    r[i] = (-b) * vi;
+  }
+}
+
+__global__ void k_fill(double* x, long long L, double val) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x)
+    x[i] = val;
+}
+
+// packed[s*N + p] = full[full_of[s]*N + p]
+__global__ void k_gather(const double* __restrict__ full, double* __restrict__ packed, const int* __restrict__ full_of,
+                         long long npts, int nn) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= npts * nn) return;
+  const int s = (int)(e / npts);
+  const long long p = e - (long long)s * npts;
+  packed[e] = full[(long long)full_of[s] * npts + p];
+}
+
+// full[full_of[s]*N + p] += packed[s*N + p]
+__global__ void k_scatter_add(const double* __restrict__ packed, double* __restrict__ full,
+                              const int* __restrict__ full_of, long long npts, int nn) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= npts * nn) return;
+  const int s = (int)(e / npts);
+  const long long p = e - (long long)s * npts;
+  const long long o = (long long)full_of[s] * npts + p;
+  full[o] = full[o] + packed[e];
+}
+
+// ritz[n*D + i] += coef[n] * v[i] for active n
+__global__ void k_ritz(const double* __restrict__ v, long long D, const double* __restrict__ coef,
+                       const int* __restrict__ active, int ngood, double* __restrict__ ritz) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (long long)gridDim.x * blockDim.x) {
+    const double vi = v[i];
+    for (int n = 0; n < ngood; ++n)
+      if (active[n]) ritz[(long long)n * D + i] += coef[n] * vi;
+  }
+}
+
+int launch_vapply(bsl_handle* h, const double* v, double* out, int mode, int j, cudaStream_t s) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  const long long N = t.npts;
+  const dim3 g(grid_for(N));
+  const long long dpk = N * t.nn;
+  if (h->precision == BSL_PREC_MIXED)
+    return launch_vapply_f32(d.vb32, g, s, t.nn, v, d.ukin, d.rot, out, N, mode, d.partials, d.counter, d.scalars,
+                             d.hist, j, dpk);
+  return launch_vapply_f64(d.vb64, g, s, t.nn, v, d.ukin, d.rot, out, N, mode, d.partials, d.counter, d.scalars,
+                           d.hist, j, dpk);
+}
+
+int launch_kinetic(bsl_handle* h, const double* v, cudaStream_t s) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  const bool mixed = h->precision == BSL_PREC_MIXED;
+  const size_t esz = mixed ? sizeof(float) : sizeof(double);
+  const size_t sm_xy = esz * t.nx * t.ny, sm_z = esz * t.nx * t.nz;
+  if (sm_xy > 200 * 1024 || sm_z > 200 * 1024) return fail(BSL_ERR_UNSUPPORTED, "grid plane too large for one CTA");
+  const dim3 gxy(t.nz, t.nn), gz(t.ny, t.nn);
+  if (mixed) {
+    cudaFuncSetAttribute(k_kin_xy_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
+    cudaFuncSetAttribute(k_kin_z_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_z);
+    k_kin_xy_mixed<<<gxy, kThreads, sm_xy, s>>>(v, d.ukin, d.tx_hi, d.tx_lo, d.ty_hi, d.ty_lo, t.nx, t.ny, t.nz);
+    k_kin_z_mixed<<<gz, kThreads, sm_z, s>>>(v, d.ukin, d.tz_hi, d.tz_lo, t.nx, t.ny, t.nz);
+  } else {
+    cudaFuncSetAttribute(k_kin_xy_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
+    cudaFuncSetAttribute(k_kin_z_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_z);
+    k_kin_xy_f64<<<gxy, kThreads, sm_xy, s>>>(v, d.ukin, d.tx, d.ty, t.nx, t.ny, t.nz);
+    k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(v, d.ukin, d.tz, t.nx, t.ny, t.nz);
+  }
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+int dev_potential_alavi(bsl_handle* h) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  const int natoms = (int)h->cage.q.size();
+  if (natoms > kMaxAtoms) return fail(BSL_ERR_UNSUPPORTED, "cage has more than 512 atoms");
+  std::vector<double> hdir((size_t)t.na * t.nb * 3);
+  const double hz = 0.03707;  // Alavi_Parameters.h:10, nm
+  for (int a = 0; a < t.na; ++a)
+    for (int b = 0; b < t.nb; ++b) {
+      double* o = &hdir[((size_t)a * t.nb + b) * 3];
+      o[0] = hz * sin(t.theta[a]) * t.gc_x[b];
+      o[1] = hz * sin(t.theta[a]) * sin(t.phi[b]);
+      o[2] = hz * t.gl_x[a];
+    }
+  double *dxyz = nullptr, *dq = nullptr, *dh = nullptr, *dx = nullptr, *dy = nullptr, *dz = nullptr;
+  int* dis_o = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(dxyz); cudaFree(dq); cudaFree(dh); cudaFree(dis_o); cudaFree(dx); cudaFree(dy); cudaFree(dz);
+  };
+  auto up = [&](void** p, const void* src, size_t bytes) -> cudaError_t {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*p, src, bytes, cudaMemcpyHostToDevice);
+  };
+  cudaError_t e;
+  if ((e = up((void**)&dxyz, h->cage.xyz.data(), h->cage.xyz.size() * 8)) != cudaSuccess ||
+      (e = up((void**)&dq, h->cage.q.data(), h->cage.q.size() * 8)) != cudaSuccess ||
+      (e = up((void**)&dis_o, h->cage.is_o.data(), h->cage.is_o.size() * 4)) != cudaSuccess ||
+      (e = up((void**)&dh, hdir.data(), hdir.size() * 8)) != cudaSuccess ||
+      (e = up((void**)&dx, t.xg.data(), t.xg.size() * 8)) != cudaSuccess ||
+      (e = up((void**)&dy, t.yg.data(), t.yg.size() * 8)) != cudaSuccess ||
+      (e = up((void**)&dz, t.zg.data(), t.zg.size() * 8)) != cudaSuccess) {
+    cleanup();
+    return cuda_fail(e, "potential upload");
+  }
+  AtomSet atoms{dxyz, dq, dis_o, natoms};
+  const long long N = t.npts;
+  const int nab = t.na * t.nb;
+  double* cm = d.ukin;  // scratch of >= N doubles
+  k_potential_cm<<<grid_for(N), kThreads, 0, d.stream>>>(atoms, dx, dy, dz, t.nx, t.ny, N, cm);
+  k_potential_alavi<<<grid_for(N * nab), kThreads, 0, d.stream>>>(atoms, dx, dy, dz, t.nx, t.ny, N, nab, dh, cm,
+                                                                  h->p.ceiling_potential, d.v1, d.v2);
+  e = cudaGetLastError();
+  cudaError_t e2 = cudaStreamSynchronize(d.stream);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(e, "potential kernel launch");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "potential kernel");
+  return BSL_OK;
+}
+
+int dev_potential_iso(bsl_handle* h) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  double *dx = nullptr, *dy = nullptr, *dz = nullptr;
+  BSL_CUDA(cudaMalloc(&dx, t.xg.size() * 8));
+  BSL_CUDA(cudaMalloc(&dy, t.yg.size() * 8));
+  BSL_CUDA(cudaMalloc(&dz, t.zg.size() * 8));
+  BSL_CUDA(cudaMemcpy(dx, t.xg.data(), t.xg.size() * 8, cudaMemcpyHostToDevice));
+  BSL_CUDA(cudaMemcpy(dy, t.yg.data(), t.yg.size() * 8, cudaMemcpyHostToDevice));
+  BSL_CUDA(cudaMemcpy(dz, t.zg.data(), t.zg.size() * 8, cudaMemcpyHostToDevice));
+  const double factor = 0.5 * h->p.iso_mass * h->p.iso_frequency * h->p.iso_frequency;
+  const long long N = t.npts;
+  const int nab = t.na * t.nb;
+  k_potential_iso<<<grid_for(N * nab), kThreads, 0, d.stream>>>(dx, dy, dz, t.nx, t.ny, N, nab, factor,
+                                                                h->p.iso_ceiling, h->p.ceiling_potential, d.v1, d.v2);
+  cudaError_t e = cudaGetLastError();
+  cudaError_t e2 = cudaStreamSynchronize(d.stream);
+  cudaFree(dx);
+  cudaFree(dy);
+  cudaFree(dz);
+  if (e != cudaSuccess) return cuda_fail(e, "isotropic oscillator kernel launch");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "isotropic oscillator kernel");
+  return BSL_OK;
+}
+
+int dev_vblocks(bsl_handle* h) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  const int nm = 2 * t.lmax + 1, nmtri = nm * (nm + 1) / 2, ntri = t.nn * (t.nn + 1) / 2;
+  std::vector<int2> mpair, spair;
+  std::vector<int> fidx;
+  std::vector<int> mindex((size_t)nm * nm, -1);
+  for (int a = 0; a < nm; ++a)
+    for (int b = a; b < nm; ++b) {
+      mindex[(size_t)a * nm + b] = (int)mpair.size();
+      mpair.push_back(make_int2(a, b));
+    }
+  for (int s = 0; s < t.nn; ++s)
+    for (int q = s; q < t.nn; ++q) {
+      spair.push_back(make_int2(s, q));
+      int ma = t.m_of[t.full_of[s]] + t.lmax, mb = t.m_of[t.full_of[q]] + t.lmax;
+      if (ma > mb) std::swap(ma, mb);
+      fidx.push_back(mindex[(size_t)ma * nm + mb]);
+    }
+  double *dt1, *dt2, *dleg, *dwa, *dwb;
+  int2 *dmp, *dsp;
+  int* dfi;
+  BSL_CUDA(cudaMalloc(&dt1, t.trig1.size() * 8));
+  BSL_CUDA(cudaMalloc(&dt2, t.trig2.size() * 8));
+  BSL_CUDA(cudaMalloc(&dleg, t.leg.size() * 8));
+  BSL_CUDA(cudaMalloc(&dwa, t.gl_w.size() * 8));
+  BSL_CUDA(cudaMalloc(&dwb, t.gc_w.size() * 8));
+  BSL_CUDA(cudaMalloc(&dmp, mpair.size() * sizeof(int2)));
+  BSL_CUDA(cudaMalloc(&dsp, spair.size() * sizeof(int2)));
+  BSL_CUDA(cudaMalloc(&dfi, fidx.size() * sizeof(int)));
+  BSL_CUDA(cudaMemcpy(dt1, t.trig1.data(), t.trig1.size() * 8, cudaMemcpyHostToDevice));
+  BSL_CUDA(cudaMemcpy(dt2, t.trig2.data(), t.trig2.size() * 8, cudaMemcpyHostToDevice));
+  BSL_CUDA(cudaMemcpy(dleg, t.leg.data(), t.leg.size() * 8, cudaMemcpyHostToDevice));
+  BSL_CUDA(cudaMemcpy(dwa, t.gl_w.data(), t.gl_w.size() * 8, cudaMemcpyHostToDevice));
+  BSL_CUDA(cudaMemcpy(dwb, t.gc_w.data(), t.gc_w.size() * 8, cudaMemcpyHostToDevice));
+  BSL_CUDA(cudaMemcpy(dmp, mpair.data(), mpair.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  BSL_CUDA(cudaMemcpy(dsp, spair.data(), spair.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  BSL_CUDA(cudaMemcpy(dfi, fidx.data(), fidx.size() * sizeof(int), cudaMemcpyHostToDevice));
+  BlockTables bt{dt1, dt2, dleg, dwa, dwb, dmp, dsp, dfi, t.na, t.nb, nm, nmtri, t.nn, ntri};
+  const size_t smem = 8 * ((size_t)2 * t.na * t.nb + (size_t)2 * nm * t.nb + (size_t)t.nn * t.na +
+                           (size_t)t.na * nmtri);
+  int rc = BSL_OK;
+  if (smem > 220 * 1024) {
+    rc = fail(BSL_ERR_UNSUPPORTED, "angular quadrature too large for the block assembly kernel");
+  } else {
+    cudaFuncSetAttribute(k_vblocks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_vblocks<<<(unsigned)t.npts, kThreads, smem, d.stream>>>(bt, d.v1, d.v2, t.npts, d.vb64, d.vb32);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(d.stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "potential block assembly");
+  }
+  cudaFree(dt1); cudaFree(dt2); cudaFree(dleg); cudaFree(dwa); cudaFree(dwb);
+  cudaFree(dmp); cudaFree(dsp); cudaFree(dfi);
+  return rc;
+}
+
+int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s) {
+  int rc = launch_kinetic(h, v, s);
+  if (rc) return rc;
+  return launch_vapply(h, v, u, 0, 0, s);
+}
+
+int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s) {
+  DeviceState& d = h->d;
+  const long long L = bsl_packed_size(h) + 1;  // + the coordinate outside the symmetry block
+  int rc = launch_kinetic(h, d.vec, s);
+  if (rc) return rc;
+  if ((rc = launch_vapply(h, d.vec, d.rvec, 1, j, s))) return rc;
+  const int g = d.red_blocks;
+  k_update_beta<<<g, kThreads, 0, s>>>(d.vec, d.rvec, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j,
+                                       d.status);
+  k_normalize_swap<<<g, kThreads, 0, s>>>(d.vec, d.rvec, L, d.scalars);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+// The same iteration with an event recorded after every kernel (ev[0] before).
+int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_t* ev) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  const long long L = bsl_packed_size(h) + 1;
+  const bool mixed = h->precision == BSL_PREC_MIXED;
+  const size_t esz = mixed ? sizeof(float) : sizeof(double);
+  const size_t sm_xy = esz * t.nx * t.ny, sm_z = esz * t.nx * t.nz;
+  const dim3 gxy(t.nz, t.nn), gz(t.ny, t.nn);
+  if (mixed) {
+    cudaFuncSetAttribute(k_kin_xy_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
+    cudaFuncSetAttribute(k_kin_z_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_z);
+  } else {
+    cudaFuncSetAttribute(k_kin_xy_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
+    cudaFuncSetAttribute(k_kin_z_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_z);
+  }
+  cudaEventRecord(ev[0], s);
+  if (mixed)
+    k_kin_xy_mixed<<<gxy, kThreads, sm_xy, s>>>(d.vec, d.ukin, d.tx_hi, d.tx_lo, d.ty_hi, d.ty_lo, t.nx, t.ny, t.nz);
+  else
+    k_kin_xy_f64<<<gxy, kThreads, sm_xy, s>>>(d.vec, d.ukin, d.tx, d.ty, t.nx, t.ny, t.nz);
+  cudaEventRecord(ev[1], s);
+  if (mixed)
+    k_kin_z_mixed<<<gz, kThreads, sm_z, s>>>(d.vec, d.ukin, d.tz_hi, d.tz_lo, t.nx, t.ny, t.nz);
+  else
+    k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(d.vec, d.ukin, d.tz, t.nx, t.ny, t.nz);
+  cudaEventRecord(ev[2], s);
+  int rc = launch_vapply(h, d.vec, d.rvec, 1, j, s);
+  if (rc) return rc;
+  cudaEventRecord(ev[3], s);
+  const int g = d.red_blocks;
+  k_update_beta<<<g, kThreads, 0, s>>>(d.vec, d.rvec, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j,
+                                       d.status);
+  cudaEventRecord(ev[4], s);
+  k_normalize_swap<<<g, kThreads, 0, s>>>(d.vec, d.rvec, L, d.scalars);
+  cudaEventRecord(ev[5], s);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+const char* dev_stage_name(bsl_handle* h, int i) {
+  const bool mixed = h->precision == BSL_PREC_MIXED;
+  static const char* n64[5] = {"k_kin_xy_f64", "k_kin_z_f64", "k_vapply<NN,double>", "k_update_beta",
+                               "k_normalize_swap"};
+  static const char* nmx[5] = {"k_kin_xy_mixed", "k_kin_z_mixed", "k_vapply<NN,float>", "k_update_beta",
+                               "k_normalize_swap"};
+  return mixed ? nmx[i] : n64[i];
+}
+
+int dev_fill(double* x, long long L, double val, cudaStream_t s) {
+  k_fill<<<1024, kThreads, 0, s>>>(x, L, val);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+int dev_gather_packed(bsl_handle* h, const double* full, double* packed, cudaStream_t s) {
+  const long long N = h->t.npts;
+  k_gather<<<grid_for(N * h->t.nn), kThreads, 0, s>>>(full, packed, h->d.full_of, N, h->t.nn);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+int dev_scatter_full(bsl_handle* h, const double* packed, double* full_accum, cudaStream_t s) {
+  const long long N = h->t.npts;
+  k_scatter_add<<<grid_for(N * h->t.nn), kThreads, 0, s>>>(packed, full_accum, h->d.full_of, N, h->t.nn);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+// Full-layout Lanczos step on device buffers v, r (length L) after r += H v.
+int dev_full_step(bsl_handle* h, double* v, double* r, long long L, int j, cudaStream_t s) {
+  DeviceState& d = h->d;
+  const int g = d.red_blocks;
+  k_dot_alpha<<<g, kThreads, 0, s>>>(v, r, L, d.partials, d.counter, d.scalars, d.hist, j);
+  k_update_beta<<<g, kThreads, 0, s>>>(v, r, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j, d.status);
+  k_normalize_swap<<<g, kThreads, 0, s>>>(v, r, L, d.scalars);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, int ngood, double* ritz,
+                        cudaStream_t s) {
+  const long long L = bsl_packed_size(h) + 1;  // with the coordinate outside the symmetry block
+  k_ritz<<<1024, kThreads, 0, s>>>(h->d.vec, L, coef, active, ngood, ritz);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+}  // namespace bsl

@@ -1,0 +1,272 @@
+// Lanczos drivers of the C ABI: the device-resident loop, the host-state
+// single step, and the Ritz-vector pass.
+//
+// Reference driver: headLoop/LanczosCode/lanczosEigenValuesVectors.cpp
+//   start vector 1/sqrt(D)                       :177-181
+//   loop 1 (alpha, beta, scale, swap)            :187-242
+//   loop 2 with Ritz accumulation and cut-off    :371-469
+//
+// The device loop runs on the packed symmetry block plus one extra
+// coordinate.  The reference keeps all (l_max+1)^2 functions and multiplies H
+// by the 0/1 symmetry mask, so the components outside the block never receive
+// an H contribution: starting from the uniform vector they stay proportional to
+// one fixed unit vector.  That direction is carried as the single extra
+// coordinate (H acts on it as 0), which reproduces the reference's recurrence
+// -- including its spurious eigenvalue at 0 -- with D_packed + 1 unknowns.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bsl_internal.h"
+
+namespace bsl {
+int dev_fill(double* x, long long L, double val, cudaStream_t s);
+int dev_full_step(bsl_handle* h, double* v, double* r, long long L, int j, cudaStream_t s);
+
+namespace {
+
+int ensure_hist(bsl_handle* h, int niter) {
+  DeviceState& d = h->d;
+  if (d.hist && d.hist_cap >= niter + 1) return BSL_OK;
+  if (d.hist) cudaFree(d.hist);
+  d.hist = nullptr;
+  d.hist_cap = niter + 1;
+  BSL_CUDA(cudaMalloc(&d.hist, 3 * (size_t)d.hist_cap * sizeof(double)));
+  BSL_CUDA(cudaMemset(d.hist, 0, 3 * (size_t)d.hist_cap * sizeof(double)));
+  return BSL_OK;
+}
+
+int ensure_staging(bsl_handle* h) {
+  DeviceState& d = h->d;
+  if (d.ref_vec) return BSL_OK;
+  const size_t Df = (size_t)bsl_basis_size(h);
+  BSL_CUDA(cudaMalloc(&d.ref_vec, Df * sizeof(double) + 16));
+  BSL_CUDA(cudaMalloc(&d.ref_out, Df * sizeof(double) + 16));
+  return BSL_OK;
+}
+
+uint64_t splitmix64(uint64_t* s) {
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// N(0,1) by Box-Muller on splitmix64 uniforms (53-bit), normalised to 1.
+void normal_vector(uint64_t seed, size_t n, std::vector<double>* v) {
+  v->resize(n);
+  uint64_t s = seed;
+  const double two_pi = 6.283185307179586;
+  for (size_t i = 0; i < n; i += 2) {
+    const double u1 = ((splitmix64(&s) >> 11) + 1.0) * (1.0 / 9007199254740993.0);
+    const double u2 = (splitmix64(&s) >> 11) * (1.0 / 9007199254740992.0);
+    const double r = std::sqrt(-2.0 * std::log(u1));
+    (*v)[i] = r * std::cos(two_pi * u2);
+    if (i + 1 < n) (*v)[i + 1] = r * std::sin(two_pi * u2);
+  }
+  double nrm = 0.0;
+  for (size_t i = 0; i < n; ++i) nrm += (*v)[i] * (*v)[i];
+  nrm = std::sqrt(nrm);
+  for (size_t i = 0; i < n; ++i) (*v)[i] /= nrm;
+}
+
+int init_state(bsl_handle* h, int start, unsigned long long seed) {
+  DeviceState& d = h->d;
+  const long long D = bsl_packed_size(h), Df = bsl_basis_size(h);
+  cudaStream_t s = d.stream;
+  int rc;
+  if (start == BSL_START_UNIFORM) {
+    if ((rc = dev_fill(d.vec, D, 1. / std::sqrt((double)Df), s))) return rc;
+    const double ghost = std::sqrt((double)(Df - D) / (double)Df);
+    BSL_CUDA(cudaMemcpyAsync(d.vec + D, &ghost, sizeof(double), cudaMemcpyHostToDevice, s));
+  } else if (start == BSL_START_NORMAL) {
+    std::vector<double> v;
+    normal_vector(seed, (size_t)D, &v);
+    v.push_back(0.0);
+    BSL_CUDA(cudaMemcpyAsync(d.vec, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    BSL_CUDA(cudaStreamSynchronize(s));
+  } else {
+    return fail(BSL_ERR_INPUT, "unknown start vector kind");
+  }
+  if ((rc = dev_fill(d.rvec, D + 1, 0.0, s))) return rc;
+  BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
+  BSL_CUDA(cudaMemsetAsync(d.scalars, 0, 16 * sizeof(double), s));
+  return BSL_OK;
+}
+
+int check_status(bsl_handle* h) {
+  int st[2] = {0, 0};
+  BSL_CUDA(cudaMemcpy(st, h->d.status, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+  if (st[0]) return fail(BSL_ERR_BREAKDOWN, "Lanczos breakdown at iteration " + std::to_string(st[1]) +
+                                                ": beta is zero or alpha/beta are not finite");
+  return BSL_OK;
+}
+
+}  // namespace
+}  // namespace bsl
+
+using namespace bsl;
+
+extern "C" {
+
+int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed, double* alpha, double* beta,
+                    double* beta2) {
+  if (!h || niter < 1 || !alpha || !beta || !beta2) return fail(BSL_ERR_INPUT, "bad arguments");
+  cudaSetDevice(h->p.device);
+  DeviceState& d = h->d;
+  int rc;
+  if ((rc = ensure_hist(h, niter)) || (rc = init_state(h, start, seed))) return rc;
+  cudaStream_t s = d.stream;
+  BSL_CUDA(cudaEventRecord(d.ev0, s));
+  for (int j = 1; j <= niter; ++j)
+    if ((rc = dev_lanczos_iteration(h, j, s))) return rc;
+  BSL_CUDA(cudaEventRecord(d.ev1, s));
+  BSL_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  BSL_CUDA(cudaEventElapsedTime(&ms, d.ev0, d.ev1));
+  h->last_ms_per_iter = ms / niter;
+  std::vector<double> hist(3 * (size_t)d.hist_cap);
+  BSL_CUDA(cudaMemcpy(hist.data(), d.hist, hist.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int j = 0; j < niter; ++j) alpha[j] = hist[j];
+  beta[0] = 0.0;
+  beta2[0] = 0.0;
+  for (int j = 1; j <= niter; ++j) {
+    beta[j] = hist[d.hist_cap + j];
+    beta2[j] = hist[2 * (size_t)d.hist_cap + j];
+  }
+  return check_status(h);
+}
+
+int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alpha_j, double* beta_j,
+                          double* beta2_j) {
+  if (!h || !vec || !rvec) return fail(BSL_ERR_INPUT, "null argument");
+  cudaSetDevice(h->p.device);
+  DeviceState& d = h->d;
+  int rc;
+  if ((rc = ensure_hist(h, 1)) || (rc = ensure_staging(h))) return rc;
+  const size_t Df = (size_t)bsl_basis_size(h);
+  cudaStream_t s = d.stream;
+  BSL_CUDA(cudaMemcpyAsync(d.ref_vec, vec, Df * sizeof(double), cudaMemcpyHostToDevice, s));
+  BSL_CUDA(cudaMemcpyAsync(d.ref_out, rvec, Df * sizeof(double), cudaMemcpyHostToDevice, s));
+  BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
+  // r += S H v: H on the packed block, nothing elsewhere
+  if ((rc = dev_gather_packed(h, d.ref_vec, d.vec, s))) return rc;
+  if ((rc = dev_hv(h, d.vec, d.rvec, s))) return rc;
+  if ((rc = dev_scatter_full(h, d.rvec, d.ref_out, s))) return rc;
+  if ((rc = dev_full_step(h, d.ref_vec, d.ref_out, (long long)Df, 1, s))) return rc;
+  BSL_CUDA(cudaMemcpyAsync(vec, d.ref_vec, Df * sizeof(double), cudaMemcpyDeviceToHost, s));
+  BSL_CUDA(cudaMemcpyAsync(rvec, d.ref_out, Df * sizeof(double), cudaMemcpyDeviceToHost, s));
+  double sc[3];
+  BSL_CUDA(cudaMemcpyAsync(sc, d.scalars, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  BSL_CUDA(cudaStreamSynchronize(s));
+  if (alpha_j) *alpha_j = sc[0];
+  if (beta_j) *beta_j = sc[1];
+  if (beta2_j) *beta2_j = sc[2];
+  return check_status(h);
+}
+
+int bsl_ritz_vectors(bsl_handle* h, int niter, const double* evtr, int ngood, double* ritz) {
+  if (!h || niter < 1 || ngood < 1 || !evtr || !ritz) return fail(BSL_ERR_INPUT, "bad arguments");
+  cudaSetDevice(h->p.device);
+  DeviceState& d = h->d;
+  const long long D = bsl_packed_size(h), Df = bsl_basis_size(h), L = D + 1;
+  int rc;
+  if ((rc = ensure_hist(h, niter)) || (rc = init_state(h, BSL_START_UNIFORM, 0))) return rc;
+  // coefficient schedule with the reference's cumulative-norm cut-off
+  std::vector<double> coef((size_t)niter * ngood);
+  std::vector<int> active((size_t)niter * ngood);
+  std::vector<double> cum(ngood, 0.0);
+  for (int j = 1; j <= niter; ++j)
+    for (int n = 0; n < ngood; ++n) {
+      const double c = evtr[(size_t)n * niter + (j - 1)];
+      cum[n] += std::pow(c, 2.);
+      coef[(size_t)(j - 1) * ngood + n] = c;
+      active[(size_t)(j - 1) * ngood + n] = (cum[n] < (1. - 1.e-16)) ? 1 : 0;
+    }
+  double* dcoef = nullptr;
+  int* dact = nullptr;
+  double* dritz = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(dcoef);
+    cudaFree(dact);
+    cudaFree(dritz);
+  };
+  cudaError_t e;
+  if ((e = cudaMalloc(&dcoef, coef.size() * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&dact, active.size() * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&dritz, (size_t)ngood * L * sizeof(double))) != cudaSuccess) {
+    cleanup();
+    return fail(BSL_ERR_NOMEM, std::string("Ritz buffers: ") + cudaGetErrorString(e));
+  }
+  cudaStream_t s = d.stream;
+  cudaMemcpyAsync(dcoef, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(dact, active.data(), active.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(dritz, 0, (size_t)ngood * L * sizeof(double), s);
+  for (int j = 1; j <= niter; ++j) {
+    rc = dev_ritz_accumulate(h, dcoef + (size_t)(j - 1) * ngood, dact + (size_t)(j - 1) * ngood, ngood, dritz, s);
+    if (!rc) rc = dev_lanczos_iteration(h, j, s);
+    if (rc) {
+      cleanup();
+      return rc;
+    }
+  }
+  std::vector<double> host((size_t)ngood * L);
+  e = cudaMemcpyAsync(host.data(), dritz, host.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(e, "Ritz vectors");
+  const Tables& t = h->t;
+  const long long N = t.npts;
+  const double off = (Df > D) ? 1.0 / std::sqrt((double)(Df - D)) : 0.0;
+  for (int n = 0; n < ngood; ++n) {
+    double* out = ritz + (size_t)n * Df;
+    const double* in = host.data() + (size_t)n * L;
+    const double masked = in[D] * off;
+    for (long long i = 0; i < Df; ++i) out[i] = masked;
+    for (int sidx = 0; sidx < t.nn; ++sidx)
+      std::memcpy(out + (size_t)t.full_of[sidx] * N, in + (size_t)sidx * N, N * sizeof(double));
+  }
+  return check_status(h);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names) {
+  if (!h || iters < 1 || !ms) return fail(BSL_ERR_INPUT, "bad arguments");
+  cudaSetDevice(h->p.device);
+  DeviceState& d = h->d;
+  int rc;
+  if ((rc = ensure_hist(h, iters))) return rc;
+  cudaEvent_t ev[6];
+  for (int i = 0; i < 6; ++i) BSL_CUDA(cudaEventCreate(&ev[i]));
+  double acc[5] = {0, 0, 0, 0, 0};
+  for (int j = 1; j <= iters && !rc; ++j) {
+    rc = dev_lanczos_iteration_timed(h, j, d.stream, ev);
+    if (rc) break;
+    cudaError_t e = cudaEventSynchronize(ev[5]);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "stage timing");
+      break;
+    }
+    for (int i = 0; i < 5; ++i) {
+      float x = 0.f;
+      cudaEventElapsedTime(&x, ev[i], ev[i + 1]);
+      acc[i] += x;
+    }
+  }
+  for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+  if (rc) return rc;
+  for (int i = 0; i < 5; ++i) {
+    ms[i] = acc[i] / iters;
+    if (names) names[i] = dev_stage_name(h, i);
+  }
+  return check_status(h);
+}
+
+int bsl_launches_per_iteration(const bsl_handle* h) { return h ? 5 : -1; }
+
+}  // extern "C"

@@ -1,0 +1,199 @@
+/*
+ * boundstate-lanczos GB300 — C ABI of the NoQuad Hv path.
+ *
+ * One process drives one GPU.  Every entry point returns a status code
+ * (BSL_OK on success) and never exits the process; the text of the last error
+ * of the calling thread is available from bsl_last_error().  No entry point
+ * takes or returns a C++ or torch type: plain pointers, sizes and a CUDA
+ * stream handle passed as void*.
+ *
+ * Layouts
+ *   reference layout  double[nx*ny*nz*(l_max+1)^2], index ((n*nz+k)*ny+j)*nx+i,
+ *                     n = composite (l,m) index with m outer (-l_max..l_max) and
+ *                     l inner (|m|..l_max); the layout of the reference's vec/uec
+ *                     (Hv-calculators/linRotor/cartSphBasis/HvCalc/NoQuadOnTheFly/
+ *                     linRotCartSphHvFullVPrepRoutines.cpp:807-822).
+ *   packed layout     double[nx*ny*nz*nn_sym] on the device, index (s*nz+k)*ny+j)*nx+i
+ *                     where s runs over the (l,m) pairs kept by the rotational
+ *                     symmetry (All: all, Even: even l, Odd: odd l) in reference
+ *                     order.  The reference multiplies every other component by
+ *                     zero (calcSym, same file :530-573), so the packed operator is
+ *                     the reference operator restricted to its non-zero block.
+ */
+#ifndef BSL_H
+#define BSL_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define BSL_OK 0
+#define BSL_ERR_INPUT 1       /* bad or missing input file / parameter */
+#define BSL_ERR_CUDA 2        /* CUDA runtime error (message has the CUDA text) */
+#define BSL_ERR_STATE 3       /* call out of order, null handle */
+#define BSL_ERR_BREAKDOWN 4   /* Lanczos breakdown: beta == 0 or non-finite alpha/beta */
+#define BSL_ERR_UNSUPPORTED 5 /* option not available in this build */
+#define BSL_ERR_NOMEM 6       /* device or host allocation failed */
+
+/* rotationalSymmetry(All/Even/Odd) */
+#define BSL_SYM_ALL 0
+#define BSL_SYM_EVEN 1
+#define BSL_SYM_ODD 2
+
+/* potential selected by the HvCalculator string */
+#define BSL_POT_ALAVI_SPCE 0  /* linRotCartSph_NoQuad_ContGrid_Alavi_SPCE */
+#define BSL_POT_ISOHARMOSC 1  /* linRotCartSph_NoQuad_IsoHarmOsc */
+
+/* arithmetic of the Hv application */
+#define BSL_PREC_FP64 0  /* every step in FP64 */
+#define BSL_PREC_MIXED 1 /* FP32 potential blocks, FP32 kinetic with split
+                            coefficients and FP64 combination, FP64 rotor
+                            diagonal and FP64 Lanczos recurrence */
+
+/* Lanczos start vector */
+#define BSL_START_UNIFORM 0 /* 1/sqrt(D) over the reference layout, as the
+                               reference driver (lanczosEigenValuesVectors.cpp:177-181) */
+#define BSL_START_NORMAL 1  /* N(0,1) from a seeded generator, normalised */
+
+typedef struct bsl_hv_params {
+  /* HvInputFile, in file order (linRotCartSphHvFullVPrepRoutines.cpp:256-320) */
+  int nx;
+  double x_max; /* full box width in nm; grid spans [-x_max/2, x_max/2] */
+  int ny;
+  double y_max;
+  int nz;
+  double z_max;
+  int l_max;
+  int theta_points; /* Gauss-Legendre nodes in cos(theta) */
+  int phi_points;   /* half of the uniform phi nodes: 2*phi_points in total */
+  int pnx;
+  double px_max;
+  int pny;
+  double py_max;
+  int pnz;
+  double pz_max;
+  double total_mass;          /* amu */
+  double rotational_constant; /* kJ/mol */
+  char geometry_filename[1024];
+  char simulation_title[256];
+  double ceiling_potential; /* kJ/mol */
+  int quadrature_study;     /* parsed, not used (the reference ignores it for NoQuad) */
+  int symmetry;             /* BSL_SYM_* */
+  /* potential */
+  int potential;       /* BSL_POT_* */
+  double iso_mass;     /* IsoHarmOsc input file (argv[3]) */
+  double iso_frequency;
+  double iso_ceiling;
+  /* execution */
+  int precision; /* BSL_PREC_* */
+  int device;    /* CUDA device ordinal */
+} bsl_hv_params;
+
+typedef struct bsl_handle bsl_handle;
+
+/* Text of the last error on the calling thread ("" if none). */
+const char* bsl_last_error(void);
+
+/* Parse an HvInputFile (two comment lines, then 22 "key= value" pairs whose keys
+   are ignored; replaces HvPrep_Internal_NoQuad's reader, linRotCartSphHvFullVPrepRoutines.cpp:246-348,
+   including its size checks).  Leaves potential/precision/device at defaults
+   (Alavi SPC/E, FP64, device 0). */
+int bsl_parse_hv_input(const char* path, bsl_hv_params* out);
+
+/* Parse the IsoHarmOsc potential file (IsoHarmOsc_Routines.cpp:41-58). */
+int bsl_parse_isoharmosc_input(const char* path, bsl_hv_params* inout);
+
+/* Map an HvCalculator string (headLoop/InterfaceCode/interface.cpp:3-250) to
+   BSL_POT_*; unknown names give BSL_ERR_INPUT. */
+int bsl_calculator_potential(const char* calculator, int* potential);
+
+/* HvPrep: build grids, tables and the potential on the device.  Replaces
+   Hv_Prep_linRotCartSph_NoQuad (linRotCartSphHvFullVPrepRoutines.cpp:798-805). */
+int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out);
+
+void bsl_destroy(bsl_handle* h);
+
+/* Sizes: reference layout (the reference's total_basis_size) and packed layout. */
+long long bsl_basis_size(const bsl_handle* h);
+long long bsl_packed_size(const bsl_handle* h);
+int bsl_packed_nn(const bsl_handle* h);
+
+/* Switch the arithmetic of later Hv applications (BSL_PREC_*). */
+int bsl_set_precision(bsl_handle* h, int precision);
+
+/* uec += H vec with host buffers in the reference layout.  Replaces
+   Hv_linRotCartSph_NoQuad (linRotCartSphHvFullVPrepRoutines.cpp:807-822):
+   same accumulation contract, same masking of the components outside the
+   symmetry block. */
+int bsl_hv_apply(bsl_handle* h, const double* vec, double* uec);
+
+/* u = H v on device buffers in the packed layout, on `stream` (cudaStream_t,
+   NULL = the legacy default stream). */
+int bsl_hv_apply_device(bsl_handle* h, const double* d_v, double* d_u, void* stream);
+
+/* Lanczos loop 1 on the device (lanczosEigenValuesVectors.cpp:170-242): niter
+   iterations from the given start vector; alpha[niter], beta[niter+1] and
+   beta2[niter+1] are written on the host (index 0 of beta/beta2 is zero).
+   Returns BSL_ERR_BREAKDOWN (with the iteration in the message) if beta
+   vanishes or alpha/beta stop being finite. */
+int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed, double* alpha, double* beta,
+                    double* beta2);
+
+/* One iteration of the reference loop body (lanczosEigenValuesVectors.cpp:191-238)
+   with the Lanczos state on the host in the reference layout: on return vec
+   holds v_{j+1} and rvec holds -beta_j v_j, alpha_j/beta_j/beta2_j are written.
+   Components outside the symmetry block follow the reference arithmetic
+   (they receive no H contribution). */
+int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alpha_j, double* beta_j,
+                          double* beta2_j);
+
+/* Cullum-Willoughby good eigenvalues in (emin, emax] with inverse-iteration
+   error estimates (lancbis.cpp:5-105 with BISEC/ISOEV/INVERR).  eval and err
+   need niter entries; *ngood receives the count. */
+int bsl_good_eigenvalues(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
+                         double emax, double* eval, double* err, int* ngood);
+
+/* Tm eigenvectors for the first ngood good eigenvalues (lanczosvectors +
+   TRIVEC, lanczosEigenValuesVectors.cpp:509-561): evtr is column-major
+   [niter x ngood]. */
+int bsl_tm_eigenvectors(int niter, const double* alpha, const double* beta, const double* beta2,
+                        const double* eval, int ngood, double* evtr);
+
+/* Lanczos loop 2 with Ritz accumulation on the device
+   (lanczosEigenValuesVectors.cpp:371-469): ritz[n*D + row] in the reference
+   layout, D = bsl_basis_size(h). */
+int bsl_ritz_vectors(bsl_handle* h, int niter, const double* evtr, int ngood, double* ritz);
+
+/* Timing of the last bsl_lanczos_run: average device milliseconds per
+   iteration, measured with CUDA events on the library's stream. */
+int bsl_last_run_ms_per_iter(const bsl_handle* h, double* ms);
+
+/* Per-kernel device time of the Lanczos iteration: runs `iters` iterations
+   (continuing the current device state) with CUDA events around every
+   kernel on the library's stream and writes the average milliseconds per
+   launch of the stages {kinetic x/y, kinetic z, potential apply + alpha,
+   update + beta, normalise + swap} into ms[0..4]; names[i] (optional) receives
+   the kernel name of stage i (static strings). */
+int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names);
+
+/* Kernel launches per Lanczos iteration of the current configuration. */
+int bsl_launches_per_iteration(const bsl_handle* h);
+
+/* The stream the library launches on (cudaStream_t as void*). */
+void* bsl_stream(const bsl_handle* h);
+
+/* Diagnostics for tests: copy the potential grid (packed halves, see
+   bsl_vgrid_size) or the potential blocks to the host, FP64. */
+long long bsl_vgrid_size(const bsl_handle* h);
+int bsl_copy_vgrid(const bsl_handle* h, double* v1, double* v2);
+long long bsl_vblock_size(const bsl_handle* h);
+int bsl_copy_vblocks(const bsl_handle* h, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BSL_H */

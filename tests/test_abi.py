@@ -1,0 +1,119 @@
+"""C ABI: the library loads and exports every entry point of include/bsl.h;
+input parsing and error reporting; the host-side Cullum-Willoughby tail
+against the oracle's restatement of the Fortran.  No GPU needed."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, REPO, case_info, load_oracle, load_package, oracle_lancbis, ptr
+
+
+@pytest.fixture(scope="module")
+def bsl():
+    pkg = load_package()
+    if not os.path.exists(pkg.LIB_PATH):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("bsl_build", os.path.join(REPO, "boundstate-lanczos_gb300",
+                                                                              "build.py"))
+        b = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(b)
+        b.build()
+    return pkg
+
+
+def header_functions():
+    txt = open(os.path.join(REPO, "include", "bsl.h")).read()
+    return sorted(set(re.findall(r"\b(bsl_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(bsl):
+    L = bsl.lib()
+    names = header_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+
+
+def test_parse_hv_input_fields(bsl, in_case_dir):
+    in_case_dir("cpu_workload")
+    p = bsl.parse_hv_input("hv_input.txt")
+    assert (p.nx, p.ny, p.nz, p.l_max, p.theta_points, p.phi_points) == (15, 15, 15, 4, 12, 12)
+    assert p.x_max == 0.08 and p.symmetry == bsl.SYM["Even"]
+    assert p.geometry_filename == b"cage_seed0.xyz"
+    assert p.ceiling_potential == 18.0 and p.rotational_constant == 0.709648713
+
+
+def test_parse_errors(bsl, tmp_path, in_case_dir):
+    with pytest.raises(bsl.BslError) as e:
+        bsl.parse_hv_input(str(tmp_path / "missing.txt"))
+    assert e.value.code == bsl.ERR_INPUT and "could not be opened" in str(e.value)
+    d, _, _ = in_case_dir("cpu_workload")
+    txt = open("hv_input.txt").read()
+    bad = tmp_path / "trunc.txt"
+    bad.write_text("\n".join(txt.split("\n")[:10]))
+    with pytest.raises(bsl.BslError) as e:
+        bsl.parse_hv_input(str(bad))
+    assert "truncated" in str(e.value)
+    sym = tmp_path / "sym.txt"
+    sym.write_text(txt.replace("rotationalSymmetry(All/Even/Odd)= Even", "rotationalSymmetry(All/Even/Odd)= Both"))
+    with pytest.raises(bsl.BslError) as e:
+        bsl.parse_hv_input(str(sym))
+    assert "Symmeterizer" in str(e.value)
+    big = tmp_path / "big.txt"
+    big.write_text(txt.replace("x_max(nm)= 0.08\n", "x_max(nm)= 0.5\n", 1))
+    with pytest.raises(bsl.BslError) as e:
+        bsl.parse_hv_input(str(big))
+    assert "potential universe" in str(e.value)
+    geo = tmp_path / "geo.txt"
+    geo.write_text(txt.replace("cage_seed0.xyz", "no_such_cage.xyz"))
+    with pytest.raises(bsl.BslError) as e:
+        bsl.parse_hv_input(str(geo))
+    assert "could not be opened" in str(e.value)
+    with pytest.raises(bsl.BslError):
+        bsl.hv_interface_setup("linRotCartSph_NoSuchCalculator")
+
+
+@pytest.mark.parametrize("name", ["cage11_n10_l3_all", "seed1_n6_l3_odd", "seed0_n5_l4_even", "iso_n20_l2_all",
+                                  "cpu_workload"])
+def test_tail_matches_oracle(bsl, name):
+    d, man, _ = case_info(name)
+    ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))
+    b = np.concatenate([[0.0], ref["beta"]])
+    ev, er = bsl.good_eigenvalues(ref["alpha"], b, b * b)
+    ev0, er0 = oracle_lancbis(ref["alpha"], b, b * b)
+    assert len(ev) == len(ev0)
+    assert np.array_equal(ev, ev0)
+    assert np.allclose(er, er0, rtol=1e-12, atol=1e-300)
+
+
+def test_tm_eigenvectors_match_oracle(bsl):
+    d, man, _ = case_info("seed1_n6_l3_odd")
+    ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))
+    a = ref["alpha"]
+    b = np.concatenate([[0.0], ref["beta"]])
+    ev, _ = bsl.good_eigenvalues(a, b, b * b)
+    ng = min(4, len(ev))
+    rows = bsl.tm_eigenvectors(a, b, b * b, ev[:ng])
+    L = load_oracle()
+    out = np.zeros(len(a) * ng)
+    L.orc_trivec(len(a), ptr(a), ptr(b), ptr(b * b), ptr(np.ascontiguousarray(ev[:ng])), ng, ptr(out))
+    assert np.allclose(rows.reshape(-1), out, rtol=0, atol=1e-14)
+    # eigenvector property on the leading block: T y = E y
+    for n in range(ng):
+        y = rows[n]
+        m = np.max(np.nonzero(np.abs(y) > 0)[0]) + 1
+        T = np.diag(a[:m]) + np.diag(b[1:m], 1) + np.diag(b[1:m], -1)
+        assert np.linalg.norm(T @ y[:m] - ev[n] * y[:m]) <= 1e-6 * max(1.0, abs(ev[n]))
+
+
+def test_tail_breakdown_free_on_tiny_matrix(bsl):
+    # 1x1 and 2x2 Lanczos matrices
+    a = np.array([1.5, -0.5])
+    b = np.array([0.0, 0.25, 0.1])
+    ev, er = bsl.good_eigenvalues(a, b, b * b, -10, 10)
+    w = np.linalg.eigvalsh(np.array([[1.5, 0.25], [0.25, -0.5]]))
+    for e in ev:
+        assert np.min(np.abs(w - e)) <= 1e-12
