@@ -261,7 +261,7 @@ int read_cage(const std::string& path, Cage* c) {
 namespace {
 
 void free_device(DeviceState& d) {
-  void* ptrs[] = {d.tx, d.ty, d.tz, d.tx_hi, d.tx_lo, d.ty_hi, d.ty_lo, d.tz_hi, d.tz_lo, d.rot,
+  void* ptrs[] = {d.tx, d.ty, d.tz, d.kx_head, d.ky_head, d.kz_head, d.kx_band, d.ky_band, d.kz_band, d.rot,
                   d.v1, d.v2, d.vb64, d.vb32, d.vec, d.rvec, d.ukin, d.partials, d.counter,
                   d.scalars, d.status, d.hist, d.ref_vec, d.ref_out, d.full_of, d.ritz};
   for (void* p : ptrs)
@@ -286,16 +286,6 @@ int upload(T** p, const std::vector<T>& host, const char* what) {
   if (rc) return rc;
   BSL_CUDA(cudaMemcpy(*p, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
   return BSL_OK;
-}
-
-// FP32 hi/lo split of a FP64 matrix: hi = fl32(T), lo = fl32(T - hi).
-void split32(const std::vector<double>& T, std::vector<float>* hi, std::vector<float>* lo) {
-  hi->resize(T.size());
-  lo->resize(T.size());
-  for (size_t i = 0; i < T.size(); ++i) {
-    (*hi)[i] = (float)T[i];
-    (*lo)[i] = (float)(T[i] - (double)(*hi)[i]);
-  }
 }
 
 int validate(const bsl_hv_params& p) {
@@ -436,31 +426,34 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
   std::vector<float> hi, lo;
   if ((rc = upload(&d.tx, t.tx, "Tx")) || (rc = upload(&d.ty, t.ty, "Ty")) || (rc = upload(&d.tz, t.tz, "Tz")))
     return bail(rc);
-  split32(t.tx, &hi, &lo);
-  if ((rc = upload(&d.tx_hi, hi, "Tx")) || (rc = upload(&d.tx_lo, lo, "Tx"))) return bail(rc);
-  split32(t.ty, &hi, &lo);
-  if ((rc = upload(&d.ty_hi, hi, "Ty")) || (rc = upload(&d.ty_lo, lo, "Ty"))) return bail(rc);
-  split32(t.tz, &hi, &lo);
-  if ((rc = upload(&d.tz_hi, hi, "Tz")) || (rc = upload(&d.tz_lo, lo, "Tz"))) return bail(rc);
+  kinetic_split_tables(t.tx, t.nx, true, &hi, &lo);
+  if ((rc = upload(&d.kx_head, hi, "Tx")) || (rc = upload(&d.kx_band, lo, "Tx"))) return bail(rc);
+  kinetic_split_tables(t.ty, t.ny, false, &hi, &lo);
+  if ((rc = upload(&d.ky_head, hi, "Ty")) || (rc = upload(&d.ky_band, lo, "Ty"))) return bail(rc);
+  kinetic_split_tables(t.tz, t.nz, false, &hi, &lo);
+  if ((rc = upload(&d.kz_head, hi, "Tz")) || (rc = upload(&d.kz_band, lo, "Tz"))) return bail(rc);
   if ((rc = upload(&d.rot, t.rot, "rotor"))) return bail(rc);
   if ((rc = upload(&d.full_of, t.full_of, "index map"))) return bail(rc);
   const size_t N = (size_t)t.npts, D = N * t.nn;
   const size_t ngrid = N * t.na * t.nb;
   const size_t ntri = (size_t)t.nn * (t.nn + 1) / 2;
+  const size_t tp = (size_t)vstream_tile_points(), tiled = (N + tp - 1) / tp * tp;
   if ((rc = dalloc(&d.v1, ngrid, "potential grid")) || (rc = dalloc(&d.v2, ngrid, "potential grid")) ||
-      (rc = dalloc(&d.vb64, ntri * N, "potential blocks")) || (rc = dalloc(&d.vb32, ntri * N, "potential blocks")) ||
+      (rc = dalloc(&d.vb64, ntri * N, "potential blocks")) || (rc = dalloc(&d.vb32, ntri * tiled, "potential blocks")) ||
       (rc = dalloc(&d.vec, D + 1, "Lanczos vector")) || (rc = dalloc(&d.rvec, D + 1, "Lanczos vector")) ||
       (rc = dalloc(&d.ukin, D, "kinetic work")))
     return bail(rc);
   d.red_blocks = 1024;
   // one partial per block of the widest reducing launch (the per-point potential apply)
-  const size_t nparts = std::max((size_t)d.red_blocks, (N + 255) / 256) + 64;
+  const size_t nparts = std::max((size_t)d.red_blocks, (N + 63) / 64) + 64;
   if ((rc = dalloc(&d.partials, nparts, "reduction scratch")) ||
       (rc = dalloc(&d.counter, 4, "reduction counter")) || (rc = dalloc(&d.scalars, 16, "scalars")) ||
       (rc = dalloc(&d.status, 4, "status")))
     return bail(rc);
   if ((e = cudaMemset(d.counter, 0, 4 * sizeof(unsigned int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
   if ((e = cudaMemset(d.status, 0, 4 * sizeof(int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
+  // zero the padding points of the last tile of the streamed FP32 blocks
+  if ((e = cudaMemset(d.vb32, 0, ntri * tiled * sizeof(float))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
   rc = (h->p.potential == BSL_POT_ALAVI_SPCE) ? dev_potential_alavi(h) : dev_potential_iso(h);
   if (rc) return bail(rc);
   if ((rc = dev_vblocks(h))) return bail(rc);

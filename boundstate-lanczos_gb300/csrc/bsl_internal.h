@@ -66,8 +66,9 @@ struct DeviceState {
   cudaStream_t stream = nullptr;
   // kinetic matrices: FP64 and the FP32 hi/lo split (T = hi + lo + O(2^-48))
   double *tx = nullptr, *ty = nullptr, *tz = nullptr;
-  float *tx_hi = nullptr, *tx_lo = nullptr, *ty_hi = nullptr, *ty_lo = nullptr, *tz_hi = nullptr,
-        *tz_lo = nullptr;
+  // FP32 heads (x transposed) and banded FP32 tails for the mixed kernels
+  float *kx_head = nullptr, *ky_head = nullptr, *kz_head = nullptr;
+  float *kx_band = nullptr, *ky_band = nullptr, *kz_band = nullptr;
   double* rot = nullptr;  // [nn]
   // potential grid V(p, a, b) for phi_b and 2pi - phi_b, p in vector order
   double *v1 = nullptr, *v2 = nullptr;
@@ -119,10 +120,18 @@ int dev_scatter_full(bsl_handle* h, const double* packed, double* full_accum, cu
 int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, int ngood, double* ritz,
                         cudaStream_t s);
 
+// mixed-precision kinetic (bsl_kinetic.cu)
+void kinetic_split_tables(const std::vector<double>& T, int n, bool transpose, std::vector<float>* head,
+                          std::vector<float>* band);
+int launch_kin_xy_mixed(bsl_handle* h, const double* v, cudaStream_t s);
+int launch_kin_z_mixed(bsl_handle* h, const double* v, cudaStream_t s);
+
 // potential-block apply (bsl_vapply_f32.cu / bsl_vapply_f64.cu)
+// FP32 blocks in the tile-major layout of bsl_vstream.cu (vstream_tile_points() points per tile)
 int launch_vapply_f32(const float* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
                       const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
-                      double* scalars, double* hist, int j, long long dpk);
+                      double* scalars, double* hist, int j, long long dpk, int* status);
+long long vstream_tile_points();
 int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
                       const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
                       double* scalars, double* hist, int j, long long dpk);

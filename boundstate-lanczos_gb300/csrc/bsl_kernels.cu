@@ -151,7 +151,7 @@ struct BlockTables {
 };
 
 __global__ void k_vblocks(BlockTables bt, const double* v1, const double* v2, long long npts, double* vb64,
-                          float* vb32) {
+                          float* vb32, long long tile_pts) {
   extern __shared__ double smem[];
   const int na = bt.na, nb = bt.nb, nab = na * nb;
   double* sV1 = smem;
@@ -194,7 +194,7 @@ __global__ void k_vblocks(BlockTables bt, const double* v1, const double* v2, lo
     double acc = 0.0;
     for (int a = 0; a < na; ++a) acc += bt.wa[a] * la[a] * lb[a] * sF[a * bt.nmtri + fi];
     vb64[(long long)t * npts + p] = acc;
-    vb32[(long long)t * npts + p] = (float)acc;
+    vb32[((p / tile_pts) * bt.ntri + t) * tile_pts + p % tile_pts] = (float)acc;
   }
 }
 
@@ -242,68 +242,6 @@ __global__ void k_kin_z_f64(const double* __restrict__ vec, double* __restrict__
     for (int q = 0; q < nz; ++q) az += __ldg(tr + q) * plane[q * nx + i];
     const long long o = sb + ((long long)k * ny + j) * nx + i;
     out[o] = az + out[o];
-  }
-}
-
-// Mixed precision: v rounded to FP32, each coefficient matrix split as
-// T = hi + lo (FP32 each).  hi.v and lo.v accumulate in FP32 separately and
-// are combined in FP64, so the FP32 rounding of the coefficients does not
-// reach the result and only the (random) rounding of v and of the sums does.
-__global__ void k_kin_xy_mixed(const double* __restrict__ vec, double* __restrict__ out,
-                               const float* __restrict__ txh, const float* __restrict__ txl,
-                               const float* __restrict__ tyh, const float* __restrict__ tyl, int nx, int ny, int nz) {
-  extern __shared__ float fplane[];
-  const int k = blockIdx.x, s = blockIdx.y;
-  const long long base = ((long long)s * nz + k) * ny * nx;
-  const int np = nx * ny;
-  for (int e = threadIdx.x; e < np; e += blockDim.x) fplane[e] = (float)vec[base + e];
-  __syncthreads();
-  for (int e = threadIdx.x; e < np; e += blockDim.x) {
-    const int j = e / nx, i = e - j * nx;
-    const float* row = fplane + j * nx;
-    const float* th = txh + (long long)i * nx;
-    const float* tl = txl + (long long)i * nx;
-    float xh = 0.f, xl = 0.f;
-    for (int q = 0; q < nx; ++q) {
-      const float pv = row[q];
-      xh = fmaf(__ldg(th + q), pv, xh);
-      xl = fmaf(__ldg(tl + q), pv, xl);
-    }
-    const float* uh = tyh + (long long)j * ny;
-    const float* ul = tyl + (long long)j * ny;
-    float yh = 0.f, yl = 0.f;
-    for (int q = 0; q < ny; ++q) {
-      const float pv = fplane[q * nx + i];
-      yh = fmaf(__ldg(uh + q), pv, yh);
-      yl = fmaf(__ldg(ul + q), pv, yl);
-    }
-    out[base + e] = ((double)yh + (double)yl) + ((double)xh + (double)xl);
-  }
-}
-
-__global__ void k_kin_z_mixed(const double* __restrict__ vec, double* __restrict__ out,
-                              const float* __restrict__ tzh, const float* __restrict__ tzl, int nx, int ny, int nz) {
-  extern __shared__ float fplane[];
-  const int j = blockIdx.x, s = blockIdx.y;
-  const long long sb = (long long)s * nz * ny * nx;
-  const int np = nx * nz;
-  for (int e = threadIdx.x; e < np; e += blockDim.x) {
-    const int k = e / nx, i = e - k * nx;
-    fplane[e] = (float)vec[sb + ((long long)k * ny + j) * nx + i];
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < np; e += blockDim.x) {
-    const int k = e / nx, i = e - k * nx;
-    const float* th = tzh + (long long)k * nz;
-    const float* tl = tzl + (long long)k * nz;
-    float zh = 0.f, zl = 0.f;
-    for (int q = 0; q < nz; ++q) {
-      const float pv = fplane[q * nx + i];
-      zh = fmaf(__ldg(th + q), pv, zh);
-      zl = fmaf(__ldg(tl + q), pv, zl);
-    }
-    const long long o = sb + ((long long)k * ny + j) * nx + i;
-    out[o] = ((double)zh + (double)zl) + out[o];
   }
 }
 
@@ -405,7 +343,7 @@ int launch_vapply(bsl_handle* h, const double* v, double* out, int mode, int j, 
   const long long dpk = N * t.nn;
   if (h->precision == BSL_PREC_MIXED)
     return launch_vapply_f32(d.vb32, g, s, t.nn, v, d.ukin, d.rot, out, N, mode, d.partials, d.counter, d.scalars,
-                             d.hist, j, dpk);
+                             d.hist, j, dpk, d.status);
   return launch_vapply_f64(d.vb64, g, s, t.nn, v, d.ukin, d.rot, out, N, mode, d.partials, d.counter, d.scalars,
                            d.hist, j, dpk);
 }
@@ -419,10 +357,9 @@ int launch_kinetic(bsl_handle* h, const double* v, cudaStream_t s) {
   if (sm_xy > 200 * 1024 || sm_z > 200 * 1024) return fail(BSL_ERR_UNSUPPORTED, "grid plane too large for one CTA");
   const dim3 gxy(t.nz, t.nn), gz(t.ny, t.nn);
   if (mixed) {
-    cudaFuncSetAttribute(k_kin_xy_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
-    cudaFuncSetAttribute(k_kin_z_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_z);
-    k_kin_xy_mixed<<<gxy, kThreads, sm_xy, s>>>(v, d.ukin, d.tx_hi, d.tx_lo, d.ty_hi, d.ty_lo, t.nx, t.ny, t.nz);
-    k_kin_z_mixed<<<gz, kThreads, sm_z, s>>>(v, d.ukin, d.tz_hi, d.tz_lo, t.nx, t.ny, t.nz);
+    int rc = launch_kin_xy_mixed(h, v, s);
+    if (!rc) rc = launch_kin_z_mixed(h, v, s);
+    return rc;
   } else {
     cudaFuncSetAttribute(k_kin_xy_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
     cudaFuncSetAttribute(k_kin_z_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_z);
@@ -559,7 +496,8 @@ int dev_vblocks(bsl_handle* h) {
     rc = fail(BSL_ERR_UNSUPPORTED, "angular quadrature too large for the block assembly kernel");
   } else {
     cudaFuncSetAttribute(k_vblocks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_vblocks<<<(unsigned)t.npts, kThreads, smem, d.stream>>>(bt, d.v1, d.v2, t.npts, d.vb64, d.vb32);
+    k_vblocks<<<(unsigned)t.npts, kThreads, smem, d.stream>>>(bt, d.v1, d.v2, t.npts, d.vb64, d.vb32,
+                                                               vstream_tile_points());
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(d.stream);
     if (e != cudaSuccess) rc = cuda_fail(e, "potential block assembly");
@@ -598,26 +536,26 @@ int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_
   const size_t esz = mixed ? sizeof(float) : sizeof(double);
   const size_t sm_xy = esz * t.nx * t.ny, sm_z = esz * t.nx * t.nz;
   const dim3 gxy(t.nz, t.nn), gz(t.ny, t.nn);
-  if (mixed) {
-    cudaFuncSetAttribute(k_kin_xy_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
-    cudaFuncSetAttribute(k_kin_z_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_z);
-  } else {
+  if (!mixed) {
     cudaFuncSetAttribute(k_kin_xy_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
     cudaFuncSetAttribute(k_kin_z_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_z);
   }
   cudaEventRecord(ev[0], s);
-  if (mixed)
-    k_kin_xy_mixed<<<gxy, kThreads, sm_xy, s>>>(d.vec, d.ukin, d.tx_hi, d.tx_lo, d.ty_hi, d.ty_lo, t.nx, t.ny, t.nz);
-  else
+  if (mixed) {
+    int rc = launch_kin_xy_mixed(h, d.vec, s);
+    if (rc) return rc;
+  } else {
     k_kin_xy_f64<<<gxy, kThreads, sm_xy, s>>>(d.vec, d.ukin, d.tx, d.ty, t.nx, t.ny, t.nz);
+  }
   cudaEventRecord(ev[1], s);
-  if (mixed)
-    k_kin_z_mixed<<<gz, kThreads, sm_z, s>>>(d.vec, d.ukin, d.tz_hi, d.tz_lo, t.nx, t.ny, t.nz);
-  else
+  if (mixed) {
+    int rc = launch_kin_z_mixed(h, d.vec, s);
+    if (rc) return rc;
+  } else {
     k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(d.vec, d.ukin, d.tz, t.nx, t.ny, t.nz);
+  }
   cudaEventRecord(ev[2], s);
-  int rc = launch_vapply(h, d.vec, d.rvec, 1, j, s);
-  if (rc) return rc;
+  if (int rc = launch_vapply(h, d.vec, d.rvec, 1, j, s)) return rc;
   cudaEventRecord(ev[3], s);
   const int g = d.red_blocks;
   k_update_beta<<<g, kThreads, 0, s>>>(d.vec, d.rvec, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j,
@@ -633,7 +571,7 @@ const char* dev_stage_name(bsl_handle* h, int i) {
   const bool mixed = h->precision == BSL_PREC_MIXED;
   static const char* n64[5] = {"k_kin_xy_f64", "k_kin_z_f64", "k_vapply<NN,double>", "k_update_beta",
                                "k_normalize_swap"};
-  static const char* nmx[5] = {"k_kin_xy_mixed", "k_kin_z_mixed", "k_vapply<NN,float>", "k_update_beta",
+  static const char* nmx[5] = {"k_kin_xy_split", "k_kin_z_split", "k_vapply<NN,float>", "k_update_beta",
                                "k_normalize_swap"};
   return mixed ? nmx[i] : n64[i];
 }
