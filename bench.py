@@ -170,8 +170,7 @@ def stage_bytes(cfg, D, N, nn, mixed):
     return [2 * D * 8,              # kinetic x/y: read v, write u_kin
             3 * D * 8,              # kinetic z: read v, read+write u_kin
             vb + 4 * D * 8,         # potential apply: blocks, v, u_kin, r (read+write)
-            3 * (D + 1) * 8,        # r -= alpha v, beta^2: read v, r; write r
-            4 * (D + 1) * 8]        # v <- r/beta, r <- -beta v: read 2, write 2
+            3 * (D + 1) * 8]        # r -= alpha v, beta^2: read v, r; write r (scales fold the swap)
 
 
 def levels_of(bsl, a, b, b2, count):
@@ -196,6 +195,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=200)
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--profile-iters", type=int, default=0,
+                    help="prep plus this many iterations only (for profiler captures)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -224,10 +226,18 @@ def main():
     torch.cuda.set_device(local)
     bsl = _load("boundstate_lanczos_gb300", os.path.join(PKG, "__init__.py"))
     t0 = time.perf_counter()
-    h = bsl.Hamiltonian(hv_path, "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE", precision="mixed", device=local)
+    h = bsl.Hamiltonian(hv_path, "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE", precision=args.precision, device=local)
     prep_s = time.perf_counter() - t0
     D, Df, nn = h.packed_size, h.basis_size, h.nn
     N = D // nn
+    if args.profile_iters:
+        # short run for profilers: prep, then the given number of iterations only
+        h.lanczos(args.profile_iters)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_iters": args.profile_iters, "ms_per_iter": h.last_ms_per_iter(),
+                          "precision": args.precision}))
+        h.close()
+        return
 
     def barrier():
         torch.cuda.synchronize()
@@ -255,8 +265,10 @@ def main():
     names = (C.c_char_p * 5)()
     bsl.lib().bsl_stage_times.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_void_p]
     rc = bsl.lib().bsl_stage_times(h.handle, 200, stage_ms.ctypes.data_as(C.POINTER(C.c_double)), names)
-    stage_names = [n.decode() for n in names] if rc == 0 else []
-    sb = stage_bytes(cfg, D, N, nn, True)
+    nst = bsl.lib().bsl_launches_per_iteration(h.handle)
+    stage_names = [names[i].decode() for i in range(nst)] if rc == 0 else []
+    stage_ms = stage_ms[:nst]
+    sb = stage_bytes(cfg, D, N, nn, True)[:nst]
     peak, peak_src = measured_peak_hbm()
     dom = int(np.argmax(stage_ms))
     achieved = sb[dom] / (stage_ms[dom] * 1e-3) / 1e9
@@ -286,6 +298,7 @@ def main():
     h.lanczos(args.fp64_steps)
     fp64_ms = h.last_ms_per_iter()
     fp64_stage = np.zeros(5)
+    bsl.lib().bsl_launches_per_iteration.argtypes = [C.c_void_p]
     bsl.lib().bsl_stage_times(h.handle, 20, fp64_stage.ctypes.data_as(C.POINTER(C.c_double)), None)
 
     # ---- level accuracy: mixed vs FP64 at the same iteration count ----
@@ -297,10 +310,28 @@ def main():
         am, bm, bm2 = h.lanczos(n_it, start="normal", seed=0)
         ref_levels = np.sort(stable_levels(bsl, a64, b64, b264))[:cfg["levels"]]
         evm, _ = bsl.good_eigenvalues(am, bm, bm2, -1.0e3, 1.0e3)
+        stable_m = stable_levels(bsl, am, bm, bm2)
         dev = np.array([np.min(np.abs(evm - e)) for e in ref_levels]) * KJ_TO_CM if len(evm) else np.array([])
+        dev_s = (np.array([np.min(np.abs(stable_m - e)) for e in ref_levels]) * KJ_TO_CM
+                 if len(stable_m) else np.array([]))
+        worst = int(np.argmax(dev)) if len(dev) else -1
         acc = {"iterations": n_it, "levels_compared": int(len(ref_levels)),
                "max_abs_dE_cm-1": float(dev.max()) if len(dev) else None,
+               "median_abs_dE_cm-1": float(np.median(dev)) if len(dev) else None,
+               "worst_level_kJ_mol": float(ref_levels[worst]) if worst >= 0 else None,
+               "dE_cm-1_per_level": [float("%.3g" % x) for x in dev],
+               "max_abs_dE_vs_mixed_stable_cm-1": float(dev_s.max()) if len(dev_s) else None,
+               "min_level_gap_cm-1": float(np.min(np.diff(ref_levels)) * KJ_TO_CM) if len(ref_levels) > 1 else None,
                "lowest_levels_kJ_mol": [float(x) for x in ref_levels[:5]], "start": "normal seed 0"}
+        # one H v at full size, mixed against FP64
+        vr = np.random.default_rng(3).standard_normal(Df)
+        u64 = np.zeros(Df)
+        um = np.zeros(Df)
+        h.set_precision("fp64")
+        h.hv(vr, u64)
+        h.set_precision("mixed")
+        h.hv(vr, um)
+        acc["hv_rel_err_mixed_vs_fp64"] = float(np.max(np.abs(um - u64)) / np.max(np.abs(u64)))
     h.close()
 
     cb = cpu_baseline(cfg, budget_s=args.cpu_budget) if rank == 0 else None
@@ -324,10 +355,10 @@ def main():
                                "frac": it_bytes / (ms_step * 1e-3) / 1e9 / world / peak},
         "stages_ms": dict(zip(stage_names, [float(x) for x in stage_ms])),
         "fp64": {"value": 1000.0 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
-                 "stages_ms": [float(x) for x in fp64_stage], "speedup_mixed_vs_fp64": fp64_ms / (ms_step)},
+                 "stages_ms": [float(x) for x in fp64_stage[:nst]], "speedup_mixed_vs_fp64": fp64_ms / (ms_step)},
         "accuracy": acc,
         "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "clocks": clocks, "gpu_launches": 5 * args.steps, "prep_seconds": prep_s,
+        "clocks": clocks, "gpu_launches": nst * args.steps, "prep_seconds": prep_s,
         "wall_ms_per_step": 1000.0 * wall / args.steps,
     }
     print(json.dumps(line))

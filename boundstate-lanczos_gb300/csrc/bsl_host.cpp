@@ -443,7 +443,7 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
       (rc = dalloc(&d.vec, D + 1, "Lanczos vector")) || (rc = dalloc(&d.rvec, D + 1, "Lanczos vector")) ||
       (rc = dalloc(&d.ukin, D, "kinetic work")))
     return bail(rc);
-  d.red_blocks = 1024;
+  d.red_blocks = 1216;
   // one partial per block of the widest reducing launch (the per-point potential apply)
   const size_t nparts = std::max((size_t)d.red_blocks, (N + 63) / 64) + 64;
   if ((rc = dalloc(&d.partials, nparts, "reduction scratch")) ||

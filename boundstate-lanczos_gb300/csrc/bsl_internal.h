@@ -66,9 +66,10 @@ struct DeviceState {
   cudaStream_t stream = nullptr;
   // kinetic matrices: FP64 and the FP32 hi/lo split (T = hi + lo + O(2^-48))
   double *tx = nullptr, *ty = nullptr, *tz = nullptr;
-  // FP32 heads (x transposed) and banded FP32 tails for the mixed kernels
+  // FP32 heads fl32(T) and tails fl32(T - head), both stored transposed, for the mixed kernels
   float *kx_head = nullptr, *ky_head = nullptr, *kz_head = nullptr;
   float *kx_band = nullptr, *ky_band = nullptr, *kz_band = nullptr;
+  int kin_grid_xy = 0, kin_grid_z = 0;  // persistent grid sizes
   double* rot = nullptr;  // [nn]
   // potential grid V(p, a, b) for phi_b and 2pi - phi_b, p in vector order
   double *v1 = nullptr, *v2 = nullptr;
@@ -79,7 +80,7 @@ struct DeviceState {
   double *vec = nullptr, *rvec = nullptr, *ukin = nullptr;
   double* partials = nullptr;  // one double per reduction block
   unsigned int* counter = nullptr;
-  double* scalars = nullptr;   // [0] alpha_j, [1] beta_j, [2] beta2_j, [3] 1/beta_j
+  double* scalars = nullptr;   // [0] alpha_j, [1] beta_j, [2] beta2_j, [3] 1/beta_j, [4] sv, [5] sr
   int* status = nullptr;       // non-zero after a breakdown
   double* hist = nullptr;      // alpha/beta/beta2 history [3][niter+1]
   int hist_cap = 0;
@@ -100,6 +101,8 @@ struct bsl_handle {
   bsl::DeviceState d;
   int precision = BSL_PREC_FP64;
   double last_ms_per_iter = 0.0;
+  int lanczos_flip = 0;           // 0: vec holds v_j and rvec r_j; 1: roles swapped
+  double init_scalars[8] = {0, 0, 0, 0, 1, 1, 0, 0};  // alpha, beta, beta2, 1/beta, sv, sr
 };
 
 namespace bsl {

@@ -299,6 +299,50 @@ __global__ void k_normalize_swap(double* __restrict__ v, double* __restrict__ r,
   }
 }
 
+// Folded-scale update of the packed loop: the buffers hold v = sv * V and
+// r' = R (scale 1 after the potential apply).  r' -= alpha v, beta^2 = r'.r';
+// the last block then records beta and sets the scales of the next iteration,
+// whose V is this R (v_{j+1} = r'/beta) and whose R is this V
+// (r_{j+1} = -beta v_j = -beta sv V), so no pass rescales or swaps memory.
+__global__ void k_update_fold(const double* __restrict__ V, double* __restrict__ R, long long L, double* partials,
+                              unsigned int* counter, double* scalars, double* hist, int hist_stride, int j,
+                              int* status) {
+  const double alpha = scalars[0], sv = scalars[4];
+  const double a = alpha * sv;
+  double acc = 0.0;
+  const long long L2 = L / 2;
+  const double2* V2 = reinterpret_cast<const double2*>(V);
+  double2* R2 = reinterpret_cast<double2*>(R);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L2; i += (long long)gridDim.x * blockDim.x) {
+    const double2 v = V2[i];
+    double2 r = R2[i];
+    r.x = r.x - a * v.x;
+    r.y = r.y - a * v.y;
+    R2[i] = r;
+    acc += r.x * r.x + r.y * r.y;
+  }
+  if ((L & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const double x = R[L - 1] - a * V[L - 1];
+    R[L - 1] = x;
+    acc += x * x;
+  }
+  double total;
+  if (reduce_grid(acc, partials, counter, &total) && threadIdx.x == 0) {
+    const double b = sqrt(total);
+    scalars[1] = b;
+    scalars[2] = total;
+    scalars[3] = 1. / b;
+    hist[hist_stride + j] = b;
+    hist[2 * hist_stride + j] = total;
+    scalars[4] = 1. / b;    // next v = R / beta
+    scalars[5] = -b * sv;   // next r = -beta v_j = (-beta sv) V
+    if (!(b > 0.0) || !isfinite(b) || !isfinite(alpha)) {
+      if (status[0] == 0) status[1] = j;
+      status[0] = 1;
+    }
+  }
+}
+
 __global__ void k_fill(double* x, long long L, double val) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x)
     x[i] = val;
@@ -325,11 +369,13 @@ __global__ void k_scatter_add(const double* __restrict__ packed, double* __restr
   full[o] = full[o] + packed[e];
 }
 
-// ritz[n*D + i] += coef[n] * v[i] for active n
-__global__ void k_ritz(const double* __restrict__ v, long long D, const double* __restrict__ coef,
-                       const int* __restrict__ active, int ngood, double* __restrict__ ritz) {
+// ritz[n*D + i] += coef[n] * v[i] for active n, v = scalars[4] * V
+__global__ void k_ritz(const double* __restrict__ V, long long D, const double* __restrict__ coef,
+                       const int* __restrict__ active, int ngood, double* __restrict__ ritz,
+                       const double* __restrict__ scalars) {
+  const double sv = scalars[4];
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (long long)gridDim.x * blockDim.x) {
-    const double vi = v[i];
+    const double vi = sv * V[i];
     for (int n = 0; n < ngood; ++n)
       if (active[n]) ritz[(long long)n * D + i] += coef[n] * vi;
   }
@@ -516,14 +562,15 @@ int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s) {
 int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s) {
   DeviceState& d = h->d;
   const long long L = bsl_packed_size(h) + 1;  // + the coordinate outside the symmetry block
-  int rc = launch_kinetic(h, d.vec, s);
+  double* V = h->lanczos_flip ? d.rvec : d.vec;
+  double* R = h->lanczos_flip ? d.vec : d.rvec;
+  int rc = launch_kinetic(h, V, s);
   if (rc) return rc;
-  if ((rc = launch_vapply(h, d.vec, d.rvec, 1, j, s))) return rc;
-  const int g = d.red_blocks;
-  k_update_beta<<<g, kThreads, 0, s>>>(d.vec, d.rvec, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j,
-                                       d.status);
-  k_normalize_swap<<<g, kThreads, 0, s>>>(d.vec, d.rvec, L, d.scalars);
+  if ((rc = launch_vapply(h, V, R, 1, j, s))) return rc;
+  k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j,
+                                                  d.status);
   BSL_CUDA(cudaGetLastError());
+  h->lanczos_flip ^= 1;
   return BSL_OK;
 }
 
@@ -533,46 +580,42 @@ int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_
   const Tables& t = h->t;
   const long long L = bsl_packed_size(h) + 1;
   const bool mixed = h->precision == BSL_PREC_MIXED;
-  const size_t esz = mixed ? sizeof(float) : sizeof(double);
-  const size_t sm_xy = esz * t.nx * t.ny, sm_z = esz * t.nx * t.nz;
+  double* V = h->lanczos_flip ? d.rvec : d.vec;
+  double* R = h->lanczos_flip ? d.vec : d.rvec;
+  const size_t sm_xy = sizeof(double) * t.nx * t.ny, sm_z = sizeof(double) * t.nx * t.nz;
   const dim3 gxy(t.nz, t.nn), gz(t.ny, t.nn);
   if (!mixed) {
     cudaFuncSetAttribute(k_kin_xy_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
     cudaFuncSetAttribute(k_kin_z_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_z);
   }
+  int rc;
   cudaEventRecord(ev[0], s);
   if (mixed) {
-    int rc = launch_kin_xy_mixed(h, d.vec, s);
-    if (rc) return rc;
+    if ((rc = launch_kin_xy_mixed(h, V, s))) return rc;
   } else {
-    k_kin_xy_f64<<<gxy, kThreads, sm_xy, s>>>(d.vec, d.ukin, d.tx, d.ty, t.nx, t.ny, t.nz);
+    k_kin_xy_f64<<<gxy, kThreads, sm_xy, s>>>(V, d.ukin, d.tx, d.ty, t.nx, t.ny, t.nz);
   }
   cudaEventRecord(ev[1], s);
   if (mixed) {
-    int rc = launch_kin_z_mixed(h, d.vec, s);
-    if (rc) return rc;
+    if ((rc = launch_kin_z_mixed(h, V, s))) return rc;
   } else {
-    k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(d.vec, d.ukin, d.tz, t.nx, t.ny, t.nz);
+    k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(V, d.ukin, d.tz, t.nx, t.ny, t.nz);
   }
   cudaEventRecord(ev[2], s);
-  if (int rc = launch_vapply(h, d.vec, d.rvec, 1, j, s)) return rc;
+  if ((rc = launch_vapply(h, V, R, 1, j, s))) return rc;
   cudaEventRecord(ev[3], s);
-  const int g = d.red_blocks;
-  k_update_beta<<<g, kThreads, 0, s>>>(d.vec, d.rvec, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j,
-                                       d.status);
+  k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j,
+                                                  d.status);
   cudaEventRecord(ev[4], s);
-  k_normalize_swap<<<g, kThreads, 0, s>>>(d.vec, d.rvec, L, d.scalars);
-  cudaEventRecord(ev[5], s);
   BSL_CUDA(cudaGetLastError());
+  h->lanczos_flip ^= 1;
   return BSL_OK;
 }
 
 const char* dev_stage_name(bsl_handle* h, int i) {
   const bool mixed = h->precision == BSL_PREC_MIXED;
-  static const char* n64[5] = {"k_kin_xy_f64", "k_kin_z_f64", "k_vapply<NN,double>", "k_update_beta",
-                               "k_normalize_swap"};
-  static const char* nmx[5] = {"k_kin_xy_split", "k_kin_z_split", "k_vapply<NN,float>", "k_update_beta",
-                               "k_normalize_swap"};
+  static const char* n64[4] = {"k_kin_xy_f64", "k_kin_z_f64", "k_vapply<NN,double>", "k_update_fold"};
+  static const char* nmx[4] = {"k_kin_xy_split", "k_kin_z_split", "k_vstream<NN>", "k_update_fold"};
   return mixed ? nmx[i] : n64[i];
 }
 
@@ -610,7 +653,8 @@ int dev_full_step(bsl_handle* h, double* v, double* r, long long L, int j, cudaS
 int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, int ngood, double* ritz,
                         cudaStream_t s) {
   const long long L = bsl_packed_size(h) + 1;  // with the coordinate outside the symmetry block
-  k_ritz<<<1024, kThreads, 0, s>>>(h->d.vec, L, coef, active, ngood, ritz);
+  const double* V = h->lanczos_flip ? h->d.rvec : h->d.vec;
+  k_ritz<<<1024, kThreads, 0, s>>>(V, L, coef, active, ngood, ritz, h->d.scalars);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }

@@ -9,31 +9,51 @@
 // contraction and the tail contraction accumulate in separate FP32 registers
 // and are combined in FP64, so the FP32 rounding of the coefficients (a
 // systematic shift of every level, several 1e-3 cm^-1 at dx = 0.015 A) does
-// not reach the result.  The tail is applied on the band |i - i'| <= kBand;
-// beyond it |T_lo| < 2^-24 |T_ii'| with |T_ii'| = c 2/(i-i')^2 <= c/40.
+// not reach the result; only the random rounding of v and of the FP32 sums
+// does.
 //
-// Work decomposition: one CTA owns one plane at a time (persistent over
-// planes): the (y, x) plane of fixed (s, z) for the x and y contractions and
-// the (z, x) plane of fixed (s, y) for the z contraction.  Each plane
-// contraction is a small dense GEMM out = A * B (A or B the plane), done with
-// 4 x 4 register tiles from shared memory; the coefficient matrices stay in
-// shared memory for the CTA's lifetime.
+// Work decomposition: persistent CTAs, one plane at a time: the (y, x) plane
+// of fixed (s, z) for the x and y contractions and the (z, x) plane of fixed
+// (s, y) for the z contraction.  Each plane contraction is a dense GEMM
+// (n x n coefficients times an n x n plane) with 4 x 4 register tiles.  Both
+// GEMM operands are read from shared memory as float4 along the output
+// index they own: the plane is kept row-major (x innermost) and transposed
+// (for the x contraction's left operand), the coefficient matrices in the
+// orientation each product needs, so a thread issues 6 128-bit shared loads
+// per 64 FMAs and the loop is FMA-bound.
 #include "bsl_device.cuh"
 
 namespace bsl {
 namespace {
 
-constexpr int kBand = 8;
-constexpr int kBandW = 2 * kBand + 1;
-
 __host__ __device__ inline int round4(int n) { return (n + 3) & ~3; }
 
+// plane elements held per thread for the next plane: ceil(64*64 / 256)
+constexpr int kPrefetch = 16;
+
 struct KinMixed {
-  const float* ta;   // x/y kernel: Tx_hi transposed [nxp][nxp]; z kernel: Tz_hi [nzp][nzp]
-  const float* tb;   // x/y kernel: Ty_hi [nyp][nyp]
-  const float* la;   // tails on the band: [kBandW][n], la[d][i] = T_lo[i][i + d - kBand]
-  const float* lb;
+  // x/y kernel: a_hi/a_lo = Tx^T [q][i] (x right operand), b_hi/b_lo = Ty^T [q][j] (y left operand)
+  // z kernel:   a_hi/a_lo = Tz^T [q][k]
+  const float *a_hi, *a_lo, *b_hi, *b_lo;
 };
+
+__device__ __forceinline__ void fma4x4(float (&acc)[4][4], const float4 a, const float4 b) {
+  const float av[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    acc[r][0] = fmaf(av[r], b.x, acc[r][0]);
+    acc[r][1] = fmaf(av[r], b.y, acc[r][1]);
+    acc[r][2] = fmaf(av[r], b.z, acc[r][2]);
+    acc[r][3] = fmaf(av[r], b.w, acc[r][3]);
+  }
+}
+
+__device__ __forceinline__ void zero(float (&acc)[4][4]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[r][c] = 0.f;
+}
 
 // x and y: out[s][k][j][i] = (Tx v)(i) + (Ty v)(j) on the plane of fixed (s, k)
 __global__ void __launch_bounds__(256) k_kin_xy_split(const double* __restrict__ vec, double* __restrict__ out,
@@ -41,73 +61,74 @@ __global__ void __launch_bounds__(256) k_kin_xy_split(const double* __restrict__
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   const int nxp = round4(nx), nyp = round4(ny);
-  const int ps = nxp + 4;  // plane row stride (floats), keeps float4 alignment
-  float* P = sm;                    // [nyp][ps]
-  float* TX = P + nyp * ps;         // [nxp][nxp]   TX[q][i] = Tx_hi[i][q]
-  float* TY = TX + nxp * nxp;       // [nyp][nyp]   TY[j][q] = Ty_hi[j][q]
-  float* LX = TY + nyp * nyp;       // [kBandW][nxp]
-  float* LY = LX + kBandW * nxp;    // [kBandW][nyp]
-  for (int e = threadIdx.x; e < nxp * nxp; e += blockDim.x) TX[e] = km.ta[e];
-  for (int e = threadIdx.x; e < nyp * nyp; e += blockDim.x) TY[e] = km.tb[e];
-  for (int e = threadIdx.x; e < kBandW * nxp; e += blockDim.x) LX[e] = km.la[e];
-  for (int e = threadIdx.x; e < kBandW * nyp; e += blockDim.x) LY[e] = km.lb[e];
+  float* P = sm;                  // [nyp][nxp]  P[j][i]
+  float* PT = P + nyp * nxp;      // [nxp][nyp]  PT[i][j]
+  float* XH = PT + nxp * nyp;     // [nxp][nxp]  XH[q][i] = Tx_hi[i][q]
+  float* XL = XH + nxp * nxp;
+  float* YH = XL + nxp * nxp;     // [nyp][nyp]  YH[q][j] = Ty_hi[j][q]
+  float* YL = YH + nyp * nyp;
+  for (int e = threadIdx.x; e < nxp * nxp; e += blockDim.x) {
+    XH[e] = km.a_hi[e];
+    XL[e] = km.a_lo[e];
+  }
+  for (int e = threadIdx.x; e < nyp * nyp; e += blockDim.x) {
+    YH[e] = km.b_hi[e];
+    YL[e] = km.b_lo[e];
+  }
   const int tcols = nxp / 4;
   const int tx = threadIdx.x % tcols, ty = threadIdx.x / tcols;
   const bool active = ty < nyp / 4;
   const int i0 = 4 * tx, j0 = 4 * ty;
+  const int npl = nyp * nxp;
+  // the next plane is loaded into registers while the current one is computed
+  double pre[kPrefetch];
+  auto load = [&](int plane) {
+    const int k = plane % nz, s = plane / nz;
+    const long long base = ((long long)s * nz + k) * ny * nx;
+#pragma unroll
+    for (int u = 0; u < kPrefetch; ++u) {
+      const int e = threadIdx.x + u * blockDim.x;
+      const int j = e / nxp, i = e - j * nxp;
+      pre[u] = (e < npl && j < ny && i < nx) ? vec[base + (long long)j * nx + i] : 0.0;
+    }
+  };
+  if (blockIdx.x < nplanes) load(blockIdx.x);
   for (int plane = blockIdx.x; plane < nplanes; plane += gridDim.x) {
     const int k = plane % nz, s = plane / nz;
     const long long base = ((long long)s * nz + k) * ny * nx;
     __syncthreads();
-    for (int e = threadIdx.x; e < nyp * nxp; e += blockDim.x) {
-      const int j = e / nxp, i = e - j * nxp;
-      P[j * ps + i] = (j < ny && i < nx) ? (float)vec[base + (long long)j * nx + i] : 0.f;
+#pragma unroll
+    for (int u = 0; u < kPrefetch; ++u) {
+      const int e = threadIdx.x + u * blockDim.x;
+      if (e < npl) {
+        const int j = e / nxp, i = e - j * nxp;
+        const float x = (float)pre[u];
+        P[e] = x;
+        PT[i * nyp + j] = x;
+      }
     }
     __syncthreads();
+    if (plane + (int)gridDim.x < nplanes) load(plane + gridDim.x);
     if (!active) continue;
-    float ax[4][4], ay[4][4], al[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) ax[r][c] = ay[r][c] = al[r][c] = 0.f;
-    // x: out[j][i] = sum_q P[j][q] TX[q][i]
+    float xh[4][4], xl[4][4], yh[4][4], yl[4][4];
+    zero(xh);
+    zero(xl);
+    zero(yh);
+    zero(yl);
+    // x: out[j][i] = sum_q P[j][q] Tx[i][q] = sum_q PT[q][j] XH[q][i]
+#pragma unroll 2
     for (int q = 0; q < nx; ++q) {
-      const float4 b = *reinterpret_cast<const float4*>(TX + q * nxp + i0);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const float a = P[(j0 + r) * ps + q];
-        ax[r][0] = fmaf(a, b.x, ax[r][0]);
-        ax[r][1] = fmaf(a, b.y, ax[r][1]);
-        ax[r][2] = fmaf(a, b.z, ax[r][2]);
-        ax[r][3] = fmaf(a, b.w, ax[r][3]);
-      }
+      const float4 a = *reinterpret_cast<const float4*>(PT + q * nyp + j0);
+      fma4x4(xh, a, *reinterpret_cast<const float4*>(XH + q * nxp + i0));
+      fma4x4(xl, a, *reinterpret_cast<const float4*>(XL + q * nxp + i0));
     }
-    // y: out[j][i] = sum_q TY[j][q] P[q][i]
+    // y: out[j][i] = sum_q Ty[j][q] P[q][i] = sum_q YH[q][j] P[q][i]
+#pragma unroll 2
     for (int q = 0; q < ny; ++q) {
-      const float4 b = *reinterpret_cast<const float4*>(P + q * ps + i0);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const float a = TY[(j0 + r) * nyp + q];
-        ay[r][0] = fmaf(a, b.x, ay[r][0]);
-        ay[r][1] = fmaf(a, b.y, ay[r][1]);
-        ay[r][2] = fmaf(a, b.z, ay[r][2]);
-        ay[r][3] = fmaf(a, b.w, ay[r][3]);
-      }
+      const float4 b = *reinterpret_cast<const float4*>(P + q * nxp + i0);
+      fma4x4(yh, *reinterpret_cast<const float4*>(YH + q * nyp + j0), b);
+      fma4x4(yl, *reinterpret_cast<const float4*>(YL + q * nyp + j0), b);
     }
-    // tails on the band (both axes share one accumulator: they are 2^-24 small)
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const int j = j0 + r, i = i0 + c;
-        float acc = 0.f;
-        for (int d = 0; d < kBandW; ++d) {
-          const int qi = i + d - kBand, qj = j + d - kBand;
-          if (qi >= 0 && qi < nx) acc = fmaf(LX[d * nxp + i], P[j * ps + qi], acc);
-          if (qj >= 0 && qj < ny) acc = fmaf(LY[d * nyp + j], P[qj * ps + i], acc);
-        }
-        al[r][c] = acc;
-      }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const int j = j0 + r;
@@ -115,7 +136,9 @@ __global__ void __launch_bounds__(256) k_kin_xy_split(const double* __restrict__
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const int i = i0 + c;
-        if (i < nx) out[base + (long long)j * nx + i] = ((double)ay[r][c] + (double)ax[r][c]) + (double)al[r][c];
+        if (i < nx)
+          out[base + (long long)j * nx + i] =
+              ((double)yh[r][c] + (double)yl[r][c]) + ((double)xh[r][c] + (double)xl[r][c]);
       }
     }
   }
@@ -127,42 +150,51 @@ __global__ void __launch_bounds__(256) k_kin_z_split(const double* __restrict__ 
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   const int nxp = round4(nx), nzp = round4(nz);
-  const int ps = nxp + 4;
-  float* P = sm;                  // [nzp][ps]   P[k][i]
-  float* TZ = P + nzp * ps;       // [nzp][nzp]  TZ[k][q] = Tz_hi[k][q]
-  float* LZ = TZ + nzp * nzp;     // [kBandW][nzp]
-  for (int e = threadIdx.x; e < nzp * nzp; e += blockDim.x) TZ[e] = km.ta[e];
-  for (int e = threadIdx.x; e < kBandW * nzp; e += blockDim.x) LZ[e] = km.la[e];
+  float* P = sm;                  // [nzp][nxp]  P[k][i]
+  float* ZH = P + nzp * nxp;      // [nzp][nzp]  ZH[q][k] = Tz_hi[k][q]
+  float* ZL = ZH + nzp * nzp;
+  for (int e = threadIdx.x; e < nzp * nzp; e += blockDim.x) {
+    ZH[e] = km.a_hi[e];
+    ZL[e] = km.a_lo[e];
+  }
   const int tcols = nxp / 4;
   const int tx = threadIdx.x % tcols, ty = threadIdx.x / tcols;
   const bool active = ty < nzp / 4;
   const int i0 = 4 * tx, k0 = 4 * ty;
   const long long plane_stride = (long long)ny * nx;
+  const int npl = nzp * nxp;
+  double pre[kPrefetch];
+  auto load = [&](int plane) {
+    const int j = plane % ny, s = plane / ny;
+    const long long sb = (long long)s * nz * plane_stride + (long long)j * nx;
+#pragma unroll
+    for (int u = 0; u < kPrefetch; ++u) {
+      const int e = threadIdx.x + u * blockDim.x;
+      const int k = e / nxp, i = e - k * nxp;
+      pre[u] = (e < npl && k < nz && i < nx) ? vec[sb + k * plane_stride + i] : 0.0;
+    }
+  };
+  if (blockIdx.x < nplanes) load(blockIdx.x);
   for (int plane = blockIdx.x; plane < nplanes; plane += gridDim.x) {
     const int j = plane % ny, s = plane / ny;
     const long long sb = (long long)s * nz * plane_stride + (long long)j * nx;
     __syncthreads();
-    for (int e = threadIdx.x; e < nzp * nxp; e += blockDim.x) {
-      const int k = e / nxp, i = e - k * nxp;
-      P[k * ps + i] = (k < nz && i < nx) ? (float)vec[sb + k * plane_stride + i] : 0.f;
+#pragma unroll
+    for (int u = 0; u < kPrefetch; ++u) {
+      const int e = threadIdx.x + u * blockDim.x;
+      if (e < npl) P[e] = (float)pre[u];
     }
     __syncthreads();
+    if (plane + (int)gridDim.x < nplanes) load(plane + gridDim.x);
     if (!active) continue;
-    float az[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) az[r][c] = 0.f;
+    float zh[4][4], zl[4][4];
+    zero(zh);
+    zero(zl);
+#pragma unroll 2
     for (int q = 0; q < nz; ++q) {
-      const float4 b = *reinterpret_cast<const float4*>(P + q * ps + i0);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const float a = TZ[(k0 + r) * nzp + q];
-        az[r][0] = fmaf(a, b.x, az[r][0]);
-        az[r][1] = fmaf(a, b.y, az[r][1]);
-        az[r][2] = fmaf(a, b.z, az[r][2]);
-        az[r][3] = fmaf(a, b.w, az[r][3]);
-      }
+      const float4 b = *reinterpret_cast<const float4*>(P + q * nxp + i0);
+      fma4x4(zh, *reinterpret_cast<const float4*>(ZH + q * nzp + k0), b);
+      fma4x4(zl, *reinterpret_cast<const float4*>(ZL + q * nzp + k0), b);
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -172,13 +204,8 @@ __global__ void __launch_bounds__(256) k_kin_z_split(const double* __restrict__ 
       for (int c = 0; c < 4; ++c) {
         const int i = i0 + c;
         if (i >= nx) continue;
-        float acc = 0.f;
-        for (int d = 0; d < kBandW; ++d) {
-          const int qk = k + d - kBand;
-          if (qk >= 0 && qk < nz) acc = fmaf(LZ[d * nzp + k], P[qk * ps + i], acc);
-        }
         const long long o = sb + k * plane_stride + i;
-        out[o] = ((double)az[r][c] + (double)acc) + out[o];
+        out[o] = ((double)zh[r][c] + (double)zl[r][c]) + out[o];
       }
     }
   }
@@ -186,29 +213,38 @@ __global__ void __launch_bounds__(256) k_kin_z_split(const double* __restrict__ 
 
 size_t smem_xy(int nx, int ny) {
   const int nxp = round4(nx), nyp = round4(ny);
-  return sizeof(float) * ((size_t)nyp * (nxp + 4) + (size_t)nxp * nxp + (size_t)nyp * nyp + kBandW * (nxp + nyp));
+  return sizeof(float) * (2 * (size_t)nyp * nxp + 2 * (size_t)nxp * nxp + 2 * (size_t)nyp * nyp);
 }
 size_t smem_z(int nx, int nz) {
   const int nxp = round4(nx), nzp = round4(nz);
-  return sizeof(float) * ((size_t)nzp * (nxp + 4) + (size_t)nzp * nzp + kBandW * nzp);
+  return sizeof(float) * ((size_t)nzp * nxp + 2 * (size_t)nzp * nzp);
+}
+
+int persistent_grid(const void* kernel, int threads, size_t smem, int nplanes) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  const int g = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  return nplanes < g ? nplanes : g;
 }
 
 }  // namespace
 
-// Host-side coefficient layouts for the kernels above.
+// Host-side coefficient layouts: transposed FP32 head and tail, [q][i] = T[i][q],
+// zero-padded to a multiple of 4.
 void kinetic_split_tables(const std::vector<double>& T, int n, bool transpose, std::vector<float>* head,
-                          std::vector<float>* band) {
+                          std::vector<float>* tail) {
+  (void)transpose;  // every operand above is stored transposed
   const int np = round4(n);
   head->assign((size_t)np * np, 0.f);
-  band->assign((size_t)kBandW * np, 0.f);
+  tail->assign((size_t)np * np, 0.f);
   for (int i = 0; i < n; ++i)
     for (int q = 0; q < n; ++q) {
       const double t = T[(size_t)i * n + q];
       const float hi = (float)t;
-      if (transpose) (*head)[(size_t)q * np + i] = hi;
-      else (*head)[(size_t)i * np + q] = hi;
-      const int d = q - i + kBand;
-      if (d >= 0 && d < kBandW) (*band)[(size_t)d * np + i] = (float)(t - (double)hi);
+      (*head)[(size_t)q * np + i] = hi;
+      (*tail)[(size_t)q * np + i] = (float)(t - (double)hi);
     }
 }
 
@@ -216,7 +252,10 @@ int kinetic_mixed_supported(int nx, int ny, int nz, size_t* sxy, size_t* sz) {
   *sxy = smem_xy(nx, ny);
   *sz = smem_z(nx, nz);
   const int threads_xy = (round4(nx) / 4) * (round4(ny) / 4), threads_z = (round4(nx) / 4) * (round4(nz) / 4);
-  return (*sxy <= 200 * 1024 && *sz <= 200 * 1024 && threads_xy <= 256 && threads_z <= 256) ? 1 : 0;
+  const int txy = (threads_xy + 31) / 32 * 32, tz = (threads_z + 31) / 32 * 32;
+  const bool covered = (long long)txy * kPrefetch >= (long long)round4(nx) * round4(ny) &&
+                       (long long)tz * kPrefetch >= (long long)round4(nx) * round4(nz);
+  return (*sxy <= 200 * 1024 && *sz <= 200 * 1024 && threads_xy <= 256 && threads_z <= 256 && covered) ? 1 : 0;
 }
 
 int launch_kin_xy_mixed(bsl_handle* h, const double* v, cudaStream_t s) {
@@ -226,11 +265,12 @@ int launch_kin_xy_mixed(bsl_handle* h, const double* v, cudaStream_t s) {
   if (!kinetic_mixed_supported(t.nx, t.ny, t.nz, &sxy, &sz))
     return fail(BSL_ERR_UNSUPPORTED, "grid too large for the mixed-precision kinetic kernels (max 64 points/axis)");
   cudaFuncSetAttribute(k_kin_xy_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sxy);
-  const int threads = (round4(t.nx) / 4) * (round4(t.ny) / 4);
+  const int threads = ((round4(t.nx) / 4) * (round4(t.ny) / 4) + 31) / 32 * 32;
   const int nplanes = t.nz * t.nn;
-  const int grid = nplanes < 8 * 152 ? nplanes : 8 * 152;
-  KinMixed km{d.kx_head, d.ky_head, d.kx_band, d.ky_band};
-  k_kin_xy_split<<<grid, ((threads + 31) / 32) * 32, sxy, s>>>(v, d.ukin, km, t.nx, t.ny, t.nz, nplanes);
+  if (!d.kin_grid_xy) d.kin_grid_xy = persistent_grid((const void*)k_kin_xy_split, threads, sxy, 1 << 30);
+  const int grid = d.kin_grid_xy;
+  KinMixed km{d.kx_head, d.kx_band, d.ky_head, d.ky_band};
+  k_kin_xy_split<<<grid < nplanes ? grid : nplanes, threads, sxy, s>>>(v, d.ukin, km, t.nx, t.ny, t.nz, nplanes);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }
@@ -242,11 +282,12 @@ int launch_kin_z_mixed(bsl_handle* h, const double* v, cudaStream_t s) {
   if (!kinetic_mixed_supported(t.nx, t.ny, t.nz, &sxy, &sz))
     return fail(BSL_ERR_UNSUPPORTED, "grid too large for the mixed-precision kinetic kernels (max 64 points/axis)");
   cudaFuncSetAttribute(k_kin_z_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
-  const int threads = (round4(t.nx) / 4) * (round4(t.nz) / 4);
+  const int threads = ((round4(t.nx) / 4) * (round4(t.nz) / 4) + 31) / 32 * 32;
   const int nplanes = t.ny * t.nn;
-  const int grid = nplanes < 8 * 152 ? nplanes : 8 * 152;
-  KinMixed km{d.kz_head, nullptr, d.kz_band, nullptr};
-  k_kin_z_split<<<grid, ((threads + 31) / 32) * 32, sz, s>>>(v, d.ukin, km, t.nx, t.ny, t.nz, nplanes);
+  if (!d.kin_grid_z) d.kin_grid_z = persistent_grid((const void*)k_kin_z_split, threads, sz, 1 << 30);
+  const int grid = d.kin_grid_z;
+  KinMixed km{d.kz_head, d.kz_band, nullptr, nullptr};
+  k_kin_z_split<<<grid < nplanes ? grid : nplanes, threads, sz, s>>>(v, d.ukin, km, t.nx, t.ny, t.nz, nplanes);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }

@@ -93,6 +93,8 @@ int init_state(bsl_handle* h, int start, unsigned long long seed) {
   if ((rc = dev_fill(d.rvec, D + 1, 0.0, s))) return rc;
   BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
   BSL_CUDA(cudaMemsetAsync(d.scalars, 0, 16 * sizeof(double), s));
+  BSL_CUDA(cudaMemcpyAsync(d.scalars, h->init_scalars, 8 * sizeof(double), cudaMemcpyHostToDevice, s));
+  h->lanczos_flip = 0;
   return BSL_OK;
 }
 
@@ -244,16 +246,17 @@ int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names) {
   if ((rc = ensure_hist(h, iters))) return rc;
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; ++i) BSL_CUDA(cudaEventCreate(&ev[i]));
+  const int nst = 4;
   double acc[5] = {0, 0, 0, 0, 0};
   for (int j = 1; j <= iters && !rc; ++j) {
     rc = dev_lanczos_iteration_timed(h, j, d.stream, ev);
     if (rc) break;
-    cudaError_t e = cudaEventSynchronize(ev[5]);
+    cudaError_t e = cudaEventSynchronize(ev[nst]);
     if (e != cudaSuccess) {
       rc = cuda_fail(e, "stage timing");
       break;
     }
-    for (int i = 0; i < 5; ++i) {
+    for (int i = 0; i < nst; ++i) {
       float x = 0.f;
       cudaEventElapsedTime(&x, ev[i], ev[i + 1]);
       acc[i] += x;
@@ -262,12 +265,12 @@ int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names) {
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   if (rc) return rc;
   for (int i = 0; i < 5; ++i) {
-    ms[i] = acc[i] / iters;
-    if (names) names[i] = dev_stage_name(h, i);
+    ms[i] = i < nst ? acc[i] / iters : 0.0;
+    if (names) names[i] = i < nst ? dev_stage_name(h, i) : "";
   }
   return check_status(h);
 }
 
-int bsl_launches_per_iteration(const bsl_handle* h) { return h ? 5 : -1; }
+int bsl_launches_per_iteration(const bsl_handle* h) { return h ? 4 : -1; }
 
 }  // extern "C"

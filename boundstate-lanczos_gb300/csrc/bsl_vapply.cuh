@@ -19,6 +19,8 @@ __global__ void __launch_bounds__(kThreads) k_vapply(const VT* __restrict__ vb, 
                                                      double* partials, unsigned int* counter, double* scalars,
                                                      double* hist, int j, long long dpk) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // logical Lanczos vectors are scale * buffer: v = sv * vec, r = sr * out
+  const double sv = mode ? scalars[4] : 1.0, sr = mode ? scalars[5] : 1.0;
   double dot = 0.0;
   if (p < npts) {
     double v[NN], acc[NN];
@@ -46,18 +48,22 @@ __global__ void __launch_bounds__(kThreads) k_vapply(const VT* __restrict__ vb, 
       if (mode == 0) {
         out[s * npts + p] = hv;
       } else {
-        const double r = out[s * npts + p] + hv;
+        const double r = sr * out[s * npts + p] + sv * hv;
         out[s * npts + p] = r;
         dot += v[s] * r;
       }
     }
   }
   if (mode == 1) {
-    if (p == 0) dot += vec[dpk] * out[dpk];  // the coordinate outside the symmetry block (H acts as 0)
+    if (p == 0) {  // the coordinate outside the symmetry block (H acts on it as 0)
+      const double rg = sr * out[dpk];
+      out[dpk] = rg;
+      dot += vec[dpk] * rg;
+    }
     double total;
     if (reduce_grid(dot, partials, counter, &total) && threadIdx.x == 0) {
-      scalars[0] = total;
-      hist[j - 1] = total;
+      scalars[0] = sv * total;
+      hist[j - 1] = sv * total;
     }
   }
 }
@@ -71,6 +77,8 @@ __global__ void __launch_bounds__(kThreads) k_vapply_generic(const double* __res
                                                              unsigned int* counter, double* scalars, double* hist,
                                                              int j, long long dpk) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // logical Lanczos vectors are scale * buffer: v = sv * vec, r = sr * out
+  const double sv = mode ? scalars[4] : 1.0, sr = mode ? scalars[5] : 1.0;
   double dot = 0.0;
   if (p < npts) {
     double v[kMaxNN], acc[kMaxNN];
@@ -89,18 +97,22 @@ __global__ void __launch_bounds__(kThreads) k_vapply_generic(const double* __res
       if (mode == 0) {
         out[s * npts + p] = acc[s];
       } else {
-        const double r = out[s * npts + p] + acc[s];
+        const double r = sr * out[s * npts + p] + sv * acc[s];
         out[s * npts + p] = r;
         dot += v[s] * r;
       }
     }
   }
   if (mode == 1) {
-    if (p == 0) dot += vec[dpk] * out[dpk];
+    if (p == 0) {
+      const double rg = sr * out[dpk];
+      out[dpk] = rg;
+      dot += vec[dpk] * rg;
+    }
     double total;
     if (reduce_grid(dot, partials, counter, &total) && threadIdx.x == 0) {
-      scalars[0] = total;
-      hist[j - 1] = total;
+      scalars[0] = sv * total;
+      hist[j - 1] = sv * total;
     }
   }
 }

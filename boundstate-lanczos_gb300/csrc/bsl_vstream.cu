@@ -100,6 +100,13 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const float* __restrict__ 
 
   const long long p = tile * kTilePts + tid;
   const bool valid = p < npts;
+  if (valid) {
+#pragma unroll
+    for (int s = 0; s < NN; ++s) {
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(ukin + s * npts + p));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(out + s * npts + p));
+    }
+  }
   float vv[NN], va[NN];
 #pragma unroll
   for (int s = 0; s < NN; ++s) {
@@ -128,6 +135,8 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const float* __restrict__ 
       }
     }
   }
+  // logical Lanczos vectors are scale * buffer: v = sv * vec, r = sr * out
+  const double sv = mode ? scalars[4] : 1.0, sr = mode ? scalars[5] : 1.0;
   double dot = 0.0;
   if (valid) {
 #pragma unroll
@@ -137,7 +146,7 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const float* __restrict__ 
       if (mode == 0) {
         out[s * npts + p] = hv;
       } else {
-        const double r = out[s * npts + p] + hv;
+        const double r = sr * out[s * npts + p] + sv * hv;
         out[s * npts + p] = r;
         dot += v * r;
       }
@@ -151,11 +160,15 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const float* __restrict__ 
       if (c >= 0) mbar_wait(&full[c % kStages], (uint32_t)((c / kStages) & 1));
   }
   if (mode == 1) {
-    if (p == 0) dot += vec[dpk] * out[dpk];  // the coordinate outside the symmetry block (H acts as 0)
+    if (p == 0) {  // the coordinate outside the symmetry block (H acts on it as 0)
+      const double rg = sr * out[dpk];
+      out[dpk] = rg;
+      dot += vec[dpk] * rg;
+    }
     double total;
     if (reduce_grid(dot, partials, counter, &total) && threadIdx.x == 0) {
-      scalars[0] = total;
-      hist[j - 1] = total;
+      scalars[0] = sv * total;
+      hist[j - 1] = sv * total;
     }
   }
 }
