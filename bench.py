@@ -317,6 +317,8 @@ def main():
         worst = int(np.argmax(dev)) if len(dev) else -1
         acc = {"iterations": n_it, "levels_compared": int(len(ref_levels)),
                "max_abs_dE_cm-1": float(dev.max()) if len(dev) else None,
+               "max_abs_dE_cm-1_lowest20": float(dev[:20].max()) if len(dev) else None,
+               "levels_within_1e-3_cm-1": int(np.sum(dev <= 1e-3)),
                "median_abs_dE_cm-1": float(np.median(dev)) if len(dev) else None,
                "worst_level_kJ_mol": float(ref_levels[worst]) if worst >= 0 else None,
                "dE_cm-1_per_level": [float("%.3g" % x) for x in dev],

@@ -262,7 +262,8 @@ namespace {
 
 void free_device(DeviceState& d) {
   void* ptrs[] = {d.tx, d.ty, d.tz, d.kx_head, d.ky_head, d.kz_head, d.kx_band, d.ky_band, d.kz_band, d.rot,
-                  d.v1, d.v2, d.vb64, d.vb32, d.vec, d.rvec, d.ukin, d.partials, d.counter,
+                  d.v1, d.v2, d.vb64, d.vb32, d.vec, d.rvec, d.ukin, d.v32, d.rot_hi, d.rot_lo, d.partials,
+                  d.counter,
                   d.scalars, d.status, d.hist, d.ref_vec, d.ref_out, d.full_of, d.ritz};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -433,6 +434,14 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
   kinetic_split_tables(t.tz, t.nz, false, &hi, &lo);
   if ((rc = upload(&d.kz_head, hi, "Tz")) || (rc = upload(&d.kz_band, lo, "Tz"))) return bail(rc);
   if ((rc = upload(&d.rot, t.rot, "rotor"))) return bail(rc);
+  {
+    std::vector<float> rh(t.rot.size()), rl(t.rot.size());
+    for (size_t i = 0; i < t.rot.size(); ++i) {
+      rh[i] = (float)t.rot[i];
+      rl[i] = (float)(t.rot[i] - (double)rh[i]);
+    }
+    if ((rc = upload(&d.rot_hi, rh, "rotor")) || (rc = upload(&d.rot_lo, rl, "rotor"))) return bail(rc);
+  }
   if ((rc = upload(&d.full_of, t.full_of, "index map"))) return bail(rc);
   const size_t N = (size_t)t.npts, D = N * t.nn;
   const size_t ngrid = N * t.na * t.nb;
@@ -441,7 +450,7 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
   if ((rc = dalloc(&d.v1, ngrid, "potential grid")) || (rc = dalloc(&d.v2, ngrid, "potential grid")) ||
       (rc = dalloc(&d.vb64, ntri * N, "potential blocks")) || (rc = dalloc(&d.vb32, ntri * tiled, "potential blocks")) ||
       (rc = dalloc(&d.vec, D + 1, "Lanczos vector")) || (rc = dalloc(&d.rvec, D + 1, "Lanczos vector")) ||
-      (rc = dalloc(&d.ukin, D, "kinetic work")))
+      (rc = dalloc(&d.ukin, D, "kinetic work")) || (rc = dalloc(&d.v32, D, "FP32 Lanczos copy")))
     return bail(rc);
   d.red_blocks = 1216;
   // one partial per block of the widest reducing launch (the per-point potential apply)
@@ -458,6 +467,13 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
   if (rc) return bail(rc);
   if ((rc = dev_vblocks(h))) return bail(rc);
   if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return bail(cuda_fail(e, "HvPrep"));
+  // the potential grid is only needed to build the blocks; keep it for
+  // inspection (bsl_copy_vgrid) when it is small
+  if (ngrid > ((size_t)1 << 26)) {
+    cudaFree(d.v1);
+    cudaFree(d.v2);
+    d.v1 = d.v2 = nullptr;
+  }
   *out = h;
   return BSL_OK;
 }
@@ -512,6 +528,7 @@ long long bsl_vgrid_size(const bsl_handle* h) { return h ? h->t.npts * h->t.na *
 // potential grid in the reference order ((i*ny+j)*nz+k)*na*nb + a*nb + b
 int bsl_copy_vgrid(const bsl_handle* h, double* v1, double* v2) {
   if (!h || !v1 || !v2) return fail(BSL_ERR_STATE, "null argument");
+  if (!h->d.v1) return fail(BSL_ERR_STATE, "the potential grid of a large problem is released after HvPrep");
   cudaSetDevice(h->p.device);
   const Tables& t = h->t;
   const size_t per = (size_t)t.na * t.nb, n = (size_t)t.npts * per;

@@ -77,10 +77,13 @@ struct DeviceState {
   double* vb64 = nullptr;
   float* vb32 = nullptr;
   // Lanczos work vectors (packed layout) and reduction scratch
-  double *vec = nullptr, *rvec = nullptr, *ukin = nullptr;
+  double *vec = nullptr, *rvec = nullptr, *ukin = nullptr;  // ukin: FP64, or (hi, lo) FP32 pairs (mixed)
+  float* v32 = nullptr;                       // FP32 copy of the current Lanczos v (mixed)
+  float *rot_hi = nullptr, *rot_lo = nullptr; // rotor energies as FP32 head + tail
   double* partials = nullptr;  // one double per reduction block
   unsigned int* counter = nullptr;
-  double* scalars = nullptr;   // [0] alpha_j, [1] beta_j, [2] beta2_j, [3] 1/beta_j, [4] sv, [5] sr
+  // [0] alpha_j, [1] beta_j, [2] beta2_j, [3] 1/beta_j, [4] sv, [5] sr, [6] sv/sr, [7] sv*sr
+  double* scalars = nullptr;
   int* status = nullptr;       // non-zero after a breakdown
   double* hist = nullptr;      // alpha/beta/beta2 history [3][niter+1]
   int hist_cap = 0;
@@ -102,7 +105,7 @@ struct bsl_handle {
   int precision = BSL_PREC_FP64;
   double last_ms_per_iter = 0.0;
   int lanczos_flip = 0;           // 0: vec holds v_j and rvec r_j; 1: roles swapped
-  double init_scalars[8] = {0, 0, 0, 0, 1, 1, 0, 0};  // alpha, beta, beta2, 1/beta, sv, sr
+  double init_scalars[8] = {0, 0, 0, 0, 1, 1, 1, 1};  // alpha, beta, beta2, 1/beta, sv, sr, sv/sr, sv*sr
 };
 
 namespace bsl {
@@ -126,14 +129,27 @@ int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, in
 // mixed-precision kinetic (bsl_kinetic.cu)
 void kinetic_split_tables(const std::vector<double>& T, int n, bool transpose, std::vector<float>* head,
                           std::vector<float>* band);
-int launch_kin_xy_mixed(bsl_handle* h, const double* v, cudaStream_t s);
-int launch_kin_z_mixed(bsl_handle* h, const double* v, cudaStream_t s);
+// mixed kinetic: FP32 input v, output u_kin as (hi, lo) FP32 pairs in d.ukin
+int launch_kin_xy_mixed(bsl_handle* h, const float* v, cudaStream_t s);
+int launch_kin_z_mixed(bsl_handle* h, const float* v, cudaStream_t s);
 
 // potential-block apply (bsl_vapply_f32.cu / bsl_vapply_f64.cu)
 // FP32 blocks in the tile-major layout of bsl_vstream.cu (vstream_tile_points() points per tile)
-int launch_vapply_f32(const float* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
-                      const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
-                      double* scalars, double* hist, int j, long long dpk, int* status);
+struct StreamArgs {
+  const float* vb;      // tile-major FP32 blocks
+  const float* v32;     // FP32 copy of v
+  const double* vec;    // FP64 v (alpha dot product, extra coordinate)
+  const float2* ukin;   // kinetic (hi, lo) pairs
+  const float* rot_hi;  // rotor energies, head and tail
+  const float* rot_lo;
+  double* out;          // mode 0: u = H v; mode 1: the Lanczos r buffer (r += c H v)
+  long long npts, dpk;
+  int mode, j;
+  double *partials, *scalars, *hist;
+  unsigned int* counter;
+  int* status;
+};
+int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s);
 long long vstream_tile_points();
 int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
                       const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,

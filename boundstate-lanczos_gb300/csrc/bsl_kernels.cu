@@ -299,16 +299,17 @@ __global__ void k_normalize_swap(double* __restrict__ v, double* __restrict__ r,
   }
 }
 
-// Folded-scale update of the packed loop: the buffers hold v = sv * V and
-// r' = R (scale 1 after the potential apply).  r' -= alpha v, beta^2 = r'.r';
-// the last block then records beta and sets the scales of the next iteration,
-// whose V is this R (v_{j+1} = r'/beta) and whose R is this V
-// (r_{j+1} = -beta v_j = -beta sv V), so no pass rescales or swaps memory.
-__global__ void k_update_fold(const double* __restrict__ V, double* __restrict__ R, long long L, double* partials,
-                              unsigned int* counter, double* scalars, double* hist, int hist_stride, int j,
-                              int* status) {
-  const double alpha = scalars[0], sv = scalars[4];
-  const double a = alpha * sv;
+// Folded-scale update of the packed loop.  The logical vectors are v = sv V and
+// r = sr R, and R already holds R + (sv/sr) H V.  This kernel forms
+// r - alpha v = sr (R - alpha (sv/sr) V), beta^2 = sr^2 |R|^2, and the scales of
+// the next iteration, whose V is this R (v_{j+1} = (sr/beta) R) and whose R is
+// this V (r_{j+1} = -beta v_j = (-beta sv) V): no pass rescales or swaps memory.
+// It also writes the FP32 copy of the next v's buffer for the mixed kernels.
+__global__ void k_update_fold(const double* __restrict__ V, double* __restrict__ R, long long L,
+                              float* __restrict__ v32_next, long long D, double* partials, unsigned int* counter,
+                              double* scalars, double* hist, int hist_stride, int j, int* status) {
+  const double alpha = scalars[0], sv = scalars[4], sr = scalars[5], c = scalars[6];
+  const double a = alpha * c;
   double acc = 0.0;
   const long long L2 = L / 2;
   const double2* V2 = reinterpret_cast<const double2*>(V);
@@ -316,31 +317,49 @@ __global__ void k_update_fold(const double* __restrict__ V, double* __restrict__
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L2; i += (long long)gridDim.x * blockDim.x) {
     const double2 v = V2[i];
     double2 r = R2[i];
-    r.x = r.x - a * v.x;
-    r.y = r.y - a * v.y;
+    r.x = fma(-a, v.x, r.x);
+    r.y = fma(-a, v.y, r.y);
     R2[i] = r;
-    acc += r.x * r.x + r.y * r.y;
+    acc = fma(r.x, r.x, acc);
+    acc = fma(r.y, r.y, acc);
+    const long long e = 2 * i;
+    if (e + 1 < D) {
+      reinterpret_cast<float2*>(v32_next)[i] = make_float2(f32_round(r.x), f32_round(r.y));
+    } else if (e < D) {
+      v32_next[e] = f32_round(r.x);
+    }
   }
   if ((L & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
-    const double x = R[L - 1] - a * V[L - 1];
+    const double x = fma(-a, V[L - 1], R[L - 1]);
     R[L - 1] = x;
-    acc += x * x;
+    acc = fma(x, x, acc);
+    if (L - 1 < D) v32_next[L - 1] = f32_round(x);
   }
   double total;
   if (reduce_grid(acc, partials, counter, &total) && threadIdx.x == 0) {
-    const double b = sqrt(total);
+    const double b2 = sr * sr * total;
+    const double b = sqrt(b2);
     scalars[1] = b;
-    scalars[2] = total;
+    scalars[2] = b2;
     scalars[3] = 1. / b;
     hist[hist_stride + j] = b;
-    hist[2 * hist_stride + j] = total;
-    scalars[4] = 1. / b;    // next v = R / beta
-    scalars[5] = -b * sv;   // next r = -beta v_j = (-beta sv) V
+    hist[2 * hist_stride + j] = b2;
+    const double sv_n = sr / b, sr_n = -b * sv;
+    scalars[4] = sv_n;
+    scalars[5] = sr_n;
+    scalars[6] = sv_n / sr_n;
+    scalars[7] = sv_n * sr_n;
     if (!(b > 0.0) || !isfinite(b) || !isfinite(alpha)) {
       if (status[0] == 0) status[1] = j;
       status[0] = 1;
     }
   }
+}
+
+// FP32 copy (rounded to nearest, integer pipe) of an FP64 vector
+__global__ void k_to_f32(const double* __restrict__ x, float* __restrict__ y, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = f32_round(x[i]);
 }
 
 __global__ void k_fill(double* x, long long L, double val) {
@@ -387,9 +406,26 @@ int launch_vapply(bsl_handle* h, const double* v, double* out, int mode, int j, 
   const long long N = t.npts;
   const dim3 g(grid_for(N));
   const long long dpk = N * t.nn;
-  if (h->precision == BSL_PREC_MIXED)
-    return launch_vapply_f32(d.vb32, g, s, t.nn, v, d.ukin, d.rot, out, N, mode, d.partials, d.counter, d.scalars,
-                             d.hist, j, dpk, d.status);
+  if (h->precision == BSL_PREC_MIXED) {
+    StreamArgs a;
+    a.vb = d.vb32;
+    a.v32 = d.v32;
+    a.vec = v;
+    a.ukin = reinterpret_cast<const float2*>(d.ukin);
+    a.rot_hi = d.rot_hi;
+    a.rot_lo = d.rot_lo;
+    a.out = out;
+    a.npts = N;
+    a.dpk = dpk;
+    a.mode = mode;
+    a.j = j;
+    a.partials = d.partials;
+    a.scalars = d.scalars;
+    a.hist = d.hist;
+    a.counter = d.counter;
+    a.status = d.status;
+    return launch_vapply_f32(a, t.nn, s);
+  }
   return launch_vapply_f64(d.vb64, g, s, t.nn, v, d.ukin, d.rot, out, N, mode, d.partials, d.counter, d.scalars,
                            d.hist, j, dpk);
 }
@@ -403,8 +439,8 @@ int launch_kinetic(bsl_handle* h, const double* v, cudaStream_t s) {
   if (sm_xy > 200 * 1024 || sm_z > 200 * 1024) return fail(BSL_ERR_UNSUPPORTED, "grid plane too large for one CTA");
   const dim3 gxy(t.nz, t.nn), gz(t.ny, t.nn);
   if (mixed) {
-    int rc = launch_kin_xy_mixed(h, v, s);
-    if (!rc) rc = launch_kin_z_mixed(h, v, s);
+    int rc = launch_kin_xy_mixed(h, d.v32, s);
+    if (!rc) rc = launch_kin_z_mixed(h, d.v32, s);
     return rc;
   } else {
     cudaFuncSetAttribute(k_kin_xy_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
@@ -554,6 +590,10 @@ int dev_vblocks(bsl_handle* h) {
 }
 
 int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s) {
+  if (h->precision == BSL_PREC_MIXED) {
+    k_to_f32<<<1024, kThreads, 0, s>>>(v, h->d.v32, bsl_packed_size(h));
+    BSL_CUDA(cudaGetLastError());
+  }
   int rc = launch_kinetic(h, v, s);
   if (rc) return rc;
   return launch_vapply(h, v, u, 0, 0, s);
@@ -567,8 +607,8 @@ int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s) {
   int rc = launch_kinetic(h, V, s);
   if (rc) return rc;
   if ((rc = launch_vapply(h, V, R, 1, j, s))) return rc;
-  k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j,
-                                                  d.status);
+  k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
+                                                  d.hist_cap, j, d.status);
   BSL_CUDA(cudaGetLastError());
   h->lanczos_flip ^= 1;
   return BSL_OK;
@@ -591,21 +631,21 @@ int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_
   int rc;
   cudaEventRecord(ev[0], s);
   if (mixed) {
-    if ((rc = launch_kin_xy_mixed(h, V, s))) return rc;
+    if ((rc = launch_kin_xy_mixed(h, d.v32, s))) return rc;
   } else {
     k_kin_xy_f64<<<gxy, kThreads, sm_xy, s>>>(V, d.ukin, d.tx, d.ty, t.nx, t.ny, t.nz);
   }
   cudaEventRecord(ev[1], s);
   if (mixed) {
-    if ((rc = launch_kin_z_mixed(h, V, s))) return rc;
+    if ((rc = launch_kin_z_mixed(h, d.v32, s))) return rc;
   } else {
     k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(V, d.ukin, d.tz, t.nx, t.ny, t.nz);
   }
   cudaEventRecord(ev[2], s);
   if ((rc = launch_vapply(h, V, R, 1, j, s))) return rc;
   cudaEventRecord(ev[3], s);
-  k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j,
-                                                  d.status);
+  k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
+                                                  d.hist_cap, j, d.status);
   cudaEventRecord(ev[4], s);
   BSL_CUDA(cudaGetLastError());
   h->lanczos_flip ^= 1;
@@ -617,6 +657,12 @@ const char* dev_stage_name(bsl_handle* h, int i) {
   static const char* n64[4] = {"k_kin_xy_f64", "k_kin_z_f64", "k_vapply<NN,double>", "k_update_fold"};
   static const char* nmx[4] = {"k_kin_xy_split", "k_kin_z_split", "k_vstream<NN>", "k_update_fold"};
   return mixed ? nmx[i] : n64[i];
+}
+
+int dev_to_f32(const double* x, float* y, long long n, cudaStream_t s) {
+  k_to_f32<<<1024, kThreads, 0, s>>>(x, y, n);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
 }
 
 int dev_fill(double* x, long long L, double val, cudaStream_t s) {

@@ -7,7 +7,8 @@
 // Precision: v is rounded to FP32; each kinetic matrix is split into an FP32
 // head T_hi = fl32(T) and an FP32 tail T_lo = fl32(T - T_hi).  The head
 // contraction and the tail contraction accumulate in separate FP32 registers
-// and are combined in FP64, so the FP32 rounding of the coefficients (a
+// and are combined into an unevaluated FP32 pair (hi + lo, error-free sums;
+// no FP64 instruction), so the FP32 rounding of the coefficients (a
 // systematic shift of every level, several 1e-3 cm^-1 at dx = 0.015 A) does
 // not reach the result; only the random rounding of v and of the FP32 sums
 // does.
@@ -56,7 +57,7 @@ __device__ __forceinline__ void zero(float (&acc)[4][4]) {
 }
 
 // x and y: out[s][k][j][i] = (Tx v)(i) + (Ty v)(j) on the plane of fixed (s, k)
-__global__ void __launch_bounds__(256) k_kin_xy_split(const double* __restrict__ vec, double* __restrict__ out,
+__global__ void __launch_bounds__(256) k_kin_xy_split(const float* __restrict__ vec, float2* __restrict__ out,
                                                       KinMixed km, int nx, int ny, int nz, int nplanes) {
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(256) k_kin_xy_split(const double* __restrict__
   const int i0 = 4 * tx, j0 = 4 * ty;
   const int npl = nyp * nxp;
   // the next plane is loaded into registers while the current one is computed
-  double pre[kPrefetch];
+  float pre[kPrefetch];
   auto load = [&](int plane) {
     const int k = plane % nz, s = plane / nz;
     const long long base = ((long long)s * nz + k) * ny * nx;
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(256) k_kin_xy_split(const double* __restrict__
     for (int u = 0; u < kPrefetch; ++u) {
       const int e = threadIdx.x + u * blockDim.x;
       const int j = e / nxp, i = e - j * nxp;
-      pre[u] = (e < npl && j < ny && i < nx) ? vec[base + (long long)j * nx + i] : 0.0;
+      pre[u] = (e < npl && j < ny && i < nx) ? vec[base + (long long)j * nx + i] : 0.f;
     }
   };
   if (blockIdx.x < nplanes) load(blockIdx.x);
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(256) k_kin_xy_split(const double* __restrict__
       const int e = threadIdx.x + u * blockDim.x;
       if (e < npl) {
         const int j = e / nxp, i = e - j * nxp;
-        const float x = (float)pre[u];
+        const float x = pre[u];
         P[e] = x;
         PT[i * nyp + j] = x;
       }
@@ -136,16 +137,21 @@ __global__ void __launch_bounds__(256) k_kin_xy_split(const double* __restrict__
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const int i = i0 + c;
-        if (i < nx)
-          out[base + (long long)j * nx + i] =
-              ((double)yh[r][c] + (double)yl[r][c]) + ((double)xh[r][c] + (double)xl[r][c]);
+        if (i < nx) {
+          // (hi, lo) pair with hi + lo = xh + yh + xl + yl to ~2^-48: no FP64 instruction
+          float sh, se;
+          two_sum(xh[r][c], yh[r][c], sh, se);
+          float hi, lo;
+          two_sum(sh, se + (xl[r][c] + yl[r][c]), hi, lo);
+          out[base + (long long)j * nx + i] = make_float2(hi, lo);
+        }
       }
     }
   }
 }
 
 // z: out[s][k][j][i] += (Tz v)(k) on the plane of fixed (s, j)
-__global__ void __launch_bounds__(256) k_kin_z_split(const double* __restrict__ vec, double* __restrict__ out,
+__global__ void __launch_bounds__(256) k_kin_z_split(const float* __restrict__ vec, float2* __restrict__ out,
                                                      KinMixed km, int nx, int ny, int nz, int nplanes) {
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
@@ -163,7 +169,7 @@ __global__ void __launch_bounds__(256) k_kin_z_split(const double* __restrict__ 
   const int i0 = 4 * tx, k0 = 4 * ty;
   const long long plane_stride = (long long)ny * nx;
   const int npl = nzp * nxp;
-  double pre[kPrefetch];
+  float pre[kPrefetch];
   auto load = [&](int plane) {
     const int j = plane % ny, s = plane / ny;
     const long long sb = (long long)s * nz * plane_stride + (long long)j * nx;
@@ -171,7 +177,7 @@ __global__ void __launch_bounds__(256) k_kin_z_split(const double* __restrict__ 
     for (int u = 0; u < kPrefetch; ++u) {
       const int e = threadIdx.x + u * blockDim.x;
       const int k = e / nxp, i = e - k * nxp;
-      pre[u] = (e < npl && k < nz && i < nx) ? vec[sb + k * plane_stride + i] : 0.0;
+      pre[u] = (e < npl && k < nz && i < nx) ? vec[sb + k * plane_stride + i] : 0.f;
     }
   };
   if (blockIdx.x < nplanes) load(blockIdx.x);
@@ -182,7 +188,7 @@ __global__ void __launch_bounds__(256) k_kin_z_split(const double* __restrict__ 
 #pragma unroll
     for (int u = 0; u < kPrefetch; ++u) {
       const int e = threadIdx.x + u * blockDim.x;
-      if (e < npl) P[e] = (float)pre[u];
+      if (e < npl) P[e] = pre[u];
     }
     __syncthreads();
     if (plane + (int)gridDim.x < nplanes) load(plane + gridDim.x);
@@ -205,7 +211,12 @@ __global__ void __launch_bounds__(256) k_kin_z_split(const double* __restrict__ 
         const int i = i0 + c;
         if (i >= nx) continue;
         const long long o = sb + k * plane_stride + i;
-        out[o] = ((double)zh[r][c] + (double)zl[r][c]) + out[o];
+        const float2 u = out[o];
+        float sh, se;
+        two_sum(u.x, zh[r][c], sh, se);
+        float hi, lo;
+        two_sum(sh, se + (u.y + zl[r][c]), hi, lo);
+        out[o] = make_float2(hi, lo);
       }
     }
   }
@@ -258,7 +269,7 @@ int kinetic_mixed_supported(int nx, int ny, int nz, size_t* sxy, size_t* sz) {
   return (*sxy <= 200 * 1024 && *sz <= 200 * 1024 && threads_xy <= 256 && threads_z <= 256 && covered) ? 1 : 0;
 }
 
-int launch_kin_xy_mixed(bsl_handle* h, const double* v, cudaStream_t s) {
+int launch_kin_xy_mixed(bsl_handle* h, const float* v, cudaStream_t s) {
   const Tables& t = h->t;
   DeviceState& d = h->d;
   size_t sxy, sz;
@@ -270,12 +281,13 @@ int launch_kin_xy_mixed(bsl_handle* h, const double* v, cudaStream_t s) {
   if (!d.kin_grid_xy) d.kin_grid_xy = persistent_grid((const void*)k_kin_xy_split, threads, sxy, 1 << 30);
   const int grid = d.kin_grid_xy;
   KinMixed km{d.kx_head, d.kx_band, d.ky_head, d.ky_band};
-  k_kin_xy_split<<<grid < nplanes ? grid : nplanes, threads, sxy, s>>>(v, d.ukin, km, t.nx, t.ny, t.nz, nplanes);
+  k_kin_xy_split<<<grid < nplanes ? grid : nplanes, threads, sxy, s>>>(v, reinterpret_cast<float2*>(d.ukin), km,
+                                                                       t.nx, t.ny, t.nz, nplanes);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }
 
-int launch_kin_z_mixed(bsl_handle* h, const double* v, cudaStream_t s) {
+int launch_kin_z_mixed(bsl_handle* h, const float* v, cudaStream_t s) {
   const Tables& t = h->t;
   DeviceState& d = h->d;
   size_t sxy, sz;
@@ -287,7 +299,8 @@ int launch_kin_z_mixed(bsl_handle* h, const double* v, cudaStream_t s) {
   if (!d.kin_grid_z) d.kin_grid_z = persistent_grid((const void*)k_kin_z_split, threads, sz, 1 << 30);
   const int grid = d.kin_grid_z;
   KinMixed km{d.kz_head, d.kz_band, nullptr, nullptr};
-  k_kin_z_split<<<grid < nplanes ? grid : nplanes, threads, sz, s>>>(v, d.ukin, km, t.nx, t.ny, t.nz, nplanes);
+  k_kin_z_split<<<grid < nplanes ? grid : nplanes, threads, sz, s>>>(v, reinterpret_cast<float2*>(d.ukin), km,
+                                                                     t.nx, t.ny, t.nz, nplanes);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }

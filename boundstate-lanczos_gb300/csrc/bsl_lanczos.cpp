@@ -23,6 +23,7 @@
 
 namespace bsl {
 int dev_fill(double* x, long long L, double val, cudaStream_t s);
+int dev_to_f32(const double* x, float* y, long long n, cudaStream_t s);
 int dev_full_step(bsl_handle* h, double* v, double* r, long long L, int j, cudaStream_t s);
 
 namespace {
@@ -94,6 +95,7 @@ int init_state(bsl_handle* h, int start, unsigned long long seed) {
   BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
   BSL_CUDA(cudaMemsetAsync(d.scalars, 0, 16 * sizeof(double), s));
   BSL_CUDA(cudaMemcpyAsync(d.scalars, h->init_scalars, 8 * sizeof(double), cudaMemcpyHostToDevice, s));
+  if ((rc = dev_to_f32(d.vec, d.v32, D, s))) return rc;
   h->lanczos_flip = 0;
   return BSL_OK;
 }

@@ -19,8 +19,9 @@ __global__ void __launch_bounds__(kThreads) k_vapply(const VT* __restrict__ vb, 
                                                      double* partials, unsigned int* counter, double* scalars,
                                                      double* hist, int j, long long dpk) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  // logical Lanczos vectors are scale * buffer: v = sv * vec, r = sr * out
-  const double sv = mode ? scalars[4] : 1.0, sr = mode ? scalars[5] : 1.0;
+  // logical Lanczos vectors are v = sv vec and r = sr out; r + H v is kept as
+  // sr (out + (sv/sr) H vec): out' = out + c H vec, alpha = sv sr (vec . out')
+  const double c = mode ? scalars[6] : 1.0;
   double dot = 0.0;
   if (p < npts) {
     double v[NN], acc[NN];
@@ -48,22 +49,18 @@ __global__ void __launch_bounds__(kThreads) k_vapply(const VT* __restrict__ vb, 
       if (mode == 0) {
         out[s * npts + p] = hv;
       } else {
-        const double r = sr * out[s * npts + p] + sv * hv;
+        const double r = fma(c, hv, out[s * npts + p]);
         out[s * npts + p] = r;
         dot += v[s] * r;
       }
     }
   }
   if (mode == 1) {
-    if (p == 0) {  // the coordinate outside the symmetry block (H acts on it as 0)
-      const double rg = sr * out[dpk];
-      out[dpk] = rg;
-      dot += vec[dpk] * rg;
-    }
+    if (p == 0) dot += vec[dpk] * out[dpk];  // the coordinate outside the symmetry block (H acts on it as 0)
     double total;
     if (reduce_grid(dot, partials, counter, &total) && threadIdx.x == 0) {
-      scalars[0] = sv * total;
-      hist[j - 1] = sv * total;
+      scalars[0] = scalars[7] * total;
+      hist[j - 1] = scalars[7] * total;
     }
   }
 }
@@ -77,8 +74,9 @@ __global__ void __launch_bounds__(kThreads) k_vapply_generic(const double* __res
                                                              unsigned int* counter, double* scalars, double* hist,
                                                              int j, long long dpk) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  // logical Lanczos vectors are scale * buffer: v = sv * vec, r = sr * out
-  const double sv = mode ? scalars[4] : 1.0, sr = mode ? scalars[5] : 1.0;
+  // logical Lanczos vectors are v = sv vec and r = sr out; r + H v is kept as
+  // sr (out + (sv/sr) H vec): out' = out + c H vec, alpha = sv sr (vec . out')
+  const double c = mode ? scalars[6] : 1.0;
   double dot = 0.0;
   if (p < npts) {
     double v[kMaxNN], acc[kMaxNN];
@@ -97,22 +95,18 @@ __global__ void __launch_bounds__(kThreads) k_vapply_generic(const double* __res
       if (mode == 0) {
         out[s * npts + p] = acc[s];
       } else {
-        const double r = sr * out[s * npts + p] + sv * acc[s];
+        const double r = fma(c, acc[s], out[s * npts + p]);
         out[s * npts + p] = r;
         dot += v[s] * r;
       }
     }
   }
   if (mode == 1) {
-    if (p == 0) {
-      const double rg = sr * out[dpk];
-      out[dpk] = rg;
-      dot += vec[dpk] * rg;
-    }
+    if (p == 0) dot += vec[dpk] * out[dpk];
     double total;
     if (reduce_grid(dot, partials, counter, &total) && threadIdx.x == 0) {
-      scalars[0] = sv * total;
-      hist[j - 1] = sv * total;
+      scalars[0] = scalars[7] * total;
+      hist[j - 1] = scalars[7] * total;
     }
   }
 }

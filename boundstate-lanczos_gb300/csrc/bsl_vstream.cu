@@ -12,8 +12,8 @@
 // rows is one contiguous copy of kChunk * 512 bytes.
 //
 // One CTA per tile of 128 grid points, one thread per point:
-//   u(s) = ukin(s) + B l(l+1) v(s) + sum_s' V_ss' v(s')   (FP32 block product, FP64 sums)
-//   mode 0: out = u;   mode 1: r += u, partial alpha = v . r (deterministic grid reduction)
+//   u(s) = ukin(s) + B l(l+1) v(s) + sum_s' V_ss' v(s')   (FP32 block product, FP32-pair sums)
+//   mode 0: out = u (FP64);   mode 1: R += c u (FP64), partial alpha = V . R (deterministic grid reduction)
 #include "bsl_device.cuh"
 
 namespace bsl {
@@ -63,12 +63,7 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t b
 }
 
 template <int NN>
-__global__ void __launch_bounds__(kTilePts) k_vstream(const float* __restrict__ vbt, long long npts,
-                                                      const double* __restrict__ vec, const double* __restrict__ ukin,
-                                                      const double* __restrict__ rot, double* __restrict__ out,
-                                                      int mode, double* partials, unsigned int* counter,
-                                                      double* scalars, double* hist, int j, long long dpk,
-                                                      int* status) {
+__global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
   constexpr int NT = NN * (NN + 1) / 2;
   constexpr int NCH = (NT + kChunk - 1) / kChunk;
   extern __shared__ float4 ring4[];
@@ -77,11 +72,12 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const float* __restrict__ 
   __shared__ int abort_flag, issued;
   const int tid = threadIdx.x;
   const long long tile = blockIdx.x;
-  const float* src_tile = vbt + tile * (long long)NT * kTilePts;
+  const long long npts = A.npts;
+  const float* src_tile = A.vb + tile * (long long)NT * kTilePts;
   if (tid == 0) {
     // a stream that already timed out in an earlier launch disables the copies
     // (and every wait) of later launches until the host has seen the error
-    abort_flag = *(volatile int*)(status + 2);
+    abort_flag = *(volatile int*)(A.status + 2);
     issued = 0;
     for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -103,14 +99,14 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const float* __restrict__ 
   if (valid) {
 #pragma unroll
     for (int s = 0; s < NN; ++s) {
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(ukin + s * npts + p));
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(out + s * npts + p));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(A.ukin + s * npts + p));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(A.out + s * npts + p));
     }
   }
   float vv[NN], va[NN];
 #pragma unroll
   for (int s = 0; s < NN; ++s) {
-    vv[s] = valid ? (float)vec[s * npts + p] : 0.f;
+    vv[s] = valid ? A.v32[s * npts + p] : 0.f;
     va[s] = 0.f;
   }
   int t = 0;
@@ -135,53 +131,53 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const float* __restrict__ 
       }
     }
   }
-  // logical Lanczos vectors are scale * buffer: v = sv * vec, r = sr * out
-  const double sv = mode ? scalars[4] : 1.0, sr = mode ? scalars[5] : 1.0;
+  // u = kinetic pair + B l(l+1) v + V v as an FP32 pair, then one FP64 value.
+  // mode 1: the logical vectors are v = sv V and r = sr R; r + H v is kept as
+  // sr (R + (sv/sr) H V), so R' = R + c H V and alpha = sv sr (V . R').
+  const double c = A.mode ? A.scalars[6] : 1.0;
   double dot = 0.0;
   if (valid) {
 #pragma unroll
     for (int s = 0; s < NN; ++s) {
-      const double v = vec[s * npts + p];
-      const double hv = (ukin[s * npts + p] + __ldg(rot + s) * v) + (double)va[s];
-      if (mode == 0) {
-        out[s * npts + p] = hv;
+      const float2 uk = A.ukin[s * npts + p];
+      const float a = fmaf(__ldg(A.rot_hi + s), vv[s], va[s]);
+      float hi, e;
+      two_sum(uk.x, a, hi, e);
+      const float lo = uk.y + e + __ldg(A.rot_lo + s) * vv[s];
+      const double hv = f64_of(hi) + f64_of(lo);
+      if (A.mode == 0) {
+        A.out[s * npts + p] = hv;
       } else {
-        const double r = sr * out[s * npts + p] + sv * hv;
-        out[s * npts + p] = r;
-        dot += v * r;
+        const double r = fma(c, hv, A.out[s * npts + p]);
+        A.out[s * npts + p] = r;
+        dot = fma(A.vec[s * npts + p], r, dot);
       }
     }
   }
   if (abort_flag && tid == 0 && issued > 0) {
     // a copy did not complete in time: record it and give the copies still in
     // flight a bounded chance to land before the CTA's shared memory is released
-    status[2] = 1;
-    for (int c = issued - kStages; c < issued; ++c)
-      if (c >= 0) mbar_wait(&full[c % kStages], (uint32_t)((c / kStages) & 1));
+    A.status[2] = 1;
+    for (int cc = issued - kStages; cc < issued; ++cc)
+      if (cc >= 0) mbar_wait(&full[cc % kStages], (uint32_t)((cc / kStages) & 1));
   }
-  if (mode == 1) {
-    if (p == 0) {  // the coordinate outside the symmetry block (H acts on it as 0)
-      const double rg = sr * out[dpk];
-      out[dpk] = rg;
-      dot += vec[dpk] * rg;
-    }
+  if (A.mode == 1) {
+    if (p == 0) dot = fma(A.vec[A.dpk], A.out[A.dpk], dot);  // extra coordinate: H acts as 0, R' = R
     double total;
-    if (reduce_grid(dot, partials, counter, &total) && threadIdx.x == 0) {
-      scalars[0] = sv * total;
-      hist[j - 1] = sv * total;
+    if (reduce_grid(dot, A.partials, A.counter, &total) && threadIdx.x == 0) {
+      const double alpha = A.scalars[7] * total;
+      A.scalars[0] = alpha;
+      A.hist[A.j - 1] = alpha;
     }
   }
 }
 
 template <int NN>
-int launch_nn(const float* vbt, cudaStream_t s, long long N, const double* v, const double* uk, const double* rot,
-              double* out, int mode, double* partials, unsigned int* counter, double* scalars, double* hist, int j,
-              long long dpk, int* status) {
+int launch_nn(const StreamArgs& a, cudaStream_t s) {
   const size_t smem = (size_t)kStages * kChunk * kTilePts * sizeof(float);
   cudaFuncSetAttribute(k_vstream<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  const long long tiles = (N + kTilePts - 1) / kTilePts;
-  k_vstream<NN><<<(unsigned)tiles, kTilePts, smem, s>>>(vbt, N, v, uk, rot, out, mode, partials, counter, scalars,
-                                                        hist, j, dpk, status);
+  const long long tiles = (a.npts + kTilePts - 1) / kTilePts;
+  k_vstream<NN><<<(unsigned)tiles, kTilePts, smem, s>>>(a);
   return BSL_OK;
 }
 
@@ -189,13 +185,10 @@ int launch_nn(const float* vbt, cudaStream_t s, long long N, const double* v, co
 
 long long vstream_tile_points() { return kTilePts; }
 
-int launch_vapply_f32(const float* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
-                      const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
-                      double* scalars, double* hist, int j, long long dpk, int* status) {
-  (void)g;
-#define BSL_CASE(K)                                                                                            \
-  case K:                                                                                                      \
-    launch_nn<K>(vb, s, N, v, uk, rot, out, mode, partials, counter, scalars, hist, j, dpk, status);           \
+int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s) {
+#define BSL_CASE(K)      \
+  case K:                \
+    launch_nn<K>(a, s);  \
     break;
   switch (nn) {
     BSL_CASE(1)
