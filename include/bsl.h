@@ -150,6 +150,30 @@ int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed
 int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alpha_j, double* beta_j,
                           double* beta2_j);
 
+/* The rest of one Lanczos iteration after r += H v, on device buffers the
+   caller owns, without allocating any device memory.  No counterpart in the
+   reference: it exists for callers that cannot call cudaMalloc at the point
+   where they run the recurrence -- code that is recording a CUDA graph (stream
+   capture forbids allocation), applications that reserve all GPU memory up
+   front in their own pool, and real-time loops that cannot afford the device
+   synchronisation an allocation implies.
+
+   d_vec holds v_j, d_rvec holds r_j + H v_j (n doubles each, any layout, FP64).
+   On return, as in the reference loop body (lanczosEigenValuesVectors.cpp:202-238):
+   alpha = v.r, r -= alpha v, beta = |r|, d_vec = r / beta, d_rvec = -beta v_j,
+   and d_abb[0..2] = {alpha, beta, beta^2} (device memory).  Work is queued on
+   `stream` (cudaStream_t as void*, NULL = legacy default stream) and runs on the
+   calling thread's current device.
+
+   The reduction scratch is one static device array of 4112 doubles (32.9 KB)
+   that every GPU loading the library holds until the process exits; it limits
+   n to 1..8,388,608 (BSL_ERR_INPUT beyond).  All calls on a device share it:
+   calls that overlap on the GPU (different streams without ordering) race and
+   give wrong results.  The first call on each device looks up the array's
+   device address (cudaGetSymbolAddress); make that first call before any
+   stream capture.  No allocation, no cudaFree, no synchronisation. */
+int bsl_lanczos_orthonormalize_static(double* d_vec, double* d_rvec, long long n, double* d_abb, void* stream);
+
 /* Cullum-Willoughby good eigenvalues in (emin, emax] with inverse-iteration
    error estimates (lancbis.cpp:5-105 with BISEC/ISOEV/INVERR).  eval and err
    need niter entries; *ngood receives the count. */
