@@ -20,8 +20,8 @@ namespace bsl {
 namespace {
 
 constexpr int kTilePts = 128;
-constexpr int kChunk = 32;    // block rows per copy (16 KiB)
-constexpr int kStages = 4;    // ring depth (64 KiB of shared memory)
+constexpr int kChunk = 16;    // block rows per copy (8 KiB)
+constexpr int kStages = 4;    // ring depth (32 KiB of shared memory)
 constexpr long long kSpinCycles = 1000000000ll;  // ~0.5 s at 2 GHz: bound on every wait
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {

@@ -195,6 +195,12 @@ int bsl_ritz_vectors(bsl_handle* h, int niter, const double* evtr, int ngood, do
    iteration, measured with CUDA events on the library's stream. */
 int bsl_last_run_ms_per_iter(const bsl_handle* h, double* ms);
 
+/* Diagnostic: one 128 x 64 x 64 TF32 product through the tensor cores
+   (tcgen05.mma from swizzled shared memory into tensor memory) on the current
+   device, compared with its exact value; *max_abs_err receives the largest
+   deviation (0 when the tensor-core path is sound). */
+int bsl_selftest_tensor_core(double* max_abs_err);
+
 /* Per-kernel device time of the Lanczos iteration: runs `iters` iterations
    (continuing the current device state) with CUDA events around every
    kernel on the library's stream and writes the average milliseconds per
