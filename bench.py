@@ -198,6 +198,8 @@ def main():
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="prep plus this many iterations only (for profiler captures)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--kinetic", default="auto", choices=["auto", "simt", "tensor"],
+                    help="kinetic engine of the mixed path (auto: tensor cores where the grid allows)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -228,6 +230,9 @@ def main():
     t0 = time.perf_counter()
     h = bsl.Hamiltonian(hv_path, "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE", precision=args.precision, device=local)
     prep_s = time.perf_counter() - t0
+    if args.kinetic != "auto":
+        h.set_kinetic_engine(args.kinetic)
+    kinetic_engine = h.kinetic_engine()
     D, Df, nn = h.packed_size, h.basis_size, h.nn
     N = D // nn
     if args.profile_iters:
@@ -235,7 +240,7 @@ def main():
         h.lanczos(args.profile_iters)
         torch.cuda.synchronize()
         print(json.dumps({"profile_iters": args.profile_iters, "ms_per_iter": h.last_ms_per_iter(),
-                          "precision": args.precision}))
+                          "precision": args.precision, "kinetic": h.kinetic_engine()}))
         h.close()
         return
 
@@ -344,7 +349,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (generated SPC/E cage, seed 1)",
-        "config": config_record(cfg, D, Df),
+        "config": dict(config_record(cfg, D, Df), kinetic_engine=kinetic_engine),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * Df * 8, "d2h_bytes_per_step": 2 * Df * 8,
                 "path": "bsl_lanczos_step_host: reference loop body with host (pinned) vec/rvec in the reference "
                         "layout, H2D + Hv + recurrence + D2H per step"},

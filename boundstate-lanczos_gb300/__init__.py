@@ -23,6 +23,7 @@ SYM = {"All": 0, "Even": 1, "Odd": 2}
 POT_ALAVI_SPCE, POT_ISOHARMOSC = 0, 1
 PREC = {"fp64": 0, "mixed": 1}
 START = {"uniform": 0, "normal": 1}
+KINETIC = {"simt": 0, "tensor": 1}
 CALCULATORS = {
     "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE": POT_ALAVI_SPCE,
     "linRotCartSph_NoQuad_IsoHarmOsc": POT_ISOHARMOSC,
@@ -75,6 +76,8 @@ def lib():
     L.bsl_hv_apply.argtypes = [C.c_void_p, _P, _P]
     L.bsl_hv_apply_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.bsl_set_precision.argtypes = [C.c_void_p, C.c_int]
+    L.bsl_set_kinetic_engine.argtypes = [C.c_void_p, C.c_int]
+    L.bsl_kinetic_engine.argtypes = [C.c_void_p]
     L.bsl_lanczos_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong, _P, _P, _P]
     L.bsl_lanczos_step_host.argtypes = [C.c_void_p, _P, _P, _P, _P, _P]
     L.bsl_good_eigenvalues.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_int)]
@@ -165,6 +168,16 @@ class Hamiltonian:
 
     def set_precision(self, precision):
         _check(lib().bsl_set_precision(self._h, PREC[precision]))
+
+    def set_kinetic_engine(self, engine):
+        """Kinetic engine of the mixed precision: "simt" or "tensor"."""
+        _check(lib().bsl_set_kinetic_engine(self._h, KINETIC[engine]))
+
+    def kinetic_engine(self):
+        e = lib().bsl_kinetic_engine(self._h)
+        if e < 0:
+            raise BslError(ERR_STATE, "closed handle")
+        return {v: k for k, v in KINETIC.items()}[e]
 
     def hv(self, vec, uec):
         """uec += H vec (host arrays, reference layout)."""

@@ -267,6 +267,10 @@ void free_device(DeviceState& d) {
                   d.scalars, d.status, d.hist, d.ref_vec, d.ref_out, d.full_of, d.ritz};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (int i = 0; i < 3; ++i) {
+    if (d.kxy_tf32[i]) cudaFree(d.kxy_tf32[i]);
+    if (d.kz_tf32[i]) cudaFree(d.kz_tf32[i]);
+  }
   if (d.ev0) cudaEventDestroy(d.ev0);
   if (d.ev1) cudaEventDestroy(d.ev1);
   if (d.stream) cudaStreamDestroy(d.stream);
@@ -433,6 +437,18 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
   if ((rc = upload(&d.ky_head, hi, "Ty")) || (rc = upload(&d.ky_band, lo, "Ty"))) return bail(rc);
   kinetic_split_tables(t.tz, t.nz, false, &hi, &lo);
   if ((rc = upload(&d.kz_head, hi, "Tz")) || (rc = upload(&d.kz_band, lo, "Tz"))) return bail(rc);
+  if (kinetic_tc_supported(t)) {
+    std::vector<float> t1, t2, t3;
+    kinetic_tf32_tables(t.tx, t.nx, &t1, &t2, &t3);
+    if ((rc = upload(&d.kxy_tf32[0], t1, "Tx")) || (rc = upload(&d.kxy_tf32[1], t2, "Tx")) ||
+        (rc = upload(&d.kxy_tf32[2], t3, "Tx")))
+      return bail(rc);
+    kinetic_tf32_tables(t.tz, t.nz, &t1, &t2, &t3);
+    if ((rc = upload(&d.kz_tf32[0], t1, "Tz")) || (rc = upload(&d.kz_tf32[1], t2, "Tz")) ||
+        (rc = upload(&d.kz_tf32[2], t3, "Tz")))
+      return bail(rc);
+    h->kinetic_engine = BSL_KIN_TENSOR;
+  }
   if ((rc = upload(&d.rot, t.rot, "rotor"))) return bail(rc);
   {
     std::vector<float> rh(t.rot.size()), rl(t.rot.size());
@@ -497,6 +513,17 @@ int bsl_set_precision(bsl_handle* h, int precision) {
   return BSL_OK;
 }
 
+int bsl_set_kinetic_engine(bsl_handle* h, int engine) {
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (engine != BSL_KIN_SIMT && engine != BSL_KIN_TENSOR) return fail(BSL_ERR_INPUT, "unknown kinetic engine");
+  if (engine == BSL_KIN_TENSOR && !h->d.kxy_tf32[0])
+    return fail(BSL_ERR_UNSUPPORTED, "tensor-core kinetic needs at most 64 points per axis and equal x and y axes");
+  h->kinetic_engine = engine;
+  return BSL_OK;
+}
+
+int bsl_kinetic_engine(const bsl_handle* h) { return h ? h->kinetic_engine : -1; }
+
 int bsl_hv_apply_device(bsl_handle* h, const double* d_v, double* d_u, void* stream) {
   if (!h || !d_v || !d_u) return fail(BSL_ERR_STATE, "null argument");
   cudaSetDevice(h->p.device);
@@ -520,6 +547,11 @@ int bsl_hv_apply(bsl_handle* h, const double* vec, double* uec) {
   if ((rc = dev_scatter_full(h, d.rvec, d.ref_out, s))) return rc;
   BSL_CUDA(cudaMemcpyAsync(uec, d.ref_out, Df * sizeof(double), cudaMemcpyDeviceToHost, s));
   BSL_CUDA(cudaStreamSynchronize(s));
+  int st[4] = {0, 0, 0, 0};
+  BSL_CUDA(cudaMemcpy(st, d.status, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st[2] || st[3])
+    return fail(BSL_ERR_CUDA, st[2] ? "potential-block stream: a bulk copy did not complete within its time limit"
+                                    : "tensor-core kinetic: an MMA did not complete within its time limit");
   return BSL_OK;
 }
 

@@ -69,6 +69,9 @@ struct DeviceState {
   // FP32 heads fl32(T) and tails fl32(T - head), both stored transposed, for the mixed kernels
   float *kx_head = nullptr, *ky_head = nullptr, *kz_head = nullptr;
   float *kx_band = nullptr, *ky_band = nullptr, *kz_band = nullptr;
+  // TF32 splits T = T1 + T2 + T3 as zero-padded 64 x 64 tiles, for the tensor-core kinetic
+  float* kxy_tf32[3] = {nullptr, nullptr, nullptr};
+  float* kz_tf32[3] = {nullptr, nullptr, nullptr};
   int kin_grid_xy = 0, kin_grid_z = 0;  // persistent grid sizes
   double* rot = nullptr;  // [nn]
   // potential grid V(p, a, b) for phi_b and 2pi - phi_b, p in vector order
@@ -84,7 +87,8 @@ struct DeviceState {
   unsigned int* counter = nullptr;
   // [0] alpha_j, [1] beta_j, [2] beta2_j, [3] 1/beta_j, [4] sv, [5] sr, [6] sv/sr, [7] sv*sr
   double* scalars = nullptr;
-  int* status = nullptr;       // non-zero after a breakdown
+  // [0] breakdown, [1] its iteration, [2] potential-block stream timeout, [3] tensor-core kinetic timeout
+  int* status = nullptr;
   double* hist = nullptr;      // alpha/beta/beta2 history [3][niter+1]
   int hist_cap = 0;
   // host-layout staging
@@ -103,6 +107,7 @@ struct bsl_handle {
   bsl::Cage cage;
   bsl::DeviceState d;
   int precision = BSL_PREC_FP64;
+  int kinetic_engine = BSL_KIN_SIMT;  // engine of the mixed-precision kinetic (BSL_KIN_*)
   double last_ms_per_iter = 0.0;
   int lanczos_flip = 0;           // 0: vec holds v_j and rvec r_j; 1: roles swapped
   double init_scalars[8] = {0, 0, 0, 0, 1, 1, 1, 1};  // alpha, beta, beta2, 1/beta, sv, sr, sv/sr, sv*sr
@@ -132,6 +137,14 @@ void kinetic_split_tables(const std::vector<double>& T, int n, bool transpose, s
 // mixed kinetic: FP32 input v, output u_kin as (hi, lo) FP32 pairs in d.ukin
 int launch_kin_xy_mixed(bsl_handle* h, const float* v, cudaStream_t s);
 int launch_kin_z_mixed(bsl_handle* h, const float* v, cudaStream_t s);
+
+// tensor-core kinetic (bsl_kinetic_tc.cu): the same contract as the mixed
+// kernels, for grids of at most 64 points per axis with Tx = Ty
+void kinetic_tf32_tables(const std::vector<double>& T, int n, std::vector<float>* t1, std::vector<float>* t2,
+                         std::vector<float>* t3);
+bool kinetic_tc_supported(const Tables& t);
+int launch_kin_xy_tc(bsl_handle* h, const float* v, cudaStream_t s);
+int launch_kin_z_tc(bsl_handle* h, const float* v, cudaStream_t s);
 
 // potential-block apply (bsl_vapply_f32.cu / bsl_vapply_f64.cu)
 // FP32 blocks in the tile-major layout of bsl_vstream.cu (vstream_tile_points() points per tile)

@@ -430,6 +430,14 @@ int launch_vapply(bsl_handle* h, const double* v, double* out, int mode, int j, 
                            d.hist, j, dpk);
 }
 
+// mixed-precision kinetic stages on the FP32 copy of v, by the selected engine
+int launch_kin_xy(bsl_handle* h, cudaStream_t s) {
+  return h->kinetic_engine == BSL_KIN_TENSOR ? launch_kin_xy_tc(h, h->d.v32, s) : launch_kin_xy_mixed(h, h->d.v32, s);
+}
+int launch_kin_z(bsl_handle* h, cudaStream_t s) {
+  return h->kinetic_engine == BSL_KIN_TENSOR ? launch_kin_z_tc(h, h->d.v32, s) : launch_kin_z_mixed(h, h->d.v32, s);
+}
+
 int launch_kinetic(bsl_handle* h, const double* v, cudaStream_t s) {
   DeviceState& d = h->d;
   const Tables& t = h->t;
@@ -439,8 +447,8 @@ int launch_kinetic(bsl_handle* h, const double* v, cudaStream_t s) {
   if (sm_xy > 200 * 1024 || sm_z > 200 * 1024) return fail(BSL_ERR_UNSUPPORTED, "grid plane too large for one CTA");
   const dim3 gxy(t.nz, t.nn), gz(t.ny, t.nn);
   if (mixed) {
-    int rc = launch_kin_xy_mixed(h, d.v32, s);
-    if (!rc) rc = launch_kin_z_mixed(h, d.v32, s);
+    int rc = launch_kin_xy(h, s);
+    if (!rc) rc = launch_kin_z(h, s);
     return rc;
   } else {
     cudaFuncSetAttribute(k_kin_xy_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
@@ -631,13 +639,13 @@ int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_
   int rc;
   cudaEventRecord(ev[0], s);
   if (mixed) {
-    if ((rc = launch_kin_xy_mixed(h, d.v32, s))) return rc;
+    if ((rc = launch_kin_xy(h, s))) return rc;
   } else {
     k_kin_xy_f64<<<gxy, kThreads, sm_xy, s>>>(V, d.ukin, d.tx, d.ty, t.nx, t.ny, t.nz);
   }
   cudaEventRecord(ev[1], s);
   if (mixed) {
-    if ((rc = launch_kin_z_mixed(h, d.v32, s))) return rc;
+    if ((rc = launch_kin_z(h, s))) return rc;
   } else {
     k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(V, d.ukin, d.tz, t.nx, t.ny, t.nz);
   }
@@ -656,7 +664,9 @@ const char* dev_stage_name(bsl_handle* h, int i) {
   const bool mixed = h->precision == BSL_PREC_MIXED;
   static const char* n64[4] = {"k_kin_xy_f64", "k_kin_z_f64", "k_vapply<NN,double>", "k_update_fold"};
   static const char* nmx[4] = {"k_kin_xy_split", "k_kin_z_split", "k_vstream<NN>", "k_update_fold"};
-  return mixed ? nmx[i] : n64[i];
+  static const char* ntc[4] = {"k_kin_xy_tc", "k_kin_z_tc", "k_vstream<NN>", "k_update_fold"};
+  if (!mixed) return n64[i];
+  return h->kinetic_engine == BSL_KIN_TENSOR ? ntc[i] : nmx[i];
 }
 
 int dev_to_f32(const double* x, float* y, long long n, cudaStream_t s) {

@@ -101,9 +101,10 @@ int init_state(bsl_handle* h, int start, unsigned long long seed) {
 }
 
 int check_status(bsl_handle* h) {
-  int st[3] = {0, 0, 0};
-  BSL_CUDA(cudaMemcpy(st, h->d.status, 3 * sizeof(int), cudaMemcpyDeviceToHost));
+  int st[4] = {0, 0, 0, 0};
+  BSL_CUDA(cudaMemcpy(st, h->d.status, 4 * sizeof(int), cudaMemcpyDeviceToHost));
   if (st[2]) return fail(BSL_ERR_CUDA, "potential-block stream: a bulk copy did not complete within its time limit");
+  if (st[3]) return fail(BSL_ERR_CUDA, "tensor-core kinetic: an MMA did not complete within its time limit");
   if (st[0]) return fail(BSL_ERR_BREAKDOWN, "Lanczos breakdown at iteration " + std::to_string(st[1]) +
                                                 ": beta is zero or alpha/beta are not finite");
   return BSL_OK;

@@ -53,6 +53,12 @@ extern "C" {
                             coefficients and FP64 combination, FP64 rotor
                             diagonal and FP64 Lanczos recurrence */
 
+/* engine of the FP32 kinetic contractions in BSL_PREC_MIXED */
+#define BSL_KIN_SIMT 0   /* FP32 head/tail coefficients on the CUDA cores */
+#define BSL_KIN_TENSOR 1 /* TF32 splits on the tensor cores (tcgen05.mma), FP32
+                            accumulation in tensor memory; grids of at most 64
+                            points per axis with equal x and y axes */
+
 /* Lanczos start vector */
 #define BSL_START_UNIFORM 0 /* 1/sqrt(D) over the reference layout, as the
                                reference driver (lanczosEigenValuesVectors.cpp:177-181) */
@@ -123,6 +129,11 @@ int bsl_packed_nn(const bsl_handle* h);
 
 /* Switch the arithmetic of later Hv applications (BSL_PREC_*). */
 int bsl_set_precision(bsl_handle* h, int precision);
+
+/* Select the kinetic engine of BSL_PREC_MIXED (BSL_KIN_*).  bsl_hv_prep picks
+   BSL_KIN_TENSOR where the grid allows it; BSL_ERR_UNSUPPORTED when it does not. */
+int bsl_set_kinetic_engine(bsl_handle* h, int engine);
+int bsl_kinetic_engine(const bsl_handle* h);
 
 /* uec += H vec with host buffers in the reference layout.  Replaces
    Hv_linRotCartSph_NoQuad (linRotCartSphHvFullVPrepRoutines.cpp:807-822):

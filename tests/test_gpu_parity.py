@@ -62,9 +62,30 @@ def test_hv_cpu_workload_fp64_and_mixed(bsl):
     assert rel(u[s["idx"]], s["val"]) <= 1e-10
     assert abs(np.linalg.norm(u) - man["hv_norm"]) <= 1e-10 * man["hv_norm"]
     h.set_precision("mixed")
-    um = np.zeros(h.basis_size)
-    h.hv(v, um)
-    assert rel(um, u) <= 2e-6
+    for engine in ("simt", "tensor"):
+        h.set_kinetic_engine(engine)
+        um = np.zeros(h.basis_size)
+        h.hv(v, um)
+        assert rel(um, u) <= 2e-6, engine
+    h.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_hv_mixed_engines_match_fp64(bsl, name):
+    """Both kinetic engines of the mixed path against the FP64 path (2e-6 relative)."""
+    h, d, man, _ = make(bsl, name)
+    v = np.random.default_rng(man["hv_seed"]).standard_normal(h.basis_size)
+    u = np.zeros(h.basis_size)
+    h.hv(v, u)
+    h.set_precision("mixed")
+    assert h.kinetic_engine() == "tensor"  # every fixture grid fits the tensor-core tiles
+    out = {}
+    for engine in ("simt", "tensor"):
+        h.set_kinetic_engine(engine)
+        out[engine] = np.zeros(h.basis_size)
+        h.hv(v, out[engine])
+        assert rel(out[engine], u) <= 2e-6, (engine, rel(out[engine], u))
+    assert rel(out["tensor"], out["simt"]) <= 2e-6
     h.close()
 
 
@@ -126,13 +147,15 @@ def test_lanczos_fp64_eigenvalues_match_reference(bsl, name):
     h.close()
 
 
-def test_lanczos_mixed_levels_within_1e3_cm(bsl):
+@pytest.mark.parametrize("engine", ["simt", "tensor"])
+def test_lanczos_mixed_levels_within_1e3_cm(bsl, engine):
     h, d, man, _ = make(bsl, "cpu_workload")
     niter = man["niter"]
     a, b, b2 = h.lanczos(niter, start="normal", seed=0)
     # bound levels: the lowest 20 converged levels below 30 kJ/mol
     stable = stable_levels(a, b[1:], emax=30.0)
     h.set_precision("mixed")
+    h.set_kinetic_engine(engine)
     am, bm, bm2 = h.lanczos(niter, start="normal", seed=0)
     evm, _ = bsl.good_eigenvalues(am, bm, bm2, -10.0, 40.0)
     low = np.sort(stable)[:20]
