@@ -198,6 +198,8 @@ def main():
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="prep plus this many iterations only (for profiler captures)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--dump-lanczos", default="",
+                    help="save the alpha/beta histories of the accuracy runs to this .npz file")
     ap.add_argument("--kinetic", default="auto", choices=["auto", "simt", "tensor"],
                     help="kinetic engine of the mixed path (auto: tensor cores where the grid allows)")
     args = ap.parse_args()
@@ -313,6 +315,8 @@ def main():
         a64, b64, b264 = h.lanczos(n_it, start="normal", seed=0)
         h.set_precision("mixed")
         am, bm, bm2 = h.lanczos(n_it, start="normal", seed=0)
+        if args.dump_lanczos:
+            np.savez(args.dump_lanczos, a64=a64, b64=b64, b264=b264, am=am, bm=bm, bm2=bm2)
         ref_levels = np.sort(stable_levels(bsl, a64, b64, b264))[:cfg["levels"]]
         evm, _ = bsl.good_eigenvalues(am, bm, bm2, -1.0e3, 1.0e3)
         stable_m = stable_levels(bsl, am, bm, bm2)

@@ -56,6 +56,55 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 }
 
 // ---------------------------------------------------------------------------
+// Double-float arithmetic on the FP32 pipe.  A value is the unevaluated sum
+// x + y of a float2 with |y| <= ulp(x)/2 (about 48 significant bits).
+// Algorithms: Dekker's exact product and fast two-sum (Numer. Math. 18, 1971),
+// Knuth's TwoSum, and the accurate addition of Hida, Li and Bailey's
+// double-double library (ARITH-15, 2001) restated for FP32 components.  Every
+// step uses the _rn intrinsics so that nothing is contracted or reassociated.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {  // |a| >= |b|
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  float s1, s2, t1, t2;
+  two_sum(a.x, b.x, s1, s2);
+  two_sum(a.y, b.y, t1, t2);
+  s2 = __fadd_rn(s2, t1);
+  fast_two_sum(s1, s2, s1, s2);
+  s2 = __fadd_rn(s2, t2);
+  fast_two_sum(s1, s2, s1, s2);
+  return make_float2(s1, s2);
+}
+
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  float s, t;
+  fast_two_sum(p, e, s, t);
+  return make_float2(s, t);
+}
+
+// a * b + c
+__device__ __forceinline__ float2 df_fma(float2 a, float2 b, float2 c) { return df_add(df_mul(a, b), c); }
+
+__device__ __forceinline__ float2 df_scale2(float2 a, float g) {  // g a power of two: exact
+  return make_float2(__fmul_rn(a.x, g), __fmul_rn(a.y, g));
+}
+
+// double-float nearest to an FP64 number (one FP64 subtraction)
+__device__ __forceinline__ float2 df_of(double d) {
+  const float hi = f32_round(d);
+  return make_float2(hi, f32_round(d - f64_of(hi)));
+}
+
+__device__ __forceinline__ double f64_of_df(float2 a) { return f64_of(a.x) + f64_of(a.y); }
+
+// ---------------------------------------------------------------------------
 // reductions: block sum, then the last block to finish sums the per-block
 // partials in a fixed order (deterministic, no second launch).
 // ---------------------------------------------------------------------------
@@ -76,6 +125,46 @@ __device__ __forceinline__ double block_sum(double v) {
   v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
   if (wid == 0) v = warp_sum(v);
   return v;  // valid in thread 0
+}
+
+__device__ __forceinline__ float2 warp_sum_df(float2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = df_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)));
+  return v;
+}
+
+// reduce_grid for double-float per-thread parts: the block sums run on the
+// FP32 pipe (double-float shuffles), only one FP64 value per block is formed,
+// and the last block adds the per-block values in FP64 in a fixed order.
+__device__ __forceinline__ bool reduce_grid_df(float2 part, double* partials, unsigned int* counter,
+                                               double* total) {
+  __shared__ float2 shd[32];
+  __shared__ bool last_df;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2 v = warp_sum_df(part);
+  if (lane == 0) shd[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    v = warp_sum_df(lane < nw ? shd[lane] : make_float2(0.f, 0.f));
+    if (lane == 0) {
+      partials[blockIdx.x] = f64_of_df(v);
+      __threadfence();
+      last_df = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  if (!last_df) return false;
+  __threadfence();
+  double acc = 0.0;
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) acc += __ldcg(partials + b);
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) {
+    *total = acc;
+    *counter = 0u;
+  }
+  return true;
 }
 
 // Stores this block's partial; returns true (in every thread) for the last

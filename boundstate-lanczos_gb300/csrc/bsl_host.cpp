@@ -267,10 +267,8 @@ void free_device(DeviceState& d) {
                   d.scalars, d.status, d.hist, d.ref_vec, d.ref_out, d.full_of, d.ritz};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  for (int i = 0; i < 3; ++i) {
-    if (d.kxy_tf32[i]) cudaFree(d.kxy_tf32[i]);
-    if (d.kz_tf32[i]) cudaFree(d.kz_tf32[i]);
-  }
+  if (d.kxy_slices) cudaFree(d.kxy_slices);
+  if (d.kz_slices) cudaFree(d.kz_slices);
   if (d.ev0) cudaEventDestroy(d.ev0);
   if (d.ev1) cudaEventDestroy(d.ev1);
   if (d.stream) cudaStreamDestroy(d.stream);
@@ -438,16 +436,11 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
   kinetic_split_tables(t.tz, t.nz, false, &hi, &lo);
   if ((rc = upload(&d.kz_head, hi, "Tz")) || (rc = upload(&d.kz_band, lo, "Tz"))) return bail(rc);
   if (kinetic_tc_supported(t)) {
-    std::vector<float> t1, t2, t3;
-    kinetic_tf32_tables(t.tx, t.nx, &t1, &t2, &t3);
-    if ((rc = upload(&d.kxy_tf32[0], t1, "Tx")) || (rc = upload(&d.kxy_tf32[1], t2, "Tx")) ||
-        (rc = upload(&d.kxy_tf32[2], t3, "Tx")))
-      return bail(rc);
-    kinetic_tf32_tables(t.tz, t.nz, &t1, &t2, &t3);
-    if ((rc = upload(&d.kz_tf32[0], t1, "Tz")) || (rc = upload(&d.kz_tf32[1], t2, "Tz")) ||
-        (rc = upload(&d.kz_tf32[2], t3, "Tz")))
-      return bail(rc);
-    h->kinetic_engine = BSL_KIN_TENSOR;
+    std::vector<uint16_t> sl;
+    kinetic_f16_slices(t.tx, t.nx, &sl, &d.e_txy);
+    if ((rc = upload(&d.kxy_slices, sl, "Tx"))) return bail(rc);
+    kinetic_f16_slices(t.tz, t.nz, &sl, &d.e_tz);
+    if ((rc = upload(&d.kz_slices, sl, "Tz"))) return bail(rc);
   }
   if ((rc = upload(&d.rot, t.rot, "rotor"))) return bail(rc);
   {
@@ -516,7 +509,7 @@ int bsl_set_precision(bsl_handle* h, int precision) {
 int bsl_set_kinetic_engine(bsl_handle* h, int engine) {
   if (!h) return fail(BSL_ERR_STATE, "null handle");
   if (engine != BSL_KIN_SIMT && engine != BSL_KIN_TENSOR) return fail(BSL_ERR_INPUT, "unknown kinetic engine");
-  if (engine == BSL_KIN_TENSOR && !h->d.kxy_tf32[0])
+  if (engine == BSL_KIN_TENSOR && !h->d.kxy_slices)
     return fail(BSL_ERR_UNSUPPORTED, "tensor-core kinetic needs at most 64 points per axis and equal x and y axes");
   h->kinetic_engine = engine;
   return BSL_OK;
@@ -539,6 +532,7 @@ int bsl_hv_apply(bsl_handle* h, const double* vec, double* uec) {
   if (!d.ref_vec && ((rc = dalloc(&d.ref_vec, Df, "staging")) || (rc = dalloc(&d.ref_out, Df, "staging")))) return rc;
   cudaStream_t s = d.stream;
   // the device Lanczos vectors serve as packed scratch here
+  h->state_pairs = -1;
   BSL_CUDA(cudaMemcpyAsync(d.ref_vec, vec, Df * sizeof(double), cudaMemcpyHostToDevice, s));
   BSL_CUDA(cudaMemcpyAsync(d.ref_out, uec, Df * sizeof(double), cudaMemcpyHostToDevice, s));
   if ((rc = dev_gather_packed(h, d.ref_vec, d.vec, s))) return rc;

@@ -69,9 +69,10 @@ struct DeviceState {
   // FP32 heads fl32(T) and tails fl32(T - head), both stored transposed, for the mixed kernels
   float *kx_head = nullptr, *ky_head = nullptr, *kz_head = nullptr;
   float *kx_band = nullptr, *ky_band = nullptr, *kz_band = nullptr;
-  // TF32 splits T = T1 + T2 + T3 as zero-padded 64 x 64 tiles, for the tensor-core kinetic
-  float* kxy_tf32[3] = {nullptr, nullptr, nullptr};
-  float* kz_tf32[3] = {nullptr, nullptr, nullptr};
+  // fixed-point FP16 slices of T (4 zero-padded 64 x 64 tiles) and their scale
+  // exponents, for the tensor-core kinetic
+  uint16_t *kxy_slices = nullptr, *kz_slices = nullptr;
+  int e_txy = 0, e_tz = 0;
   int kin_grid_xy = 0, kin_grid_z = 0;  // persistent grid sizes
   double* rot = nullptr;  // [nn]
   // potential grid V(p, a, b) for phi_b and 2pi - phi_b, p in vector order
@@ -85,7 +86,9 @@ struct DeviceState {
   float *rot_hi = nullptr, *rot_lo = nullptr; // rotor energies as FP32 head + tail
   double* partials = nullptr;  // one double per reduction block
   unsigned int* counter = nullptr;
-  // [0] alpha_j, [1] beta_j, [2] beta2_j, [3] 1/beta_j, [4] sv, [5] sr, [6] sv/sr, [7] sv*sr
+  // [0] alpha_j, [1] beta_j, [2] beta2_j, [3] 1/beta_j, [4] sv, [5] sr, [6] sv/sr, [7] sv*sr;
+  // pair state: [8] sv/sr and [9] -alpha sv/sr as double-float pairs, [10] (int) exponent of
+  // the update's power-of-two factor
   double* scalars = nullptr;
   // [0] breakdown, [1] its iteration, [2] potential-block stream timeout, [3] tensor-core kinetic timeout
   int* status = nullptr;
@@ -110,6 +113,7 @@ struct bsl_handle {
   int kinetic_engine = BSL_KIN_SIMT;  // engine of the mixed-precision kinetic (BSL_KIN_*)
   double last_ms_per_iter = 0.0;
   int lanczos_flip = 0;           // 0: vec holds v_j and rvec r_j; 1: roles swapped
+  int state_pairs = -1;           // Lanczos buffers: 0 FP64, 1 double-float pairs (mixed), -1 not set up
   double init_scalars[8] = {0, 0, 0, 0, 1, 1, 1, 1};  // alpha, beta, beta2, 1/beta, sv, sr, sv/sr, sv*sr
 };
 
@@ -140,8 +144,7 @@ int launch_kin_z_mixed(bsl_handle* h, const float* v, cudaStream_t s);
 
 // tensor-core kinetic (bsl_kinetic_tc.cu): the same contract as the mixed
 // kernels, for grids of at most 64 points per axis with Tx = Ty
-void kinetic_tf32_tables(const std::vector<double>& T, int n, std::vector<float>* t1, std::vector<float>* t2,
-                         std::vector<float>* t3);
+void kinetic_f16_slices(const std::vector<double>& T, int n, std::vector<uint16_t>* slices, int* e_t);
 bool kinetic_tc_supported(const Tables& t);
 int launch_kin_xy_tc(bsl_handle* h, const float* v, cudaStream_t s);
 int launch_kin_z_tc(bsl_handle* h, const float* v, cudaStream_t s);
@@ -157,6 +160,7 @@ struct StreamArgs {
   const float* rot_lo;
   double* out;          // mode 0: u = H v; mode 1: the Lanczos r buffer (r += c H v)
   long long npts, dpk;
+  long long tiles_per_cta;  // set by the launcher
   int mode, j;
   double *partials, *scalars, *hist;
   unsigned int* counter;

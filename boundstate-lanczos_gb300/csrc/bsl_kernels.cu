@@ -356,6 +356,95 @@ __global__ void k_update_fold(const double* __restrict__ V, double* __restrict__
   }
 }
 
+// k_update_fold for Lanczos buffers stored as double-float pairs (mixed
+// precision): every per-element operation runs on the FP32 pipe.  The new R
+// buffer is also multiplied by a power of two g (exact) chosen from the
+// previous beta so that its norm stays near 1 whatever the scales sv, sr do
+// over many iterations: the FP32 exponent range of the pairs (and of the FP32
+// copy the kinetic reads) is never approached.  The logical r keeps its value
+// through sr / g.
+__global__ void __launch_bounds__(256, 4) k_update_pair(const float2* __restrict__ V, float2* __restrict__ R,
+                                                        long long L, float* __restrict__ v32_next, long long D,
+                                                        double* partials, unsigned int* counter, double* scalars,
+                                                        double* hist, int hist_stride, int j, int* status) {
+  // per-thread constants prepared by the previous kernels' last blocks (no FP64 work per thread)
+  const float2 na = reinterpret_cast<const float2*>(scalars)[9];  // -alpha c
+  const int e = reinterpret_cast<const int*>(scalars)[20];         // g = 2^e, e = ilogb(sr) - ilogb(beta_{j-1})
+  const float g = ldexpf(1.f, e);
+  float2 acc = make_float2(0.f, 0.f);
+  // two elements per 16-byte access, kUnroll accesses in flight per thread
+  constexpr int kUnroll = 4;
+  const long long L2 = L / 2;
+  const float4* V4 = reinterpret_cast<const float4*>(V);
+  float4* R4 = reinterpret_cast<float4*>(R);
+  const long long stride = (long long)gridDim.x * blockDim.x * kUnroll;
+  for (long long base = (long long)blockIdx.x * blockDim.x * kUnroll + threadIdx.x; base < L2; base += stride) {
+    float4 v[kUnroll], r[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const long long q = base + (long long)u * blockDim.x;
+      if (q < L2) {
+        v[u] = V4[q];
+        r[u] = R4[q];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const long long q = base + (long long)u * blockDim.x;
+      if (q < L2) {
+        const float2 r0 = df_scale2(df_fma(na, make_float2(v[u].x, v[u].y), make_float2(r[u].x, r[u].y)), g);
+        const float2 r1 = df_scale2(df_fma(na, make_float2(v[u].z, v[u].w), make_float2(r[u].z, r[u].w)), g);
+        R4[q] = make_float4(r0.x, r0.y, r1.x, r1.y);
+        acc = df_fma(r0, r0, acc);
+        acc = df_fma(r1, r1, acc);
+        const long long e0 = 2 * q;
+        if (e0 + 1 < D)
+          reinterpret_cast<float2*>(v32_next)[q] = make_float2(r0.x, r1.x);
+        else if (e0 < D)
+          v32_next[e0] = r0.x;
+      }
+    }
+  }
+  if ((L & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const long long i = L - 1;
+    const float2 r = df_scale2(df_fma(na, V[i], R[i]), g);
+    R[i] = r;
+    acc = df_fma(r, r, acc);
+    if (i < D) v32_next[i] = r.x;
+  }
+  double total;
+  if (reduce_grid_df(acc, partials, counter, &total) && threadIdx.x == 0) {
+    const double alpha = scalars[0], sv = scalars[4], sr = scalars[5];
+    const double sr_g = ldexp(sr, -e);  // r = (sr / g) R_new
+    const double b2 = sr_g * sr_g * total;
+    const double b = sqrt(b2);
+    scalars[1] = b;
+    scalars[2] = b2;
+    scalars[3] = 1. / b;
+    hist[hist_stride + j] = b;
+    hist[2 * hist_stride + j] = b2;
+    const double sv_n = sr_g / b, sr_n = -b * sv;
+    scalars[4] = sv_n;
+    scalars[5] = sr_n;
+    scalars[6] = sv_n / sr_n;
+    scalars[7] = sv_n * sr_n;
+    reinterpret_cast<float2*>(scalars)[8] = df_of(sv_n / sr_n);
+    // next update: ||R_next|| = beta_{j+1} / |sr_n| ~ b / |sr_n|, so g = 2^(ilogb(sr_n) - ilogb(b))
+    int en = (b > 0.0 && isfinite(b) && sr_n != 0.0) ? ilogb(sr_n) - ilogb(b) : 0;
+    reinterpret_cast<int*>(scalars)[20] = max(-60, min(60, en));
+    if (!(b > 0.0) || !isfinite(b) || !isfinite(alpha)) {
+      if (status[0] == 0) status[1] = j;
+      status[0] = 1;
+    }
+  }
+}
+
+// FP64 vector to double-float pairs in place (same 8 bytes per element)
+__global__ void k_to_pair(double* x, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    reinterpret_cast<float2*>(x)[i] = df_of(x[i]);
+}
+
 // FP32 copy (rounded to nearest, integer pipe) of an FP64 vector
 __global__ void k_to_f32(const double* __restrict__ x, float* __restrict__ y, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -391,10 +480,10 @@ __global__ void k_scatter_add(const double* __restrict__ packed, double* __restr
 // ritz[n*D + i] += coef[n] * v[i] for active n, v = scalars[4] * V
 __global__ void k_ritz(const double* __restrict__ V, long long D, const double* __restrict__ coef,
                        const int* __restrict__ active, int ngood, double* __restrict__ ritz,
-                       const double* __restrict__ scalars) {
+                       const double* __restrict__ scalars, int pairs) {
   const double sv = scalars[4];
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (long long)gridDim.x * blockDim.x) {
-    const double vi = sv * V[i];
+    const double vi = sv * (pairs ? f64_of_df(reinterpret_cast<const float2*>(V)[i]) : V[i]);
     for (int n = 0; n < ngood; ++n)
       if (active[n]) ritz[(long long)n * D + i] += coef[n] * vi;
   }
@@ -607,6 +696,20 @@ int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s) {
   return launch_vapply(h, v, u, 0, 0, s);
 }
 
+// r -= alpha v, beta and the next scales, on FP64 or double-float buffers
+int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaStream_t s) {
+  DeviceState& d = h->d;
+  if (h->state_pairs == 1)
+    k_update_pair<<<d.red_blocks, kThreads, 0, s>>>(reinterpret_cast<const float2*>(V), reinterpret_cast<float2*>(R),
+                                                    L, d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
+                                                    d.hist_cap, j, d.status);
+  else
+    k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
+                                                    d.hist_cap, j, d.status);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
 int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s) {
   DeviceState& d = h->d;
   const long long L = bsl_packed_size(h) + 1;  // + the coordinate outside the symmetry block
@@ -614,10 +717,8 @@ int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s) {
   double* R = h->lanczos_flip ? d.vec : d.rvec;
   int rc = launch_kinetic(h, V, s);
   if (rc) return rc;
-  if ((rc = launch_vapply(h, V, R, 1, j, s))) return rc;
-  k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
-                                                  d.hist_cap, j, d.status);
-  BSL_CUDA(cudaGetLastError());
+  if ((rc = launch_vapply(h, V, R, h->state_pairs == 1 ? 2 : 1, j, s))) return rc;
+  if ((rc = launch_update(h, V, R, L, j, s))) return rc;
   h->lanczos_flip ^= 1;
   return BSL_OK;
 }
@@ -650,10 +751,9 @@ int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_
     k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(V, d.ukin, d.tz, t.nx, t.ny, t.nz);
   }
   cudaEventRecord(ev[2], s);
-  if ((rc = launch_vapply(h, V, R, 1, j, s))) return rc;
+  if ((rc = launch_vapply(h, V, R, h->state_pairs == 1 ? 2 : 1, j, s))) return rc;
   cudaEventRecord(ev[3], s);
-  k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
-                                                  d.hist_cap, j, d.status);
+  if ((rc = launch_update(h, V, R, L, j, s))) return rc;
   cudaEventRecord(ev[4], s);
   BSL_CUDA(cudaGetLastError());
   h->lanczos_flip ^= 1;
@@ -663,10 +763,16 @@ int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_
 const char* dev_stage_name(bsl_handle* h, int i) {
   const bool mixed = h->precision == BSL_PREC_MIXED;
   static const char* n64[4] = {"k_kin_xy_f64", "k_kin_z_f64", "k_vapply<NN,double>", "k_update_fold"};
-  static const char* nmx[4] = {"k_kin_xy_split", "k_kin_z_split", "k_vstream<NN>", "k_update_fold"};
-  static const char* ntc[4] = {"k_kin_xy_tc", "k_kin_z_tc", "k_vstream<NN>", "k_update_fold"};
+  static const char* nmx[4] = {"k_kin_xy_split", "k_kin_z_split", "k_vstream<NN>", "k_update_pair"};
+  static const char* ntc[4] = {"k_kin_xy_tc", "k_kin_z_tc", "k_vstream<NN>", "k_update_pair"};
   if (!mixed) return n64[i];
   return h->kinetic_engine == BSL_KIN_TENSOR ? ntc[i] : nmx[i];
+}
+
+int dev_to_pair(double* x, long long n, cudaStream_t s) {
+  k_to_pair<<<1024, kThreads, 0, s>>>(x, n);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
 }
 
 int dev_to_f32(const double* x, float* y, long long n, cudaStream_t s) {
@@ -710,7 +816,7 @@ int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, in
                         cudaStream_t s) {
   const long long L = bsl_packed_size(h) + 1;  // with the coordinate outside the symmetry block
   const double* V = h->lanczos_flip ? h->d.rvec : h->d.vec;
-  k_ritz<<<1024, kThreads, 0, s>>>(V, L, coef, active, ngood, ritz, h->d.scalars);
+  k_ritz<<<1024, kThreads, 0, s>>>(V, L, coef, active, ngood, ritz, h->d.scalars, h->state_pairs == 1);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }

@@ -24,6 +24,7 @@
 namespace bsl {
 int dev_fill(double* x, long long L, double val, cudaStream_t s);
 int dev_to_f32(const double* x, float* y, long long n, cudaStream_t s);
+int dev_to_pair(double* x, long long n, cudaStream_t s);
 int dev_full_step(bsl_handle* h, double* v, double* r, long long L, int j, cudaStream_t s);
 
 namespace {
@@ -95,7 +96,14 @@ int init_state(bsl_handle* h, int start, unsigned long long seed) {
   BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
   BSL_CUDA(cudaMemsetAsync(d.scalars, 0, 16 * sizeof(double), s));
   BSL_CUDA(cudaMemcpyAsync(d.scalars, h->init_scalars, 8 * sizeof(double), cudaMemcpyHostToDevice, s));
+  // pair-state constants: [8] c = 1 as a double-float pair, [10] the update's exponent 0
+  static const float kOnePair[2] = {1.f, 0.f};
+  BSL_CUDA(cudaMemcpyAsync(d.scalars + 8, kOnePair, sizeof(kOnePair), cudaMemcpyHostToDevice, s));
   if ((rc = dev_to_f32(d.vec, d.v32, D, s))) return rc;
+  // mixed precision keeps the Lanczos buffers as double-float pairs (the zero
+  // R buffer is the same bits either way)
+  h->state_pairs = h->precision == BSL_PREC_MIXED ? 1 : 0;
+  if (h->state_pairs && (rc = dev_to_pair(d.vec, D + 1, s))) return rc;
   h->lanczos_flip = 0;
   return BSL_OK;
 }
@@ -157,7 +165,9 @@ int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alph
   BSL_CUDA(cudaMemcpyAsync(d.ref_vec, vec, Df * sizeof(double), cudaMemcpyHostToDevice, s));
   BSL_CUDA(cudaMemcpyAsync(d.ref_out, rvec, Df * sizeof(double), cudaMemcpyHostToDevice, s));
   BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
-  // r += S H v: H on the packed block, nothing elsewhere
+  // r += S H v: H on the packed block, nothing elsewhere (the device Lanczos
+  // vectors serve as packed scratch)
+  h->state_pairs = -1;
   if ((rc = dev_gather_packed(h, d.ref_vec, d.vec, s))) return rc;
   if ((rc = dev_hv(h, d.vec, d.rvec, s))) return rc;
   if ((rc = dev_scatter_full(h, d.rvec, d.ref_out, s))) return rc;
@@ -247,6 +257,9 @@ int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names) {
   DeviceState& d = h->d;
   int rc;
   if ((rc = ensure_hist(h, iters))) return rc;
+  // the state must match the current precision's buffer format
+  if (h->state_pairs != (h->precision == BSL_PREC_MIXED ? 1 : 0) && (rc = init_state(h, BSL_START_UNIFORM, 0)))
+    return rc;
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; ++i) BSL_CUDA(cudaEventCreate(&ev[i]));
   const int nst = 4;

@@ -11,9 +11,10 @@
 // so one tile's ntri x kTilePts floats are contiguous and a chunk of kChunk
 // rows is one contiguous copy of kChunk * 512 bytes.
 //
-// One CTA per tile of 128 grid points, one thread per point:
+// One thread per grid point of a tile of 128 points:
 //   u(s) = ukin(s) + B l(l+1) v(s) + sum_s' V_ss' v(s')   (FP32 block product, FP32-pair sums)
-//   mode 0: out = u (FP64);   mode 1: R += c u (FP64), partial alpha = V . R (deterministic grid reduction)
+//   mode 0: out = u (FP64);   mode 1: R += c u (FP64), partial alpha = V . R (deterministic grid reduction);
+//   mode 2: mode 1 with V and R as double-float pairs
 #include "bsl_device.cuh"
 
 namespace bsl {
@@ -55,13 +56,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return true;
 }
 
-__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+// L2 policy for the block stream: read once per iteration, so evicted first and
+// the Lanczos vectors (about 90 MB at 54^3) have the best chance to stay in L2
+__device__ __forceinline__ uint64_t evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+__device__ __forceinline__ void bulk_copy_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                               uint64_t pol) {
   asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
       : "memory");
 }
 
+// Persistent: CTA b owns the contiguous tiles [b * A.tiles_per_cta, ...), and
+// its copy ring runs across tile boundaries, so the next tile's blocks are in
+// flight while the current tile finishes its epilogue.
 template <int NN>
 __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
   constexpr int NT = NN * (NN + 1) / 2;
@@ -69,11 +83,16 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
   extern __shared__ float4 ring4[];
   float* ring = reinterpret_cast<float*>(ring4);  // [kStages][kChunk][kTilePts]
   __shared__ uint64_t full[kStages];
-  __shared__ int abort_flag, issued;
+  __shared__ int abort_flag;
+  __shared__ long long issued;
   const int tid = threadIdx.x;
-  const long long tile = blockIdx.x;
   const long long npts = A.npts;
-  const float* src_tile = A.vb + tile * (long long)NT * kTilePts;
+  const long long ntiles = (npts + kTilePts - 1) / kTilePts;
+  const long long t0 = (long long)blockIdx.x * A.tiles_per_cta;
+  const long long t1 = t0 + A.tiles_per_cta < ntiles ? t0 + A.tiles_per_cta : ntiles;
+  const long long nchunks = (t1 > t0 ? t1 - t0 : 0) * NCH;
+  const float* src0 = A.vb + t0 * (long long)NT * kTilePts;
+  const uint64_t pol = evict_first_policy();
   if (tid == 0) {
     // a stream that already timed out in an earlier launch disables the copies
     // (and every wait) of later launches until the host has seen the error
@@ -83,74 +102,113 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  auto issue = [&](int c) {
-    const int st = c % kStages;
+  // chunk g of this CTA: tile t0 + g / NCH, rows [c * kChunk, ...) with c = g % NCH
+  auto issue = [&](long long g) {
+    const int st = (int)(g % kStages);
+    const int c = (int)(g % NCH);
     const int rows = (c == NCH - 1) ? (NT - c * kChunk) : kChunk;
     const uint32_t bytes = (uint32_t)rows * kTilePts * sizeof(float);
     mbar_expect_tx(&full[st], bytes);
-    issued = c + 1;
-    bulk_copy(ring + (size_t)st * kChunk * kTilePts, src_tile + (size_t)c * kChunk * kTilePts, bytes, &full[st]);
+    issued = g + 1;
+    bulk_copy_hint(ring + (size_t)st * kChunk * kTilePts,
+                   src0 + ((g / NCH) * NT + (long long)c * kChunk) * kTilePts, bytes, &full[st], pol);
   };
   if (tid == 0 && !abort_flag)
-    for (int c = 0; c < NCH && c < kStages; ++c) issue(c);
+    for (long long g = 0; g < nchunks && g < kStages; ++g) issue(g);
 
-  const long long p = tile * kTilePts + tid;
-  const bool valid = p < npts;
-  if (valid) {
+  const float2* Vp = reinterpret_cast<const float2*>(A.vec);
+  float2* Rp = reinterpret_cast<float2*>(A.out);
+  const double c = A.mode == 1 ? A.scalars[6] : 1.0;
+  const float2 cc = reinterpret_cast<const float2*>(A.scalars)[8];  // c as a pair (mode 2)
+  double dot = 0.0;
+  float2 dacc = make_float2(0.f, 0.f);
+  long long g0 = 0;  // first chunk of the current tile
+  for (long long tile = t0; tile < t1; ++tile, g0 += NCH) {
+    const long long p = tile * kTilePts + tid;
+    const bool valid = p < npts;
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < NN; ++s) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(A.ukin + s * npts + p));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(A.out + s * npts + p));
+        if (A.mode) asm volatile("prefetch.global.L2 [%0];" ::"l"(A.vec + s * npts + p));
+      }
+    }
+    float vv[NN], va[NN];
 #pragma unroll
     for (int s = 0; s < NN; ++s) {
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(A.ukin + s * npts + p));
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(A.out + s * npts + p));
+      vv[s] = valid ? A.v32[s * npts + p] : 0.f;
+      va[s] = 0.f;
     }
-  }
-  float vv[NN], va[NN];
+    int t = 0;
 #pragma unroll
-  for (int s = 0; s < NN; ++s) {
-    vv[s] = valid ? A.v32[s * npts + p] : 0.f;
-    va[s] = 0.f;
-  }
-  int t = 0;
+    for (int s = 0; s < NN; ++s) {
 #pragma unroll
-  for (int s = 0; s < NN; ++s) {
-#pragma unroll
-    for (int q = s; q < NN; ++q, ++t) {
-      const int c = t / kChunk;
-      const int st = c % kStages;
-      if (t % kChunk == 0) {
-        if (!abort_flag && !mbar_wait(&full[st], (uint32_t)((c / kStages) & 1))) abort_flag = 1;
-      }
-      const float x = ring[((size_t)st * kChunk + (t % kChunk)) * kTilePts + tid];
-      va[s] = fmaf(x, vv[q], va[s]);
-      if (q != s) va[q] = fmaf(x, vv[s], va[q]);
-      if (t % kChunk == kChunk - 1 || t == NT - 1) {
-        __syncthreads();  // every thread is done with this stage
-        if (tid == 0 && !abort_flag && c + kStages < NCH) {
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          issue(c + kStages);
+      for (int q = s; q < NN; ++q, ++t) {
+        const long long g = g0 + t / kChunk;
+        const int st = (int)(g % kStages);
+        if (t % kChunk == 0) {
+          if (!abort_flag && !mbar_wait(&full[st], (uint32_t)((g / kStages) & 1))) abort_flag = 1;
+        }
+        const float x = ring[((size_t)st * kChunk + (t % kChunk)) * kTilePts + tid];
+        va[s] = fmaf(x, vv[q], va[s]);
+        if (q != s) va[q] = fmaf(x, vv[s], va[q]);
+        if (t % kChunk == kChunk - 1 || t == NT - 1) {
+          __syncthreads();  // every thread is done with this stage
+          if (tid == 0 && !abort_flag && g + kStages < nchunks) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(g + kStages);
+          }
         }
       }
     }
-  }
-  // u = kinetic pair + B l(l+1) v + V v as an FP32 pair, then one FP64 value.
-  // mode 1: the logical vectors are v = sv V and r = sr R; r + H v is kept as
-  // sr (R + (sv/sr) H V), so R' = R + c H V and alpha = sv sr (V . R').
-  const double c = A.mode ? A.scalars[6] : 1.0;
-  double dot = 0.0;
-  if (valid) {
+    // u = kinetic pair + B l(l+1) v + V v as an FP32 pair.
+    // mode 1: the logical vectors are v = sv V and r = sr R; r + H v is kept as
+    // sr (R + (sv/sr) H V), so R' = R + c H V and alpha = sv sr (V . R').
+    // mode 2: the same with V and R stored as double-float pairs, all on the FP32 pipe.
+    if (valid) {
+      if (A.mode == 2) {
+        constexpr int kGroup = 7;  // loads of kGroup functions in flight before their arithmetic
 #pragma unroll
-    for (int s = 0; s < NN; ++s) {
-      const float2 uk = A.ukin[s * npts + p];
-      const float a = fmaf(__ldg(A.rot_hi + s), vv[s], va[s]);
-      float hi, e;
-      two_sum(uk.x, a, hi, e);
-      const float lo = uk.y + e + __ldg(A.rot_lo + s) * vv[s];
-      const double hv = f64_of(hi) + f64_of(lo);
-      if (A.mode == 0) {
-        A.out[s * npts + p] = hv;
+        for (int s0 = 0; s0 < NN; s0 += kGroup) {
+          float2 uk[kGroup], rr[kGroup], vq[kGroup];
+#pragma unroll
+          for (int u = 0; u < kGroup; ++u)
+            if (s0 + u < NN) {
+              uk[u] = A.ukin[(s0 + u) * npts + p];
+              rr[u] = Rp[(s0 + u) * npts + p];
+              vq[u] = Vp[(s0 + u) * npts + p];
+            }
+#pragma unroll
+          for (int u = 0; u < kGroup; ++u)
+            if (s0 + u < NN) {
+              const int s = s0 + u;
+              const float a = fmaf(__ldg(A.rot_hi + s), vv[s], va[s]);
+              float hi, e, lo;
+              two_sum(uk[u].x, a, hi, e);
+              two_sum(hi, uk[u].y + e + __ldg(A.rot_lo + s) * vv[s], hi, lo);
+              const float2 r = df_fma(cc, make_float2(hi, lo), rr[u]);
+              Rp[s * npts + p] = r;
+              dacc = df_fma(vq[u], r, dacc);
+            }
+        }
       } else {
-        const double r = fma(c, hv, A.out[s * npts + p]);
-        A.out[s * npts + p] = r;
-        dot = fma(A.vec[s * npts + p], r, dot);
+#pragma unroll
+        for (int s = 0; s < NN; ++s) {
+          const float2 uk = A.ukin[s * npts + p];
+          const float a = fmaf(__ldg(A.rot_hi + s), vv[s], va[s]);
+          float hi, e;
+          two_sum(uk.x, a, hi, e);
+          const float lo = uk.y + e + __ldg(A.rot_lo + s) * vv[s];
+          const double hv = f64_of(hi) + f64_of(lo);
+          if (A.mode == 0) {
+            A.out[s * npts + p] = hv;
+          } else {
+            const double r = fma(c, hv, A.out[s * npts + p]);
+            A.out[s * npts + p] = r;
+            dot = fma(A.vec[s * npts + p], r, dot);
+          }
+        }
       }
     }
   }
@@ -158,26 +216,42 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
     // a copy did not complete in time: record it and give the copies still in
     // flight a bounded chance to land before the CTA's shared memory is released
     A.status[2] = 1;
-    for (int cc = issued - kStages; cc < issued; ++cc)
-      if (cc >= 0) mbar_wait(&full[cc % kStages], (uint32_t)((cc / kStages) & 1));
+    for (long long g = issued - kStages; g < issued; ++g)
+      if (g >= 0) mbar_wait(&full[g % kStages], (uint32_t)((g / kStages) & 1));
   }
-  if (A.mode == 1) {
-    if (p == 0) dot = fma(A.vec[A.dpk], A.out[A.dpk], dot);  // extra coordinate: H acts as 0, R' = R
+  if (A.mode != 0) {
+    // extra coordinate: H acts as 0, R' = R
+    if (blockIdx.x == 0 && tid == 0) {
+      if (A.mode == 2)
+        dacc = df_fma(Vp[A.dpk], Rp[A.dpk], dacc);
+      else
+        dot = fma(A.vec[A.dpk], A.out[A.dpk], dot);
+    }
     double total;
-    if (reduce_grid(dot, A.partials, A.counter, &total) && threadIdx.x == 0) {
+    const bool last = A.mode == 2 ? reduce_grid_df(dacc, A.partials, A.counter, &total)
+                                  : reduce_grid(dot, A.partials, A.counter, &total);
+    if (last && threadIdx.x == 0) {
       const double alpha = A.scalars[7] * total;
       A.scalars[0] = alpha;
       A.hist[A.j - 1] = alpha;
+      reinterpret_cast<float2*>(A.scalars)[9] = df_of(-alpha * A.scalars[6]);  // for the pair update
     }
   }
 }
 
 template <int NN>
-int launch_nn(const StreamArgs& a, cudaStream_t s) {
+int launch_nn(StreamArgs a, cudaStream_t s) {
   const size_t smem = (size_t)kStages * kChunk * kTilePts * sizeof(float);
   cudaFuncSetAttribute(k_vstream<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const long long tiles = (a.npts + kTilePts - 1) / kTilePts;
-  k_vstream<NN><<<(unsigned)tiles, kTilePts, smem, s>>>(a);
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vstream<NN>, kTilePts, smem);
+  const long long slots = (long long)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  a.tiles_per_cta = (tiles + slots - 1) / slots;
+  const long long grid = (tiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
+  k_vstream<NN><<<(unsigned)grid, kTilePts, smem, s>>>(a);
   return BSL_OK;
 }
 

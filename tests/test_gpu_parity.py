@@ -78,7 +78,7 @@ def test_hv_mixed_engines_match_fp64(bsl, name):
     u = np.zeros(h.basis_size)
     h.hv(v, u)
     h.set_precision("mixed")
-    assert h.kinetic_engine() == "tensor"  # every fixture grid fits the tensor-core tiles
+    assert h.kinetic_engine() == "simt"  # the default engine
     out = {}
     for engine in ("simt", "tensor"):
         h.set_kinetic_engine(engine)
@@ -223,3 +223,31 @@ def test_ritz_vectors_match_oracle(bsl):
         assert np.linalg.norm(u[keep] - ev[n] * x[keep]) <= 1e-4
     h.close()
     m.close()
+
+
+def test_mixed_recurrence_tracks_fp64(bsl):
+    """Mixed path (FP32 blocks and kinetic, double-float Lanczos buffers): the
+    first 40 alpha/beta agree with the FP64 path to 1e-5 relative."""
+    h, d, man, _ = make(bsl, "cpu_workload")
+    a, b, _ = h.lanczos(40)
+    h.set_precision("mixed")
+    am, bm, _ = h.lanczos(40)
+    scale = np.max(np.abs(a))
+    assert np.max(np.abs(am - a)) <= 1e-5 * scale
+    assert np.max(np.abs(bm[1:] - b[1:])) <= 1e-5 * scale
+    h.close()
+
+
+def test_ritz_vectors_mixed_match_fp64(bsl):
+    """Loop 2 on the double-float buffers gives the FP64 Ritz vectors to 1e-4."""
+    h, d, man, extra = make(bsl, "seed1_n6_l3_odd")
+    niter = 120
+    a, b, b2 = h.lanczos(niter)
+    ev, _ = bsl.good_eigenvalues(a, b, b2)
+    rows = bsl.tm_eigenvectors(a, b, b2, ev[:2])
+    R64 = h.ritz(niter, rows)
+    h.set_precision("mixed")
+    Rm = h.ritz(niter, rows)
+    for n in range(2):
+        assert np.max(np.abs(Rm[n] - R64[n])) <= 1e-4 * np.max(np.abs(R64[n]))
+    h.close()
