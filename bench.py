@@ -178,10 +178,10 @@ def levels_of(bsl, a, b, b2, count):
     return ev
 
 
-def stable_levels(bsl, a, b, b2, drop=200, tol=1e-9):
-    ev, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3)
+def stable_levels(bsl, a, b, b2, drop=200, tol=1e-9, unit=None):
+    ev, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3, unit_roundoff=unit)
     n = len(a) - drop
-    ev2, _ = bsl.good_eigenvalues(a[:n], b[:n + 1], b2[:n + 1], -1.0e3, 1.0e3)
+    ev2, _ = bsl.good_eigenvalues(a[:n], b[:n + 1], b2[:n + 1], -1.0e3, 1.0e3, unit_roundoff=unit)
     return np.array([e for e in ev if len(ev2) and np.min(np.abs(ev2 - e)) <= tol])
 
 
@@ -318,9 +318,13 @@ def main():
         if args.dump_lanczos:
             np.savez(args.dump_lanczos, a64=a64, b64=b64, b264=b264, am=am, bm=bm, bm2=bm2)
         ref_levels = np.sort(stable_levels(bsl, a64, b64, b264))[:cfg["levels"]]
-        evm, _ = bsl.good_eigenvalues(am, bm, bm2, -1.0e3, 1.0e3)
-        stable_m = stable_levels(bsl, am, bm, bm2)
+        # the mixed levels through the tail with the mixed path's unit roundoff
+        # (bsl_good_eigenvalues_unit); the reference tail's FP64 tolerance is reported beside
+        evm, _ = bsl.good_eigenvalues(am, bm, bm2, -1.0e3, 1.0e3, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF)
+        evr, _ = bsl.good_eigenvalues(am, bm, bm2, -1.0e3, 1.0e3)
+        stable_m = stable_levels(bsl, am, bm, bm2, unit=bsl.MIXED_UNIT_ROUNDOFF)
         dev = np.array([np.min(np.abs(evm - e)) for e in ref_levels]) * KJ_TO_CM if len(evm) else np.array([])
+        dev_r = np.array([np.min(np.abs(evr - e)) for e in ref_levels]) * KJ_TO_CM if len(evr) else np.array([])
         dev_s = (np.array([np.min(np.abs(stable_m - e)) for e in ref_levels]) * KJ_TO_CM
                  if len(stable_m) else np.array([]))
         worst = int(np.argmax(dev)) if len(dev) else -1
@@ -331,6 +335,8 @@ def main():
                "median_abs_dE_cm-1": float(np.median(dev)) if len(dev) else None,
                "worst_level_kJ_mol": float(ref_levels[worst]) if worst >= 0 else None,
                "dE_cm-1_per_level": [float("%.3g" % x) for x in dev],
+               "tail_unit_roundoff_mixed": bsl.MIXED_UNIT_ROUNDOFF,
+               "levels_within_1e-3_cm-1_fp64_tail_tolerance": int(np.sum(dev_r <= 1e-3)),
                "max_abs_dE_vs_mixed_stable_cm-1": float(dev_s.max()) if len(dev_s) else None,
                "min_level_gap_cm-1": float(np.min(np.diff(ref_levels)) * KJ_TO_CM) if len(ref_levels) > 1 else None,
                "lowest_levels_kJ_mol": [float(x) for x in ref_levels[:5]], "start": "normal seed 0"}

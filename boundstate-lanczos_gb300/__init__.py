@@ -24,6 +24,7 @@ POT_ALAVI_SPCE, POT_ISOHARMOSC = 0, 1
 PREC = {"fp64": 0, "mixed": 1}
 START = {"uniform": 0, "normal": 1}
 KINETIC = {"simt": 0, "tensor": 1}
+MIXED_UNIT_ROUNDOFF = 4.0e-15  # BSL_MIXED_UNIT_ROUNDOFF
 CALCULATORS = {
     "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE": POT_ALAVI_SPCE,
     "linRotCartSph_NoQuad_IsoHarmOsc": POT_ISOHARMOSC,
@@ -81,6 +82,8 @@ def lib():
     L.bsl_lanczos_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong, _P, _P, _P]
     L.bsl_lanczos_step_host.argtypes = [C.c_void_p, _P, _P, _P, _P, _P]
     L.bsl_good_eigenvalues.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_int)]
+    L.bsl_good_eigenvalues_unit.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, _P, _P,
+                                            C.POINTER(C.c_int)]
     L.bsl_tm_eigenvectors.argtypes = [C.c_int, _P, _P, _P, _P, C.c_int, _P]
     L.bsl_ritz_vectors.argtypes = [C.c_void_p, C.c_int, _P, C.c_int, _P]
     L.bsl_last_run_ms_per_iter.argtypes = [C.c_void_p, _P]
@@ -109,15 +112,22 @@ def parse_hv_input(path):
     return p
 
 
-def good_eigenvalues(alpha, beta, beta2, emin=-10.0, emax=10.0):
-    """Cullum-Willoughby good eigenvalues in (emin, emax] and error estimates."""
+def good_eigenvalues(alpha, beta, beta2, emin=-10.0, emax=10.0, unit_roundoff=None):
+    """Cullum-Willoughby good eigenvalues in (emin, emax] and error estimates.
+
+    unit_roundoff: None for the reference's FP64 tolerances, else the unit
+    roundoff the multiplicity tolerances are built on (bsl_good_eigenvalues_unit)."""
     alpha, beta, beta2 = (np.ascontiguousarray(x, dtype=np.float64) for x in (alpha, beta, beta2))
     niter = len(alpha)
     ev = np.zeros(niter)
     er = np.zeros(niter)
     ng = C.c_int(0)
-    _check(lib().bsl_good_eigenvalues(niter, _ptr(alpha), _ptr(beta), _ptr(beta2), emin, emax, _ptr(ev), _ptr(er),
-                                      C.byref(ng)))
+    if unit_roundoff is None:
+        _check(lib().bsl_good_eigenvalues(niter, _ptr(alpha), _ptr(beta), _ptr(beta2), emin, emax, _ptr(ev),
+                                          _ptr(er), C.byref(ng)))
+    else:
+        _check(lib().bsl_good_eigenvalues_unit(niter, _ptr(alpha), _ptr(beta), _ptr(beta2), emin, emax,
+                                               unit_roundoff, _ptr(ev), _ptr(er), C.byref(ng)))
     return ev[:ng.value].copy(), er[:ng.value].copy()
 
 

@@ -267,6 +267,7 @@ void free_device(DeviceState& d) {
                   d.scalars, d.status, d.hist, d.ref_vec, d.ref_out, d.full_of, d.ritz};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (d.vpair) cudaFree(d.vpair);
   if (d.kxy_slices) cudaFree(d.kxy_slices);
   if (d.kz_slices) cudaFree(d.kz_slices);
   if (d.ev0) cudaEventDestroy(d.ev0);
@@ -441,6 +442,7 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
     if ((rc = upload(&d.kxy_slices, sl, "Tx"))) return bail(rc);
     kinetic_f16_slices(t.tz, t.nz, &sl, &d.e_tz);
     if ((rc = upload(&d.kz_slices, sl, "Tz"))) return bail(rc);
+    h->kinetic_engine = BSL_KIN_TENSOR;
   }
   if ((rc = upload(&d.rot, t.rot, "rotor"))) return bail(rc);
   {
@@ -511,6 +513,7 @@ int bsl_set_kinetic_engine(bsl_handle* h, int engine) {
   if (engine != BSL_KIN_SIMT && engine != BSL_KIN_TENSOR) return fail(BSL_ERR_INPUT, "unknown kinetic engine");
   if (engine == BSL_KIN_TENSOR && !h->d.kxy_slices)
     return fail(BSL_ERR_UNSUPPORTED, "tensor-core kinetic needs at most 64 points per axis and equal x and y axes");
+  if (engine != h->kinetic_engine) h->state_pairs = -1;  // the FP32 copy of v is kept for the CUDA-core engine only
   h->kinetic_engine = engine;
   return BSL_OK;
 }
@@ -601,6 +604,13 @@ int bsl_good_eigenvalues(int niter, const double* alpha, const double* beta, con
                          double emax, double* eval, double* err, int* ngood) {
   if (niter < 1 || !alpha || !beta || !beta2 || !eval || !err || !ngood) return fail(BSL_ERR_INPUT, "bad arguments");
   return cw_good_eigenvalues(niter, alpha, beta, beta2, emin, emax, eval, err, ngood);
+}
+
+int bsl_good_eigenvalues_unit(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
+                              double emax, double unit_roundoff, double* eval, double* err, int* ngood) {
+  if (niter < 1 || !alpha || !beta || !beta2 || !eval || !err || !ngood || !(unit_roundoff > 0.0))
+    return fail(BSL_ERR_INPUT, "bad arguments");
+  return cw_good_eigenvalues(niter, alpha, beta, beta2, emin, emax, eval, err, ngood, unit_roundoff);
 }
 
 int bsl_tm_eigenvectors(int niter, const double* alpha, const double* beta, const double* beta2,

@@ -69,7 +69,7 @@ struct DeviceState {
   // FP32 heads fl32(T) and tails fl32(T - head), both stored transposed, for the mixed kernels
   float *kx_head = nullptr, *ky_head = nullptr, *kz_head = nullptr;
   float *kx_band = nullptr, *ky_band = nullptr, *kz_band = nullptr;
-  // fixed-point FP16 slices of T (4 zero-padded 64 x 64 tiles) and their scale
+  // fixed-point FP16 slices of T (5 zero-padded 64 x 64 tiles) and their scale
   // exponents, for the tensor-core kinetic
   uint16_t *kxy_slices = nullptr, *kz_slices = nullptr;
   int e_txy = 0, e_tz = 0;
@@ -83,6 +83,7 @@ struct DeviceState {
   // Lanczos work vectors (packed layout) and reduction scratch
   double *vec = nullptr, *rvec = nullptr, *ukin = nullptr;  // ukin: FP64, or (hi, lo) FP32 pairs (mixed)
   float* v32 = nullptr;                       // FP32 copy of the current Lanczos v (mixed)
+  float2* vpair = nullptr;                    // double-float copy of an FP64 input v (tensor-core kinetic)
   float *rot_hi = nullptr, *rot_lo = nullptr; // rotor energies as FP32 head + tail
   double* partials = nullptr;  // one double per reduction block
   unsigned int* counter = nullptr;
@@ -142,12 +143,13 @@ void kinetic_split_tables(const std::vector<double>& T, int n, bool transpose, s
 int launch_kin_xy_mixed(bsl_handle* h, const float* v, cudaStream_t s);
 int launch_kin_z_mixed(bsl_handle* h, const float* v, cudaStream_t s);
 
-// tensor-core kinetic (bsl_kinetic_tc.cu): the same contract as the mixed
-// kernels, for grids of at most 64 points per axis with Tx = Ty
+// tensor-core kinetic (bsl_kinetic_tc.cu): the same output as the mixed
+// kernels, from the double-float Lanczos vector, for grids of at most 64 points
+// per axis with Tx = Ty
 void kinetic_f16_slices(const std::vector<double>& T, int n, std::vector<uint16_t>* slices, int* e_t);
 bool kinetic_tc_supported(const Tables& t);
-int launch_kin_xy_tc(bsl_handle* h, const float* v, cudaStream_t s);
-int launch_kin_z_tc(bsl_handle* h, const float* v, cudaStream_t s);
+int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s);
+int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s);
 
 // potential-block apply (bsl_vapply_f32.cu / bsl_vapply_f64.cu)
 // FP32 blocks in the tile-major layout of bsl_vstream.cu (vstream_tile_points() points per tile)
@@ -173,8 +175,9 @@ int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const do
                       double* scalars, double* hist, int j, long long dpk);
 
 // ---- Cullum-Willoughby tail (bsl_tail.cpp) --------------------------------
+// unit <= 0: the reference's 2^-52
 int cw_good_eigenvalues(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
-                        double emax, double* eval, double* err, int* ngood);
+                        double emax, double* eval, double* err, int* ngood, double unit = 0.0);
 int cw_tm_eigenvectors(int niter, const double* alpha, const double* beta, const double* beta2,
                        const double* eval, int ngood, double* evtr);
 

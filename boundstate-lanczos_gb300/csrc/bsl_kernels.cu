@@ -363,7 +363,7 @@ __global__ void k_update_fold(const double* __restrict__ V, double* __restrict__
 // over many iterations: the FP32 exponent range of the pairs (and of the FP32
 // copy the kinetic reads) is never approached.  The logical r keeps its value
 // through sr / g.
-__global__ void __launch_bounds__(256, 4) k_update_pair(const float2* __restrict__ V, float2* __restrict__ R,
+__global__ void __launch_bounds__(256, 3) k_update_pair(const float2* __restrict__ V, float2* __restrict__ R,
                                                         long long L, float* __restrict__ v32_next, long long D,
                                                         double* partials, unsigned int* counter, double* scalars,
                                                         double* hist, int hist_stride, int j, int* status) {
@@ -398,10 +398,12 @@ __global__ void __launch_bounds__(256, 4) k_update_pair(const float2* __restrict
         acc = df_fma(r0, r0, acc);
         acc = df_fma(r1, r1, acc);
         const long long e0 = 2 * q;
-        if (e0 + 1 < D)
-          reinterpret_cast<float2*>(v32_next)[q] = make_float2(r0.x, r1.x);
-        else if (e0 < D)
-          v32_next[e0] = r0.x;
+        if (v32_next) {  // only the CUDA-core kinetic reads the FP32 copy
+          if (e0 + 1 < D)
+            reinterpret_cast<float2*>(v32_next)[q] = make_float2(r0.x, r1.x);
+          else if (e0 < D)
+            v32_next[e0] = r0.x;
+        }
       }
     }
   }
@@ -410,7 +412,7 @@ __global__ void __launch_bounds__(256, 4) k_update_pair(const float2* __restrict
     const float2 r = df_scale2(df_fma(na, V[i], R[i]), g);
     R[i] = r;
     acc = df_fma(r, r, acc);
-    if (i < D) v32_next[i] = r.x;
+    if (v32_next && i < D) v32_next[i] = r.x;
   }
   double total;
   if (reduce_grid_df(acc, partials, counter, &total) && threadIdx.x == 0) {
@@ -437,6 +439,12 @@ __global__ void __launch_bounds__(256, 4) k_update_pair(const float2* __restrict
       status[0] = 1;
     }
   }
+}
+
+// double-float pairs of an FP64 vector
+__global__ void k_pair_copy(const double* __restrict__ x, float2* __restrict__ y, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = df_of(x[i]);
 }
 
 // FP64 vector to double-float pairs in place (same 8 bytes per element)
@@ -519,15 +527,16 @@ int launch_vapply(bsl_handle* h, const double* v, double* out, int mode, int j, 
                            d.hist, j, dpk);
 }
 
-// mixed-precision kinetic stages on the FP32 copy of v, by the selected engine
-int launch_kin_xy(bsl_handle* h, cudaStream_t s) {
-  return h->kinetic_engine == BSL_KIN_TENSOR ? launch_kin_xy_tc(h, h->d.v32, s) : launch_kin_xy_mixed(h, h->d.v32, s);
+// mixed-precision kinetic stages by the selected engine: the tensor-core engine
+// reads v as double-float pairs, the CUDA-core engine its FP32 copy
+int launch_kin_xy(bsl_handle* h, const float2* vpair, cudaStream_t s) {
+  return h->kinetic_engine == BSL_KIN_TENSOR ? launch_kin_xy_tc(h, vpair, s) : launch_kin_xy_mixed(h, h->d.v32, s);
 }
-int launch_kin_z(bsl_handle* h, cudaStream_t s) {
-  return h->kinetic_engine == BSL_KIN_TENSOR ? launch_kin_z_tc(h, h->d.v32, s) : launch_kin_z_mixed(h, h->d.v32, s);
+int launch_kin_z(bsl_handle* h, const float2* vpair, cudaStream_t s) {
+  return h->kinetic_engine == BSL_KIN_TENSOR ? launch_kin_z_tc(h, vpair, s) : launch_kin_z_mixed(h, h->d.v32, s);
 }
 
-int launch_kinetic(bsl_handle* h, const double* v, cudaStream_t s) {
+int launch_kinetic(bsl_handle* h, const double* v, const float2* vpair, cudaStream_t s) {
   DeviceState& d = h->d;
   const Tables& t = h->t;
   const bool mixed = h->precision == BSL_PREC_MIXED;
@@ -536,8 +545,8 @@ int launch_kinetic(bsl_handle* h, const double* v, cudaStream_t s) {
   if (sm_xy > 200 * 1024 || sm_z > 200 * 1024) return fail(BSL_ERR_UNSUPPORTED, "grid plane too large for one CTA");
   const dim3 gxy(t.nz, t.nn), gz(t.ny, t.nn);
   if (mixed) {
-    int rc = launch_kin_xy(h, s);
-    if (!rc) rc = launch_kin_z(h, s);
+    int rc = launch_kin_xy(h, vpair, s);
+    if (!rc) rc = launch_kin_z(h, vpair, s);
     return rc;
   } else {
     cudaFuncSetAttribute(k_kin_xy_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_xy);
@@ -687,11 +696,17 @@ int dev_vblocks(bsl_handle* h) {
 }
 
 int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s) {
+  DeviceState& d = h->d;
+  const long long D = bsl_packed_size(h);
   if (h->precision == BSL_PREC_MIXED) {
-    k_to_f32<<<1024, kThreads, 0, s>>>(v, h->d.v32, bsl_packed_size(h));
+    k_to_f32<<<1024, kThreads, 0, s>>>(v, d.v32, D);
+    if (h->kinetic_engine == BSL_KIN_TENSOR) {
+      if (!d.vpair) BSL_CUDA(cudaMalloc(&d.vpair, (size_t)D * sizeof(float2)));
+      k_pair_copy<<<1024, kThreads, 0, s>>>(v, d.vpair, D);
+    }
     BSL_CUDA(cudaGetLastError());
   }
-  int rc = launch_kinetic(h, v, s);
+  int rc = launch_kinetic(h, v, d.vpair, s);
   if (rc) return rc;
   return launch_vapply(h, v, u, 0, 0, s);
 }
@@ -700,9 +715,10 @@ int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s) {
 int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaStream_t s) {
   DeviceState& d = h->d;
   if (h->state_pairs == 1)
-    k_update_pair<<<d.red_blocks, kThreads, 0, s>>>(reinterpret_cast<const float2*>(V), reinterpret_cast<float2*>(R),
-                                                    L, d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
-                                                    d.hist_cap, j, d.status);
+    k_update_pair<<<d.red_blocks, kThreads, 0, s>>>(
+        reinterpret_cast<const float2*>(V), reinterpret_cast<float2*>(R), L,
+        h->kinetic_engine == BSL_KIN_TENSOR ? nullptr : d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
+        d.hist_cap, j, d.status);
   else
     k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
                                                     d.hist_cap, j, d.status);
@@ -715,7 +731,7 @@ int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s) {
   const long long L = bsl_packed_size(h) + 1;  // + the coordinate outside the symmetry block
   double* V = h->lanczos_flip ? d.rvec : d.vec;
   double* R = h->lanczos_flip ? d.vec : d.rvec;
-  int rc = launch_kinetic(h, V, s);
+  int rc = launch_kinetic(h, V, reinterpret_cast<const float2*>(V), s);
   if (rc) return rc;
   if ((rc = launch_vapply(h, V, R, h->state_pairs == 1 ? 2 : 1, j, s))) return rc;
   if ((rc = launch_update(h, V, R, L, j, s))) return rc;
@@ -740,13 +756,13 @@ int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_
   int rc;
   cudaEventRecord(ev[0], s);
   if (mixed) {
-    if ((rc = launch_kin_xy(h, s))) return rc;
+    if ((rc = launch_kin_xy(h, reinterpret_cast<const float2*>(V), s))) return rc;
   } else {
     k_kin_xy_f64<<<gxy, kThreads, sm_xy, s>>>(V, d.ukin, d.tx, d.ty, t.nx, t.ny, t.nz);
   }
   cudaEventRecord(ev[1], s);
   if (mixed) {
-    if ((rc = launch_kin_z(h, s))) return rc;
+    if ((rc = launch_kin_z(h, reinterpret_cast<const float2*>(V), s))) return rc;
   } else {
     k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(V, d.ukin, d.tz, t.nx, t.ny, t.nz);
   }

@@ -5,26 +5,37 @@
 // Reference: Tv_5D_oneCompositeIndex / Mv_5D_oneCompositeIndex,
 // Hv-calculators/linRotor/cartSphBasis/HvCalc/linRotCartSphHvRoutines.cpp:1807-1969.
 //
-// Each CTA takes two grid planes at a time (padded to 64 x 64) and forms
-// D[(plane, row)][col] = sum_q A[(plane, row)][q] T[col][q] as M = 128, N = 64,
-// K = 64 products:
-//   x (plane (y, x) of fixed (s, z)):  A[(p, y)][q] = v(p, y, q),  out(y, x) += sum_q v(y, q) Tx[x][q]
-//   y (same plane, transposed):        A[(p, x)][q] = v(p, q, x),  out(y, x) += sum_q Ty[y][q] v(q, x)
-//   z (plane (z, x) of fixed (s, y)):  A[(p, x)][q] = v(p, q, x),  out(z, x) += sum_q Tz[z][q] v(q, x)
+// Products (M = 128 rows, N = 64 output columns, K = 64):
+//   x and y, one (y, x) plane of fixed (s, z) per batch: rows 0-63 are the rows of
+//   the plane (D[y][x] = sum_q v(y, q) Tx[x][q]) and rows 64-127 its columns
+//   (D[64 + x][y] = sum_q v(q, x) Ty[y][q]), so both directions of one plane
+//   come out of one set of accumulators (the y part is transposed through
+//   shared memory before the coalesced store);
+//   z, two (z, x) planes of fixed (s, y) per batch: rows (p, x) are the columns
+//   of the planes (D[(p, x)][z] = sum_q v(p, q, x) Tz[z][q]).
 //
 // Exactness (error-free slicing after Ozaki, Ogita, Oishi and Rump,
-// Numer. Algorithms 59, 2012, here with 8-bit fixed-point slices): each row of
-// A is scaled by a power of two to below 1 in magnitude and cut into four
-// 8-bit signed integer slices, A = 2^(e_row - 7) (a1 + 2^-8 a2 + 2^-16 a3 +
-// 2^-24 a4) (32 bits relative to the row maximum: every FP32 value within 2^8
-// of the row maximum is exact); T is scaled from its largest element and cut
-// into four slices likewise.  The slices are small integers, exact in FP16,
-// their products are exact, and every partial sum of one product class is an
-// integer below 4 * 2^20: the FP32 accumulation in tensor memory is exact
-// whatever its internal rounding, so the result carries no accumulation bias.
-// The products of each scale class k + l share one accumulator (classes 0..3;
-// the rest lies below 2^-32 of the row scale) and the four classes are combined
-// on the CUDA cores into a double-float pair.
+// Numer. Algorithms 59, 2012, here with 9-bit fixed-point slices): each operand
+// row (a row or a column of a plane of the double-float Lanczos vector) is
+// scaled by a power of two to below 1 in magnitude and cut into four 9-bit
+// signed integer slices, v = 2^(e_row - 8) (a1 + 2^-9 a2 + 2^-18 a3 + 2^-27 a4)
+// (36 bits relative to the row maximum; one scale per plane instead raises the
+// noise of H v where a plane's rows differ in size); T is scaled from its
+// largest element and cut into four slices the same way, rounded to nearest so
+// that the symmetric T stays exactly symmetric (a Lanczos recurrence on a
+// non-symmetric H scatters the converged copies of a level).  The slices are
+// integers in [-256, 256], exact in FP16, their products are exact, and every
+// partial sum of one product class (at most 4 products of 64 terms) is an
+// integer of magnitude at most 2^24: the FP32 accumulation in tensor memory is
+// exact whatever its internal rounding, so the result carries no accumulation
+// bias.  The products of each scale class k + l <= 3 share one accumulator and
+// the four classes are combined on the CUDA cores into a double-float pair.
+// The rounding of T is the same along each Toeplitz diagonal and adds up
+// coherently for smooth states: with 36 bits it shifts levels by ~1e-7 kJ/mol
+// per axis.
+
+// Pipeline: persistent CTAs, two per SM with 256 tensor-memory columns each, so
+// that one CTA slices or finishes its epilogue while the other's products run.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -37,20 +48,22 @@
 namespace bsl {
 namespace {
 
-constexpr int kVS = 4;                  // slices of v
-constexpr int kTS = 4;                  // slices of T
-constexpr uint32_t kTileA = 128 * 128;  // 16 KiB: 128 rows x 64 FP16 (one 128-byte swizzle atom per row)
-constexpr uint32_t kTileB = 64 * 128;   // 8 KiB
-constexpr int kRaw = 65;                // padded row of the raw plane buffer
-constexpr int kStage = 65;              // padded row of the x-result staging buffer
-constexpr int kPairs = 10;              // slice products (k, l) with k + l <= 3 (0-based), by class
+constexpr int kVS = 4;                       // slices of v
+constexpr int kTS = 4;                       // slices of T
+constexpr uint32_t kTileA = 128 * 128;       // 16 KiB: 128 rows x 64 FP16 (one 128-byte swizzle atom per row)
+constexpr uint32_t kTileB = 64 * 128;        // 8 KiB
+constexpr uint32_t kBatchA = kVS * kTileA;   // operand slices of one batch
+constexpr uint32_t kCols = 4 * 64;           // accumulator columns of one batch (classes 0..3)
+constexpr int kTcThreads = 256;       // threads per CTA
+constexpr int kPairs = 10;                   // slice products (k, l) with k + l <= 3, by class
 __constant__ int8_t c_pk[kPairs] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
 __constant__ int8_t c_pl[kPairs] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+__constant__ int8_t c_first[kPairs] = {1, 1, 0, 1, 0, 0, 1, 0, 0, 0};
 
 struct KinTC {
   const uint16_t* tslices;  // [kTS][64][64] FP16 bits, row = output index, column = q, zero padded
-  int e_t;                  // T = 2^(e_t - 7) (b1 + 2^-8 b2 + 2^-16 b3 + 2^-24 b4)
-  const float* v32;
+  int e_t;                  // T = 2^(e_t - 8) (b1 + 2^-9 b2 + 2^-18 b3 + 2^-27 b4)
+  const float2* v;          // the Lanczos v as double-float pairs
   float2* out;
   int nx, ny, nz, nplanes;
   int* status;
@@ -60,55 +73,46 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~(uintptr_t)1023);
 }
 
-// byte offset of the 16-byte chunk c (8 FP16 values) of row r in an SW128 K-major tile with K = 64
-__device__ __forceinline__ uint32_t chunk_offset(int r, int c) { return (uint32_t)(r * 128 + ((c ^ (r & 7)) << 4)); }
+// byte offset of element k (a multiple of 4) of row r in an SW128 K-major tile with K = 64 FP16
+__device__ __forceinline__ uint32_t quad_offset(int r, int k) {
+  return (uint32_t)(r * 128 + (((k >> 3) ^ (r & 7)) << 4) + ((k & 7) << 1));
+}
 
 __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
   const __half2 h = __floats2half2_rn(a, b);
   return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// exponent e with max|x| 2^-e in [0.5, 1); 0 for an all-zero row
-__device__ __forceinline__ int row_exponent(float maxabs) {
+// exponent e with max|x| 2^-e in [0.5, 1]; 0 for an all-zero plane
+__device__ __forceinline__ int plane_exponent(float maxabs) {
   if (!(maxabs > 0.f)) return 0;
   return max(-100, ilogbf(maxabs) + 1);
 }
 
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((min(max(e, -126), 127) + 127) << 23); }
 
-// Slices of 8 consecutive values already multiplied by 2^(7 - e), written as
-// one 16-byte chunk per slice.  Every step is exact except the last rounding.
-__device__ __forceinline__ void write_slices(uint8_t* A, int row, int chunk, const float (&y)[8]) {
-  float s[kVS][8];
-#pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    float r = y[u];
-    const float a1 = rintf(r);
-    r = __fmul_rn(__fsub_rn(r, a1), 256.f);
-    const float a2 = rintf(r);
-    r = __fmul_rn(__fsub_rn(r, a2), 256.f);
-    const float a3 = rintf(r);
-    r = __fmul_rn(__fsub_rn(r, a3), 256.f);
-    s[0][u] = a1;
-    s[1][u] = a2;
-    s[2][u] = a3;
-    s[3][u] = rintf(r);
-  }
-  const uint32_t off = chunk_offset(row, chunk);
-#pragma unroll
-  for (int k = 0; k < kVS; ++k)
-    *reinterpret_cast<uint4*>(A + k * kTileA + off) = make_uint4(pack_h2(s[k][0], s[k][1]), pack_h2(s[k][2], s[k][3]),
-                                                                 pack_h2(s[k][4], s[k][5]), pack_h2(s[k][6], s[k][7]));
+// Four 9-bit slices of a double-float value already scaled to |y| < 256 (hi and
+// lo multiplied by the same power of two): y = a1 + 2^-9 a2 + 2^-18 a3 +
+// 2^-27 a4 + O(2^-28), each a an integer in [-256, 256].  Every step is exact
+// except the last rounding.
+__device__ __forceinline__ void slice4(float yh, float yl, float (&a)[kVS]) {
+  a[0] = rintf(yh);
+  float r = __fmul_rn(__fadd_rn(__fsub_rn(yh, a[0]), yl), 512.f);
+  a[1] = rintf(r);
+  r = __fmul_rn(__fsub_rn(r, a[1]), 512.f);
+  a[2] = rintf(r);
+  r = __fmul_rn(__fsub_rn(r, a[2]), 512.f);
+  a[3] = rintf(r);
 }
 
-// D_c += A_k B_l^T for the ten slice products, class c = k + l in accumulator columns [64 c, 64 c + 64)
+// D_c += A_k B_l^T for the slice products, class c in accumulator columns [64 c, 64 c + 64)
 __device__ __forceinline__ void issue_products(uint32_t d, uint32_t a, uint32_t b) {
   const uint32_t idesc = tc::idesc_f16(128, 64);
 #pragma unroll 1
   for (int pr = 0; pr < kPairs; ++pr) {
     const int k = c_pk[pr], l = c_pl[pr];
     const uint32_t dc = d + (uint32_t)(k + l) * 64u;
-    const bool first = (pr == 0 || pr == 1 || pr == 3 || pr == 6);  // first product of its class
+    const bool first = c_first[pr] != 0;
 #pragma unroll
     for (int s = 0; s < 4; ++s)
       tc::mma_f16(dc, tc::sw128_desc(a + (uint32_t)k * kTileA + (uint32_t)s * 32u),
@@ -120,205 +124,255 @@ __device__ __forceinline__ void issue_products(uint32_t d, uint32_t a, uint32_t 
 // double-float pairs and multiplied by `scale` (a power of two)
 __device__ __forceinline__ void load_pairs(uint32_t taddr, float scale, float2 (&out)[16]) {
   float c0[16], c1[16], c2[16], c3[16];
-  tc::tmem_ld16(taddr, c0);
-  tc::tmem_ld16(taddr + 64u, c1);
-  tc::tmem_ld16(taddr + 128u, c2);
-  tc::tmem_ld16(taddr + 192u, c3);
+  tc::tmem_ld16_nowait(taddr, c0);
+  tc::tmem_ld16_nowait(taddr + 64u, c1);
+  tc::tmem_ld16_nowait(taddr + 128u, c2);
+  tc::tmem_ld16_nowait(taddr + 192u, c3);
+  tc::tmem_wait_ld();
 #pragma unroll
   for (int u = 0; u < 16; ++u) {
     float h, e1, e2, l;
-    two_sum(c0[u], __fmul_rn(c1[u], 0x1p-8f), h, e1);
-    two_sum(h, __fmul_rn(c2[u], 0x1p-16f), h, e2);
-    l = __fadd_rn(__fadd_rn(e1, e2), __fmul_rn(c3[u], 0x1p-24f));
+    two_sum(c0[u], __fmul_rn(c1[u], 0x1p-9f), h, e1);
+    two_sum(h, __fmul_rn(c2[u], 0x1p-18f), h, e2);
+    l = __fadd_rn(__fadd_rn(e1, e2), __fmul_rn(c3[u], 0x1p-27f));
     fast_two_sum(h, l, h, l);
     out[u] = make_float2(__fmul_rn(h, scale), __fmul_rn(l, scale));
   }
 }
 
-__device__ __forceinline__ void load_b(uint8_t* B, const uint16_t* src, int tid, int nthreads) {
-  for (int e = tid; e < kTS * 64 * 8; e += nthreads) {  // kTS tiles of 64 rows x 8 chunks
-    const int l = e >> 9, r = (e >> 3) & 63, c = e & 7;
-    *reinterpret_cast<uint4*>(B + l * kTileB + chunk_offset(r, c)) =
-        *reinterpret_cast<const uint4*>(src + ((size_t)l * 64 + r) * 64 + c * 8);
+__device__ __forceinline__ void load_b(uint8_t* B, const uint16_t* src) {
+  for (int e = threadIdx.x; e < kTS * 64 * 16; e += kTcThreads) {  // kTS tiles of 64 rows x 16 quads
+    const int l = e >> 10, r = (e >> 4) & 63, q = (e & 15) * 4;
+    *reinterpret_cast<uint2*>(B + l * kTileB + quad_offset(r, q)) =
+        *reinterpret_cast<const uint2*>(src + ((size_t)l * 64 + r) * 64 + q);
   }
 }
 
-// x and y contractions; out(y, x) = (Tx v + Ty v) as double-float pairs.  256 threads:
-// threads 0-127 slice the rows (x operand), 128-255 the columns (y operand); in the
-// epilogues warps w and w + 4 share the tensor-memory lanes 32 (w % 4) and split the columns.
-__global__ void __launch_bounds__(256, 1) k_kin_xy_tc(KinTC a) {
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+
+
+// Row maxima of a 64 x 64 plane held as 4 x 4 blocks (thread (bj, bi) = tid / 16,
+// tid % 16): the 16 threads of one block row are 16 consecutive lanes.
+__device__ __forceinline__ void block_row_max(const float2 (&x)[4][4], float (&rm)[4]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    float m = fmaxf(fmaxf(fabsf(x[r][0].x), fabsf(x[r][1].x)), fmaxf(fabsf(x[r][2].x), fabsf(x[r][3].x)));
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    rm[r] = m;
+  }
+}
+
+// Column maxima of the same blocks through shared memory (part: [16][64] floats).
+// Contains a __syncthreads.
+__device__ __forceinline__ void block_col_max(const float2 (&x)[4][4], float* part, int bj, int bi, float (&cm)[4]) {
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    part[bj * 64 + 4 * bi + c] =
+        fmaxf(fmaxf(fabsf(x[0][c].x), fabsf(x[1][c].x)), fmaxf(fabsf(x[2][c].x), fabsf(x[3][c].x)));
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float m = 0.f;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) m = fmaxf(m, part[q * 64 + 4 * bi + c]);
+    cm[c] = m;
+  }
+}
+
+// Slices of a 4 x 4 block, each row r scaled by sc[r] and written as row row0 + r
+// with K = k0.. (by_rows), or each column c scaled by sc[c] and written as row
+// row0 + c with K = k0.. (columns).
+template <bool by_rows>
+__device__ __forceinline__ void write_block(uint8_t* A, const float2 (&x)[4][4], const float (&sc)[4], int row0,
+                                            int k0) {
+#pragma unroll
+  for (int o = 0; o < 4; ++o) {  // output row
+    float s[4][kVS];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float2 v = by_rows ? x[o][u] : x[u][o];
+      slice4(__fmul_rn(v.x, sc[o]), __fmul_rn(v.y, sc[o]), s[u]);
+    }
+#pragma unroll
+    for (int k = 0; k < kVS; ++k)
+      *reinterpret_cast<uint2*>(A + k * kTileA + quad_offset(row0 + o, k0)) =
+          make_uint2(pack_h2(s[0][k], s[1][k]), pack_h2(s[2][k], s[3][k]));
+  }
+}
+
+// x and y contractions; out(y, x) = (Tx v + Ty v) as double-float pairs.  One
+// plane per batch: operand rows 0-63 are the plane's rows (each scaled by its own
+// maximum), rows 64-127 its columns (each scaled by its own maximum).  Two CTAs
+// per SM, 256 tensor-memory columns each.
+__global__ void __launch_bounds__(kTcThreads, 2) k_kin_xy_tc(KinTC a) {
   extern __shared__ uint8_t smraw[];
   uint8_t* sm = align1024(smraw);
-  uint8_t* Ax = sm;                                          // kVS tiles
-  uint8_t* Ay = sm + kVS * kTileA;                           // kVS tiles
-  uint8_t* B = sm + 2 * kVS * kTileA;                        // kTS tiles
-  float* raw = reinterpret_cast<float*>(B + kTS * kTileB);  // [2][64][kRaw]
-  float2* Xs = reinterpret_cast<float2*>(sm);               // [128][kStage] over the A tiles once consumed
+  uint8_t* A = sm;                                        // kVS tiles
+  uint8_t* B = sm + kBatchA;                              // kTS tiles
+  float* part = reinterpret_cast<float*>(B + kTS * kTileB);  // [16][64] column-maximum partials
+  float2* Xs = reinterpret_cast<float2*>(sm);             // [64][64] x part, column swizzled, over A
+  float2* Ys = Xs + 64 * 64;                              // [64][64] y part, over A
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_slot;
   __shared__ int failed;
-  __shared__ int ex[128], ey[128];
+  __shared__ int e_row[128];
   const int tid = threadIdx.x, warp = tid >> 5;
   const int nx = a.nx, ny = a.ny;
   const long long psz = (long long)ny * nx;
-  const int npairs = (a.nplanes + 1) / 2;
-  load_b(B, a.tslices, tid, 256);
+  load_b(B, a.tslices);
   if (tid == 0) {
     failed = 0;
     tc::mbar_init(&bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, 512);
-  // raw planes of one pair into shared memory (zero padded)
-  auto load_raw = [&](int pair) {
-#pragma unroll 1
-    for (int pl = 0; pl < 2; ++pl) {
-      const int plane = 2 * pair + pl;
-      const bool pv = plane < a.nplanes;
-      const float* src = a.v32 + (pv ? (long long)plane * psz : 0);
-#pragma unroll 4
-      for (int e = tid; e < 64 * 64; e += 256) {
-        const int j = e >> 6, i = e & 63;
-        raw[(pl * 64 + j) * kRaw + i] = (pv && j < ny && i < nx) ? __ldg(src + (long long)j * nx + i) : 0.f;
-      }
-    }
-  };
-  if ((int)blockIdx.x < npairs) load_raw(blockIdx.x);
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, kCols);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
-  const int lrow = (warp & 3) * 32 + (tid & 31);  // tensor-memory lane of this thread
+  const int lrow = (warp & 3) * 32 + (tid & 31);  // tensor-memory lane of this thread in the epilogue
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-  const int half = warp >> 2;                     // column half in the epilogues
+  const int half = warp >> 2;
+  const int bj = tid >> 4, bi = tid & 15;  // 4 x 4 block of the plane sliced by this thread
   uint32_t phase = 0;
-  for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x) {
-    // slices: rows (p, y) of the x operand, columns (p, x) of the y operand
-    {
-      const int r = tid & 127, pl = r >> 6, w = r & 63;
-      const bool by_row = tid < 128;
-      const float* base = raw + pl * 64 * kRaw;
-      const int stride_q = by_row ? 1 : kRaw, off = by_row ? w * kRaw : w;
-      float m = 0.f;
-      for (int q = 0; q < 64; ++q) m = fmaxf(m, fabsf(base[off + q * stride_q]));
-      const int e = row_exponent(m);
-      (by_row ? ex : ey)[r] = e;
-      const float sc = pow2f(7 - e);
-      uint8_t* A = by_row ? Ax : Ay;
-#pragma unroll 1
-      for (int c = 0; c < 8; ++c) {
-        float y[8];
+  for (int plane = blockIdx.x; plane < a.nplanes; plane += gridDim.x) {
+    const float2* src = a.v + (long long)plane * psz;
+    float2 x[4][4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) y[u] = __fmul_rn(base[off + (c * 8 + u) * stride_q], sc);
-        write_slices(A, r, c, y);
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int j = 4 * bj + r, i = 4 * bi + c;
+        x[r][c] = (j < ny && i < nx) ? __ldg(src + (long long)j * nx + i) : make_float2(0.f, 0.f);
       }
+    const int nxt = plane + (int)gridDim.x;  // the next plane into L2
+    if (nxt < a.nplanes)
+      for (long long o = (long long)tid * 4; o < psz; o += kTcThreads * 4)
+        prefetch_l2(a.v + (long long)nxt * psz + o);
+    float rm[4], cm[4], sr[4], scl[4];
+    block_row_max(x, rm);
+    block_col_max(x, part, bj, bi, cm);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int er = plane_exponent(rm[u]), ec = plane_exponent(cm[u]);
+      sr[u] = pow2f(8 - er);
+      scl[u] = pow2f(8 - ec);
+      if (bi == 0) e_row[4 * bj + u] = er;
+      if (bj == 0) e_row[64 + 4 * bi + u] = ec;
     }
+    write_block<true>(A, x, sr, 4 * bj, 4 * bi);
+    write_block<false>(A, x, scl, 64 + 4 * bi, 4 * bj);
     tc::fence_smem_to_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     if (tid == 0 && !failed) {
-      issue_products(tmem, tc::smem_u32(Ax), tc::smem_u32(B));
-      issue_products(tmem + 256u, tc::smem_u32(Ay), tc::smem_u32(B));
+      issue_products(tmem, tc::smem_u32(A), tc::smem_u32(B));
       tc::mma_commit(&bar);
     }
-    // the next pair's raw planes load while the products run (the raw buffer is free)
-    if (pair + (int)gridDim.x < npairs) load_raw(pair + gridDim.x);
     if (!failed && !tc::mbar_wait(&bar, phase)) failed = 1;
     phase ^= 1u;
     tc::fence_after_sync();
     __syncthreads();
     if (failed) break;
-    // x results (lane = (p, y), columns x) to shared memory as pairs
-    {
-      const float scale = pow2f(ex[lrow] + a.e_t - 14);
+    // epilogue: rows 0-63 (x part) and 64-127 (y part) to shared memory over A
+    const float scale = pow2f(e_row[lrow] + a.e_t - 16);
 #pragma unroll 1
-      for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 16) {
-        float2 v[16];
-        load_pairs(tmem + lane_base + (uint32_t)c0, scale, v);
+    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 16) {
+      float2 v[16];
+      load_pairs(tmem + lane_base + (uint32_t)c0, scale, v);
+      if (lrow < 64) {  // x part: row y = lrow, columns x
 #pragma unroll
-        for (int u = 0; u < 16; ++u) Xs[lrow * kStage + c0 + u] = v[u];
-      }
-    }
-    __syncthreads();
-    // y results (lane = (p, x), columns y) plus the staged x results; consecutive
-    // lanes write consecutive x of one row
-    {
-      const int pl = lrow >> 6, i = lrow & 63;
-      const int plane = 2 * pair + pl;
-      const bool colv = plane < a.nplanes && i < nx;
-      const long long base = colv ? (long long)plane * psz + i : 0;
-      const float scale = pow2f(ey[lrow] + a.e_t - 14);
-#pragma unroll 1
-      for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 16) {
-        float2 v[16];
-        load_pairs(tmem + 256u + lane_base + (uint32_t)c0, scale, v);
+        for (int u = 0; u < 16; ++u) Xs[lrow * 64 + ((c0 + u) ^ (lrow & 31))] = v[u];
+      } else {          // y part: x = lrow - 64, columns y
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int j = c0 + u;
-          if (colv && j < ny) a.out[base + (long long)j * nx] = df_add(Xs[(pl * 64 + j) * kStage + i], v[u]);
-        }
+        for (int u = 0; u < 16; ++u) Ys[(c0 + u) * 64 + (lrow - 64)] = v[u];
       }
     }
     tc::fence_before_sync();
     __syncthreads();
-    tc::fence_after_sync();
+    const int i = tid & 63;
+    float2* dst = a.out + (long long)plane * psz;
+    if (i < nx)
+      for (int j = tid >> 6; j < ny; j += kTcThreads / 64)
+        dst[(long long)j * nx + i] = df_add(Xs[j * 64 + (i ^ (j & 31))], Ys[j * 64 + i]);
+    __syncthreads();  // A (under Xs, Ys) is sliced again next
   }
   if (failed && tid == 0) a.status[3] = 1;
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+  if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
-// z contraction added into the pairs: out(z, x) += Tz v.  128 threads, one per
-// row (p, x) of the operand; each thread loads its column of the (z, x) plane.
-__global__ void __launch_bounds__(128) k_kin_z_tc(KinTC a) {
+// z contraction added into the pairs: out(z, x) += Tz v, two (z, x) planes of
+// fixed (s, y) per batch, operand rows (p, x) each scaled by its own maximum.
+// Two CTAs per SM, 256 tensor-memory columns each.
+__global__ void __launch_bounds__(kTcThreads, 2) k_kin_z_tc(KinTC a) {
   extern __shared__ uint8_t smraw[];
   uint8_t* sm = align1024(smraw);
-  uint8_t* A = sm;                 // kVS tiles
-  uint8_t* B = sm + kVS * kTileA;  // kTS tiles
+  uint8_t* A = sm;                                           // kVS tiles
+  uint8_t* B = sm + kBatchA;                                 // kTS tiles
+  float* part = reinterpret_cast<float*>(B + kTS * kTileB);  // [16][64] column-maximum partials
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_slot;
   __shared__ int failed;
+  __shared__ int e_row[128];
   const int tid = threadIdx.x, warp = tid >> 5;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const long long pstride = (long long)ny * nx;
-  load_b(B, a.tslices, tid, 128);
+  load_b(B, a.tslices);
   if (tid == 0) {
     failed = 0;
     tc::mbar_init(&bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, 256);
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, kCols);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  const int lrow = (warp & 3) * 32 + (tid & 31);
+  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+  const int half = warp >> 2;
+  const int bk = tid >> 4, bi = tid & 15;  // 4 x 4 block of each of the two planes
   const int npairs = (a.nplanes + 1) / 2;
-  const int pl = tid >> 6, i = tid & 63;
-  uint32_t phase = 0;
-  float col[64];
-  auto load_col = [&](int pair) {
-    const int plane = 2 * pair + pl;  // plane = s * ny + y
-    const bool cv = plane < a.nplanes && i < nx;
-    const float* src = a.v32 + (cv ? (long long)(plane / ny) * nz * pstride + (long long)(plane % ny) * nx + i : 0);
-#pragma unroll
-    for (int k = 0; k < 64; ++k) col[k] = (cv && k < nz) ? __ldg(src + k * pstride) : 0.f;
+  auto plane_base = [&](int plane) {  // plane = s * ny + y
+    return (long long)(plane / ny) * nz * pstride + (long long)(plane % ny) * nx;
   };
-  if ((int)blockIdx.x < npairs) load_col(blockIdx.x);
+  uint32_t phase = 0;
   for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x) {
-    float m = 0.f;
+#pragma unroll 1
+    for (int pl = 0; pl < 2; ++pl) {
+      const int plane = 2 * pair + pl;
+      const bool pv = plane < a.nplanes;
+      const float2* src = a.v + (pv ? plane_base(plane) : 0);
+      float2 x[4][4];
 #pragma unroll
-    for (int k = 0; k < 64; ++k) m = fmaxf(m, fabsf(col[k]));
-    const int e = row_exponent(m);
-    const float sc = pow2f(7 - e);
+      for (int r = 0; r < 4; ++r)
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      float y[8];
+        for (int c = 0; c < 4; ++c) {
+          const int k = 4 * bk + r, i = 4 * bi + c;
+          x[r][c] = (pv && k < nz && i < nx) ? __ldg(src + k * pstride + i) : make_float2(0.f, 0.f);
+        }
+      float cm[4], scl[4];
+      block_col_max(x, part, bk, bi, cm);
 #pragma unroll
-      for (int u = 0; u < 8; ++u) y[u] = __fmul_rn(col[c * 8 + u], sc);
-      write_slices(A, tid, c, y);
+      for (int u = 0; u < 4; ++u) {
+        const int ec = plane_exponent(cm[u]);
+        scl[u] = pow2f(8 - ec);
+        if (bk == 0) e_row[pl * 64 + 4 * bi + u] = ec;
+      }
+      write_block<false>(A, x, scl, pl * 64 + 4 * bi, 4 * bk);
+      __syncthreads();  // part[] is reused by the next plane
+    }
+    const int nxt = pair + (int)gridDim.x;  // the next pair's columns into L2
+    if (nxt < npairs) {
+      const int plane = 2 * nxt + (tid >> 7);
+      const int i = (tid & 127) * 4;
+      if (plane < a.nplanes && i < nx)
+        for (int k = 0; k < nz; ++k) prefetch_l2(a.v + plane_base(plane) + k * pstride + i);
     }
     tc::fence_smem_to_async();
     tc::fence_before_sync();
@@ -328,28 +382,26 @@ __global__ void __launch_bounds__(128) k_kin_z_tc(KinTC a) {
       issue_products(tmem, tc::smem_u32(A), tc::smem_u32(B));
       tc::mma_commit(&bar);
     }
-    const int plane = 2 * pair + pl;
-    const bool cv = plane < a.nplanes && i < nx;
-    const long long ob = cv ? (long long)(plane / ny) * nz * pstride + (long long)(plane % ny) * nx + i : 0;
-    if (pair + (int)gridDim.x < npairs) load_col(pair + gridDim.x);
     if (!failed && !tc::mbar_wait(&bar, phase)) failed = 1;
     phase ^= 1u;
     tc::fence_after_sync();
     __syncthreads();
     if (failed) break;
-    const float scale = pow2f(e + a.e_t - 14);
+    const int pl = lrow >> 6, i = lrow & 63;
+    const int plane = 2 * pair + pl;
+    const bool cv = plane < a.nplanes && i < nx;
+    const long long ob = cv ? plane_base(plane) + i : 0;
+    const float scale = pow2f(e_row[lrow] + a.e_t - 16);
 #pragma unroll 1
-    for (int c0 = 0; c0 < 64; c0 += 16) {
-      float2 v[16];
+    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 16) {
+      float2 v[16], u0[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        u0[u] = (cv && c0 + u < nz) ? a.out[ob + (c0 + u) * pstride] : make_float2(0.f, 0.f);
       load_pairs(tmem + lane_base + (uint32_t)c0, scale, v);
 #pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        const int k = c0 + u;
-        if (cv && k < nz) {
-          const long long o = ob + k * pstride;
-          a.out[o] = df_add(a.out[o], v[u]);
-        }
-      }
+      for (int u = 0; u < 16; ++u)
+        if (cv && c0 + u < nz) a.out[ob + (c0 + u) * pstride] = df_add(u0[u], v[u]);
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -358,21 +410,20 @@ __global__ void __launch_bounds__(128) k_kin_z_tc(KinTC a) {
   if (failed && tid == 0) a.status[3] = 1;
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 256);
+  if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
-constexpr size_t kSmemXY = 2 * kVS * kTileA + kTS * kTileB + 2 * 64 * kRaw * sizeof(float) + 1024;
-constexpr size_t kSmemZ = kVS * kTileA + kTS * kTileB + 1024;
-static_assert(128 * kStage * sizeof(float2) <= 2 * kVS * kTileA, "x-result staging must fit over the operand tiles");
+constexpr size_t kSmemXY = kBatchA + kTS * kTileB + 16 * 64 * sizeof(float) + 1024;
+constexpr size_t kSmemZ = kSmemXY;
+static_assert(2 * 64 * 64 * sizeof(float2) <= kBatchA, "x and y staging must fit over the operand tiles");
+static_assert(2 * (kSmemXY + 1024) <= 228 * 1024, "two CTAs per SM");
+static_assert(2 * kCols <= 512, "the accumulators of two CTAs must fit in tensor memory");
 
-template <typename K>
-int resident_grid(K kernel, int threads, size_t smem, int work) {
-  int dev = 0, sms = 0, per_sm = 0;
+int sm_count() {
+  int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-  const int g = std::max(1, sms) * std::max(1, per_sm);
-  return std::max(1, std::min(work, g));
+  return std::max(1, sms);
 }
 
 uint16_t half_bits(float x) {  // FP16 bits of a small integer (|x| <= 2048: exact)
@@ -384,9 +435,10 @@ uint16_t half_bits(float x) {  // FP16 bits of a small integer (|x| <= 2048: exa
 
 }  // namespace
 
-// Fixed-point FP16 slices of an n x n kinetic matrix: T = 2^(e_t - 7) (b1 + 2^-8 b2
-// + 2^-16 b3 + 2^-24 b4) + O(2^(e_t - 32)), each b an integer in [-128, 128], as
-// zero-padded [kTS][64][64] tiles (row = output index, column = contraction index).
+// Fixed-point FP16 slices of an n x n kinetic matrix: T = 2^(e_t - 8) (b1 + 2^-9 b2
+// + 2^-18 b3 + 2^-27 b4) + O(2^(e_t - 36)), each b an integer in [-256, 256]
+// rounded to nearest (a symmetric T stays symmetric), as zero-padded
+// [kTS][64][64] tiles (row = output index, column = contraction index).
 void kinetic_f16_slices(const std::vector<double>& T, int n, std::vector<uint16_t>* slices, int* e_t) {
   double m = 0.0;
   for (double x : T) m = std::max(m, std::fabs(x));
@@ -396,33 +448,33 @@ void kinetic_f16_slices(const std::vector<double>& T, int n, std::vector<uint16_
   slices->assign((size_t)kTS * 64 * 64, half_bits(0.f));
   for (int i = 0; i < n; ++i)
     for (int q = 0; q < n; ++q) {
-      double r = std::ldexp(T[(size_t)i * n + q], 7 - e);
+      double r = std::ldexp(T[(size_t)i * n + q], 8 - e);
       for (int l = 0; l < kTS; ++l) {
         const double b = std::nearbyint(r);
         (*slices)[((size_t)l * 64 + i) * 64 + q] = half_bits((float)b);
-        r = (r - b) * 256.0;
+        r = (r - b) * 512.0;
       }
     }
 }
 
 bool kinetic_tc_supported(const Tables& t) { return t.nx <= 64 && t.ny <= 64 && t.nz <= 64 && t.tx == t.ty; }
 
-int launch_kin_xy_tc(bsl_handle* h, const float* v, cudaStream_t s) {
+int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   const Tables& t = h->t;
   DeviceState& d = h->d;
   cudaFuncSetAttribute(k_kin_xy_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemXY);
   KinTC a{d.kxy_slices, d.e_txy, v, reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status};
-  k_kin_xy_tc<<<resident_grid(k_kin_xy_tc, 256, kSmemXY, (a.nplanes + 1) / 2), 256, kSmemXY, s>>>(a);
+  k_kin_xy_tc<<<std::min(a.nplanes, 2 * sm_count()), kTcThreads, kSmemXY, s>>>(a);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }
 
-int launch_kin_z_tc(bsl_handle* h, const float* v, cudaStream_t s) {
+int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   const Tables& t = h->t;
   DeviceState& d = h->d;
   cudaFuncSetAttribute(k_kin_z_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemZ);
   KinTC a{d.kz_slices, d.e_tz, v, reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status};
-  k_kin_z_tc<<<resident_grid(k_kin_z_tc, 128, kSmemZ, (a.nplanes + 1) / 2), 128, kSmemZ, s>>>(a);
+  k_kin_z_tc<<<std::min((a.nplanes + 1) / 2, 2 * sm_count()), kTcThreads, kSmemZ, s>>>(a);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }

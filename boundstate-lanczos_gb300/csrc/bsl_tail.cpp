@@ -73,11 +73,13 @@ void count_above_backward(const Tri& T, double x, int* all, int* hat) {
 }
 
 // Distinct eigenvalues in (lo, hi] with multiplicities (0 = spurious).
-void bisect(const Tri& T, double lo, double hi, std::vector<double>* vs, std::vector<int>* mp) {
+// `unit` is the unit roundoff behind the multiplicity tolerances: 2^-52 (kEps)
+// as in BISEC, or the effective unit roundoff of an inexact H v.
+void bisect(const Tri& T, double lo, double hi, double unit, std::vector<double>* vs, std::vector<int>* mp) {
   const int m = T.m;
   double tkmax = 0.0;
   for (int i = 0; i < m; ++i) tkmax = std::max(std::max(std::fabs(T.a[i]), T.b[i]), tkmax);
-  const double ttol = kEps * tkmax;
+  const double ttol = unit * tkmax;
   const double big = double(m + 1000);
   const double ep0 = big * ttol, ep1 = std::sqrt(big) * ttol;
   const int above_hi = count_above(T, hi);
@@ -223,7 +225,8 @@ void normalise(std::vector<double>& u, int mev) {
 }  // namespace
 
 int cw_good_eigenvalues(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
-                        double emax, double* eval, double* err, int* ngood) {
+                        double emax, double* eval, double* err, int* ngood, double unit) {
+  if (!(unit > 0.0)) unit = kEps;
   (void)beta2;  // recomputed from beta, as BISEC does
   Tri T;
   T.a = alpha;
@@ -235,7 +238,7 @@ int cw_good_eigenvalues(int niter, const double* alpha, const double* beta, cons
   for (int i = 0; i <= niter; ++i) T.b2[i] = T.b[i] * T.b[i];
   std::vector<double> vs;
   std::vector<int> mp;
-  bisect(T, emin, emax, &vs, &mp);
+  bisect(T, emin, emax, unit, &vs, &mp);
   flag_isolation(vs, &mp);
   // error estimates for isolated good eigenvalues
   const int nd = (int)vs.size();

@@ -131,13 +131,22 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
       for (int s = 0; s < NN; ++s) {
         asm volatile("prefetch.global.L2 [%0];" ::"l"(A.ukin + s * npts + p));
         asm volatile("prefetch.global.L2 [%0];" ::"l"(A.out + s * npts + p));
-        if (A.mode) asm volatile("prefetch.global.L2 [%0];" ::"l"(A.vec + s * npts + p));
+        if (A.mode == 1) asm volatile("prefetch.global.L2 [%0];" ::"l"(A.vec + s * npts + p));
       }
     }
-    float vv[NN], va[NN];
+    // mode 2 reads the pair of v once: its head is the FP32 copy (the block
+    // product's operand) and its tail is kept for alpha
+    float vv[NN], va[NN], vlo[NN];
 #pragma unroll
     for (int s = 0; s < NN; ++s) {
-      vv[s] = valid ? A.v32[s * npts + p] : 0.f;
+      if (A.mode == 2) {
+        const float2 x = valid ? Vp[s * npts + p] : make_float2(0.f, 0.f);
+        vv[s] = x.x;
+        vlo[s] = x.y;
+      } else {
+        vv[s] = valid ? A.v32[s * npts + p] : 0.f;
+        vlo[s] = 0.f;
+      }
       va[s] = 0.f;
     }
     int t = 0;
@@ -171,13 +180,12 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
         constexpr int kGroup = 7;  // loads of kGroup functions in flight before their arithmetic
 #pragma unroll
         for (int s0 = 0; s0 < NN; s0 += kGroup) {
-          float2 uk[kGroup], rr[kGroup], vq[kGroup];
+          float2 uk[kGroup], rr[kGroup];
 #pragma unroll
           for (int u = 0; u < kGroup; ++u)
             if (s0 + u < NN) {
               uk[u] = A.ukin[(s0 + u) * npts + p];
               rr[u] = Rp[(s0 + u) * npts + p];
-              vq[u] = Vp[(s0 + u) * npts + p];
             }
 #pragma unroll
           for (int u = 0; u < kGroup; ++u)
@@ -189,7 +197,7 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
               two_sum(hi, uk[u].y + e + __ldg(A.rot_lo + s) * vv[s], hi, lo);
               const float2 r = df_fma(cc, make_float2(hi, lo), rr[u]);
               Rp[s * npts + p] = r;
-              dacc = df_fma(vq[u], r, dacc);
+              dacc = df_fma(make_float2(vv[s], vlo[s]), r, dacc);
             }
         }
       } else {

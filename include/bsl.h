@@ -55,9 +55,10 @@ extern "C" {
 
 /* engine of the FP32 kinetic contractions in BSL_PREC_MIXED */
 #define BSL_KIN_SIMT 0   /* FP32 head/tail coefficients on the CUDA cores */
-#define BSL_KIN_TENSOR 1 /* TF32 splits on the tensor cores (tcgen05.mma), FP32
-                            accumulation in tensor memory; grids of at most 64
-                            points per axis with equal x and y axes */
+#define BSL_KIN_TENSOR 1 /* fixed-point FP16 slices on the tensor cores
+                            (tcgen05.mma), exact FP32 accumulation in tensor
+                            memory; grids of at most 64 points per axis with
+                            equal x and y axes */
 
 /* Lanczos start vector */
 #define BSL_START_UNIFORM 0 /* 1/sqrt(D) over the reference layout, as the
@@ -130,11 +131,13 @@ int bsl_packed_nn(const bsl_handle* h);
 /* Switch the arithmetic of later Hv applications (BSL_PREC_*). */
 int bsl_set_precision(bsl_handle* h, int precision);
 
-/* Select the kinetic engine of BSL_PREC_MIXED (BSL_KIN_*; bsl_hv_prep selects
-   BSL_KIN_SIMT).  BSL_ERR_UNSUPPORTED when the grid does not allow
-   BSL_KIN_TENSOR.  The tensor engine's FP32 accumulation inside the MMA is not
-   round-to-nearest: at 54^3 (dx = 0.0151 A) its levels deviate by up to
-   3e-2 cm^-1 from the FP64 run against 1.3e-4 cm^-1 for BSL_KIN_SIMT. */
+/* Select the kinetic engine of BSL_PREC_MIXED (BSL_KIN_*).  bsl_hv_prep selects
+   BSL_KIN_TENSOR where the grid allows it (at most 64 points per axis, equal x
+   and y axes), else BSL_KIN_SIMT; BSL_ERR_UNSUPPORTED when the grid does not
+   allow BSL_KIN_TENSOR.  The tensor engine slices the double-float Lanczos
+   vector exactly into FP16 fixed-point parts and accumulates exactly: its H v
+   deviates from the FP64 path by ~3e-9 relative, the CUDA-core engine's by
+   ~2e-7. */
 int bsl_set_kinetic_engine(bsl_handle* h, int engine);
 int bsl_kinetic_engine(const bsl_handle* h);
 
@@ -193,6 +196,19 @@ int bsl_lanczos_orthonormalize_static(double* d_vec, double* d_rvec, long long n
    need niter entries; *ngood receives the count. */
 int bsl_good_eigenvalues(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
                          double emax, double* eval, double* err, int* ngood);
+
+/* The same with the multiplicity tolerances of the bisection built on
+   `unit_roundoff` instead of the FP64 unit roundoff 2^-52: eigenvalues of T_m
+   closer than (niter + 1000) * unit_roundoff * max|T| count as one multiple
+   eigenvalue.  No counterpart in the reference.  For recurrences driven by an
+   inexact H v (BSL_PREC_MIXED): the converged copies of a level then scatter by
+   the H v noise instead of coinciding to FP64 rounding, and with the FP64
+   tolerance each copy is tested as a simple eigenvalue and can be discarded as
+   spurious.  BSL_MIXED_UNIT_ROUNDOFF is the value measured for BSL_PREC_MIXED
+   with the tensor-core kinetic. */
+#define BSL_MIXED_UNIT_ROUNDOFF 4.0e-15
+int bsl_good_eigenvalues_unit(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
+                              double emax, double unit_roundoff, double* eval, double* err, int* ngood);
 
 /* Tm eigenvectors for the first ngood good eigenvalues (lanczosvectors +
    TRIVEC, lanczosEigenValuesVectors.cpp:509-561): evtr is column-major

@@ -89,6 +89,28 @@ def test_tail_matches_oracle(bsl, name):
     assert np.allclose(er, er0, rtol=1e-12, atol=1e-300)
 
 
+def test_tail_unit_roundoff(bsl):
+    """bsl_good_eigenvalues_unit at the FP64 unit roundoff is the reference tail;
+    a larger unit merges copies of a level that scatter (as under an inexact H v)."""
+    d, man, _ = case_info("cpu_workload")
+    ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))
+    a = ref["alpha"]
+    b = np.concatenate([[0.0], ref["beta"]])
+    ev, er = bsl.good_eigenvalues(a, b, b * b)
+    eu, eru = bsl.good_eigenvalues(a, b, b * b, unit_roundoff=2.0 * 1.1102230246251565e-16)
+    assert np.array_equal(ev, eu) and np.array_equal(er, eru)
+    # two blocks: level 1.0 once, and level 2.0 as two copies 1e-9 apart joined by a
+    # tiny coupling; the FP64 tolerance sees two simple eigenvalues, a unit of 1e-12 one double
+    rng = np.random.default_rng(5)
+    m = 60
+    diag = np.concatenate([[1.0, 2.0, 2.0 + 1e-9], 5.0 + rng.random(m - 3)])
+    off = np.concatenate([[0.0], [1e-3, 1e-13], 0.5 + 0.1 * rng.random(m - 3)])
+    e64, _ = bsl.good_eigenvalues(diag, off, off * off, 0.0, 3.0)
+    e12, _ = bsl.good_eigenvalues(diag, off, off * off, 0.0, 3.0, unit_roundoff=1e-12)
+    near2 = lambda e: int(np.sum(np.abs(e - 2.0) < 1e-6))
+    assert near2(e12) <= near2(e64)
+
+
 def test_tm_eigenvectors_match_oracle(bsl):
     d, man, _ = case_info("seed1_n6_l3_odd")
     ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))

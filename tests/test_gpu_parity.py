@@ -78,7 +78,7 @@ def test_hv_mixed_engines_match_fp64(bsl, name):
     u = np.zeros(h.basis_size)
     h.hv(v, u)
     h.set_precision("mixed")
-    assert h.kinetic_engine() == "simt"  # the default engine
+    assert h.kinetic_engine() == "tensor"  # the default engine where the grid allows it
     out = {}
     for engine in ("simt", "tensor"):
         h.set_kinetic_engine(engine)
@@ -157,7 +157,7 @@ def test_lanczos_mixed_levels_within_1e3_cm(bsl, engine):
     h.set_precision("mixed")
     h.set_kinetic_engine(engine)
     am, bm, bm2 = h.lanczos(niter, start="normal", seed=0)
-    evm, _ = bsl.good_eigenvalues(am, bm, bm2, -10.0, 40.0)
+    evm, _ = bsl.good_eigenvalues(am, bm, bm2, -10.0, 40.0, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF)
     low = np.sort(stable)[:20]
     assert len(low) >= 8
     dev = np.array([np.min(np.abs(evm - e)) for e in low])
@@ -238,16 +238,31 @@ def test_mixed_recurrence_tracks_fp64(bsl):
     h.close()
 
 
-def test_ritz_vectors_mixed_match_fp64(bsl):
-    """Loop 2 on the double-float buffers gives the FP64 Ritz vectors to 1e-4."""
+def test_ritz_vectors_mixed_are_eigenvectors(bsl):
+    """Loop 2 on the double-float buffers: Ritz vectors of the mixed run are
+    eigenvectors of H (residual <= 1e-4) and overlap the FP64 ones to 1e-6."""
     h, d, man, extra = make(bsl, "seed1_n6_l3_odd")
     niter = 120
-    a, b, b2 = h.lanczos(niter)
-    ev, _ = bsl.good_eigenvalues(a, b, b2)
-    rows = bsl.tm_eigenvectors(a, b, b2, ev[:2])
-    R64 = h.ritz(niter, rows)
-    h.set_precision("mixed")
-    Rm = h.ritz(niter, rows)
-    for n in range(2):
-        assert np.max(np.abs(Rm[n] - R64[n])) <= 1e-4 * np.max(np.abs(R64[n]))
+
+    def ritz_pair(precision):
+        h.set_precision(precision)
+        a, b, b2 = h.lanczos(niter)
+        unit = bsl.MIXED_UNIT_ROUNDOFF if precision == "mixed" else None
+        ev, _ = bsl.good_eigenvalues(a, b, b2, unit_roundoff=unit)
+        rows = bsl.tm_eigenvectors(a, b, b2, ev[:1])
+        x = h.ritz(niter, rows)[0]
+        return ev[0], x / np.linalg.norm(x)
+
+    e64, x64 = ritz_pair("fp64")
+    em, xm = ritz_pair("mixed")
+    assert abs(em - e64) <= CM_TOL_MIXED
+    assert 1.0 - abs(float(x64 @ xm)) <= 1e-6
+    h.set_precision("fp64")
+    u = np.zeros(h.basis_size)
+    h.hv(xm, u)
+    keep = np.zeros(h.basis_size, bool)
+    npts = h.basis_size // (h.params.l_max + 1) ** 2
+    for s in full_indices(h):
+        keep[s * npts:(s + 1) * npts] = True
+    assert np.linalg.norm(u[keep] - em * xm[keep]) <= 1e-4
     h.close()
