@@ -163,6 +163,15 @@ def measured_peak_hbm():
         return 6800.0, "fallback 6.8 TB/s"
 
 
+# DRAM bytes (read + write) per launch from one ncu capture of each mixed-path
+# kernel at the metric workload (profiles/k_*_54cubed_odd_l5.md).  Writes that
+# stay in L2 until after the kernel are not counted there.
+NCU_TRAFFIC = {"k_kin_xy_tc": (26.59e6, "profiles/k_kin_xy_tc_54cubed_odd_l5.md"),
+               "k_kin_z_tc": (53.14e6, "profiles/k_kin_z_tc_54cubed_odd_l5.md"),
+               "k_vstream<NN>": (229.86e6, "profiles/k_vstream_54cubed_odd_l5.md"),
+               "k_update_pair": (52.97e6, "profiles/k_update_pair_54cubed_odd_l5.md")}
+
+
 def stage_bytes(cfg, D, N, nn, mixed):
     """Algorithmic bytes per launch of each stage of one Lanczos iteration."""
     ntri = nn * (nn + 1) // 2
@@ -365,7 +374,11 @@ def main():
                         "layout, H2D + Hv + recurrence + D2H per step"},
         "roofline": {"bound": "hbm", "kernel": stage_names[dom] if stage_names else None,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": peak_src + " (of measured)",
+                     "traffic": (NCU_TRAFFIC[stage_names[dom]][0]
+                                 if stage_names and stage_names[dom] in NCU_TRAFFIC else None),
+                     "traffic_source": (NCU_TRAFFIC[stage_names[dom]][1]
+                                        if stage_names and stage_names[dom] in NCU_TRAFFIC else None),
+                     "peak_source": peak_src + " (of measured)",
                      "algorithmic_bytes_per_launch": sb[dom], "ms_per_launch": float(stage_ms[dom])},
         "iteration_roofline": {"bytes_per_iteration": it_bytes,
                                "achieved_GBs": it_bytes / (ms_step * 1e-3) / 1e9 / world,
