@@ -84,6 +84,9 @@ def lib():
     L.bsl_good_eigenvalues.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_int)]
     L.bsl_good_eigenvalues_unit.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, _P, _P,
                                             C.POINTER(C.c_int)]
+    L.bsl_write_boundstates.argtypes = [C.c_char_p, C.c_char_p, C.c_int, _P, _P]
+    L.bsl_write_tm_vectors.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, _P]
+    L.bsl_write_ritz_vectors.argtypes = [C.c_char_p, C.c_char_p, C.c_longlong, C.c_int, _P]
     L.bsl_tm_eigenvectors.argtypes = [C.c_int, _P, _P, _P, _P, C.c_int, _P]
     L.bsl_ritz_vectors.argtypes = [C.c_void_p, C.c_int, _P, C.c_int, _P]
     L.bsl_last_run_ms_per_iter.argtypes = [C.c_void_p, _P]
@@ -137,6 +140,26 @@ def tm_eigenvectors(alpha, beta, beta2, evals):
     out = np.zeros(niter * ngood)
     _check(lib().bsl_tm_eigenvectors(niter, _ptr(alpha), _ptr(beta), _ptr(beta2), _ptr(evals), ngood, _ptr(out)))
     return out.reshape(ngood, niter)  # row n = column n of the column-major evtr
+
+
+def write_boundstates(directory, sim_descr, evals, errs):
+    """boundstates.txt and states_zpe.txt in the reference's format."""
+    evals, errs = (np.ascontiguousarray(x, dtype=np.float64) for x in (evals, errs))
+    _check(lib().bsl_write_boundstates(directory.encode(), sim_descr.encode(), len(evals), _ptr(evals), _ptr(errs)))
+
+
+def write_tm_vectors(directory, sim_descr, evtr_rows):
+    """lv: squared Tm eigenvector coefficients (rows as from tm_eigenvectors)."""
+    rows = np.ascontiguousarray(evtr_rows, dtype=np.float64)
+    ngood, niter = rows.shape
+    _check(lib().bsl_write_tm_vectors(directory.encode(), sim_descr.encode(), niter, ngood, _ptr(rows.reshape(-1))))
+
+
+def write_ritz_vectors(directory, sim_descr, ritz):
+    """eigVecFile.txt: Ritz vectors (ngood x basis_size) in the reference layout."""
+    r = np.ascontiguousarray(ritz, dtype=np.float64)
+    ngood, size = r.shape
+    _check(lib().bsl_write_ritz_vectors(directory.encode(), sim_descr.encode(), size, ngood, _ptr(r.reshape(-1))))
 
 
 class Hamiltonian:

@@ -16,9 +16,9 @@ inline int grid_for(long long n) {
 
 // ---------------------------------------------------------------------------
 // FP64 <-> FP32 conversions with integer operations only.  GB300 executes FP64
-// arithmetic at about 1/64 of the FP32 rate, so the mixed-precision kernels
-// keep FP64 instructions for the Lanczos recurrence and do conversions on the
-// integer pipe.
+// arithmetic at about one operation per clock per SM, so the mixed-precision
+// kernels avoid FP64 instructions per vector element: conversions run on the
+// integer pipe and the Lanczos recurrence in double-float arithmetic below.
 // ---------------------------------------------------------------------------
 // FP32 value of an FP64 number rounded to nearest, ties to even (the same as
 // a hardware conversion for normal results); magnitudes below the FP32 normal
@@ -89,8 +89,33 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
   return make_float2(s, t);
 }
 
+// Double-float addition without the second error term ("sloppy" addition,
+// 11 operations): relative error ~2^-44 of |a| + |b| rather than of the sum;
+// for adding terms whose own error is already larger than that.
+__device__ __forceinline__ float2 df_add_fast(float2 a, float2 b) {
+  float s, e;
+  two_sum(a.x, b.x, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+  fast_two_sum(s, e, s, e);
+  return make_float2(s, e);
+}
+
 // a * b + c
 __device__ __forceinline__ float2 df_fma(float2 a, float2 b, float2 c) { return df_add(df_mul(a, b), c); }
+
+// a * b + c with the fast addition: for accumulations and updates whose terms
+// carry FP32-level noise of their own (relative error ~2^-44 of |a b| + |c|)
+__device__ __forceinline__ float2 df_fma_fast(float2 a, float2 b, float2 c) { return df_add_fast(df_mul(a, b), c); }
+
+// a^2 as a double-float (exact head product, 5 operations)
+__device__ __forceinline__ float2 df_sqr(float2 a) {
+  const float p = __fmul_rn(a.x, a.x);
+  float e = __fmaf_rn(a.x, a.x, -p);
+  e = __fmaf_rn(__fmul_rn(2.f, a.x), a.y, e);
+  float s, t;
+  fast_two_sum(p, e, s, t);
+  return make_float2(s, t);
+}
 
 __device__ __forceinline__ float2 df_scale2(float2 a, float g) {  // g a power of two: exact
   return make_float2(__fmul_rn(a.x, g), __fmul_rn(a.y, g));

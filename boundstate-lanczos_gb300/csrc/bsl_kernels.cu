@@ -392,11 +392,11 @@ __global__ void __launch_bounds__(256, 3) k_update_pair(const float2* __restrict
     for (int u = 0; u < kUnroll; ++u) {
       const long long q = base + (long long)u * blockDim.x;
       if (q < L2) {
-        const float2 r0 = df_scale2(df_fma(na, make_float2(v[u].x, v[u].y), make_float2(r[u].x, r[u].y)), g);
-        const float2 r1 = df_scale2(df_fma(na, make_float2(v[u].z, v[u].w), make_float2(r[u].z, r[u].w)), g);
+        const float2 r0 = df_scale2(df_fma_fast(na, make_float2(v[u].x, v[u].y), make_float2(r[u].x, r[u].y)), g);
+        const float2 r1 = df_scale2(df_fma_fast(na, make_float2(v[u].z, v[u].w), make_float2(r[u].z, r[u].w)), g);
         R4[q] = make_float4(r0.x, r0.y, r1.x, r1.y);
-        acc = df_fma(r0, r0, acc);
-        acc = df_fma(r1, r1, acc);
+        acc = df_add_fast(df_sqr(r0), acc);
+        acc = df_add_fast(df_sqr(r1), acc);
         const long long e0 = 2 * q;
         if (v32_next) {  // only the CUDA-core kinetic reads the FP32 copy
           if (e0 + 1 < D)
@@ -409,9 +409,9 @@ __global__ void __launch_bounds__(256, 3) k_update_pair(const float2* __restrict
   }
   if ((L & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
     const long long i = L - 1;
-    const float2 r = df_scale2(df_fma(na, V[i], R[i]), g);
+    const float2 r = df_scale2(df_fma_fast(na, V[i], R[i]), g);
     R[i] = r;
-    acc = df_fma(r, r, acc);
+    acc = df_add_fast(df_sqr(r), acc);
     if (v32_next && i < D) v32_next[i] = r.x;
   }
   double total;

@@ -15,15 +15,16 @@
 //   of the planes (D[(p, x)][z] = sum_q v(p, q, x) Tz[z][q]).
 //
 // Exactness (error-free slicing after Ozaki, Ogita, Oishi and Rump,
-// Numer. Algorithms 59, 2012, here with 9-bit fixed-point slices): each operand
-// row (a row or a column of a plane of the double-float Lanczos vector) is
-// scaled by a power of two to below 1 in magnitude and cut into four 9-bit
-// signed integer slices, v = 2^(e_row - 8) (a1 + 2^-9 a2 + 2^-18 a3 + 2^-27 a4)
-// (36 bits relative to the row maximum; one scale per plane instead raises the
-// noise of H v where a plane's rows differ in size); T is scaled from its
-// largest element and cut into four slices the same way, rounded to nearest so
-// that the symmetric T stays exactly symmetric (a Lanczos recurrence on a
-// non-symmetric H scatters the converged copies of a level).  The slices are
+// Numer. Algorithms 59, 2012, here with 9-bit fixed-point slices): the values of
+// the double-float Lanczos vector are scaled by a power of two to below 1 in
+// magnitude -- one scale per (y, x) plane for x and y, one per operand row for
+// z -- and cut into four 9-bit signed integer slices,
+// v = 2^(e - 8) (a1 + 2^-9 a2 + 2^-18 a3 + 2^-27 a4) (36 bits relative to the
+// scale's maximum: far below the FP32 noise of the potential apply); T is
+// scaled from its largest element and cut into four slices the same way,
+// rounded to nearest so that the symmetric T stays exactly symmetric (a
+// Lanczos recurrence on a non-symmetric H scatters the converged copies of a
+// level).  The slices are
 // integers in [-256, 256], exact in FP16, their products are exact, and every
 // partial sum of one product class (at most 4 products of 64 terms) is an
 // integer of magnitude at most 2^24: the FP32 accumulation in tensor memory is
@@ -33,7 +34,7 @@
 // The rounding of T is the same along each Toeplitz diagonal and adds up
 // coherently for smooth states: with 36 bits it shifts levels by ~1e-7 kJ/mol
 // per axis.
-
+//
 // Pipeline: persistent CTAs, two per SM with 256 tensor-memory columns each, so
 // that one CTA slices or finishes its epilogue while the other's products run.
 #include <cuda_fp16.h>
@@ -120,17 +121,17 @@ __device__ __forceinline__ void issue_products(uint32_t d, uint32_t a, uint32_t 
   }
 }
 
-// the four class accumulators of 16 consecutive columns combined into
+// the four class accumulators of 8 consecutive columns combined into
 // double-float pairs and multiplied by `scale` (a power of two)
-__device__ __forceinline__ void load_pairs(uint32_t taddr, float scale, float2 (&out)[16]) {
-  float c0[16], c1[16], c2[16], c3[16];
-  tc::tmem_ld16_nowait(taddr, c0);
-  tc::tmem_ld16_nowait(taddr + 64u, c1);
-  tc::tmem_ld16_nowait(taddr + 128u, c2);
-  tc::tmem_ld16_nowait(taddr + 192u, c3);
+__device__ __forceinline__ void load_pairs8(uint32_t taddr, float scale, float2 (&out)[8]) {
+  float c0[8], c1[8], c2[8], c3[8];
+  tc::tmem_ld8_nowait(taddr, c0);
+  tc::tmem_ld8_nowait(taddr + 64u, c1);
+  tc::tmem_ld8_nowait(taddr + 128u, c2);
+  tc::tmem_ld8_nowait(taddr + 192u, c3);
   tc::tmem_wait_ld();
 #pragma unroll
-  for (int u = 0; u < 16; ++u) {
+  for (int u = 0; u < 8; ++u) {
     float h, e1, e2, l;
     two_sum(c0[u], __fmul_rn(c1[u], 0x1p-9f), h, e1);
     two_sum(h, __fmul_rn(c2[u], 0x1p-18f), h, e2);
@@ -152,33 +153,26 @@ __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefe
 
 
 
-// Row maxima of a 64 x 64 plane held as 4 x 4 blocks (thread (bj, bi) = tid / 16,
-// tid % 16): the 16 threads of one block row are 16 consecutive lanes.
-__device__ __forceinline__ void block_row_max(const float2 (&x)[4][4], float (&rm)[4]) {
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    float m = fmaxf(fmaxf(fabsf(x[r][0].x), fabsf(x[r][1].x)), fmaxf(fabsf(x[r][2].x), fabsf(x[r][3].x)));
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    rm[r] = m;
-  }
-}
-
-// Column maxima of the same blocks through shared memory (part: [16][64] floats).
-// Contains a __syncthreads.
+// Column maxima of the same blocks through shared memory (part: [16][64]
+// partials, then [64] maxima).  Contains two __syncthreads.
 __device__ __forceinline__ void block_col_max(const float2 (&x)[4][4], float* part, int bj, int bi, float (&cm)[4]) {
 #pragma unroll
   for (int c = 0; c < 4; ++c)
     part[bj * 64 + 4 * bi + c] =
         fmaxf(fmaxf(fabsf(x[0][c].x), fabsf(x[1][c].x)), fmaxf(fabsf(x[2][c].x), fabsf(x[3][c].x)));
   __syncthreads();
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
+  if (threadIdx.x < 64) {
     float m = 0.f;
 #pragma unroll
-    for (int q = 0; q < 16; ++q) m = fmaxf(m, part[q * 64 + 4 * bi + c]);
-    cm[c] = m;
+    for (int q = 0; q < 16; ++q) m = fmaxf(m, part[q * 64 + threadIdx.x]);
+    part[16 * 64 + threadIdx.x] = m;
   }
+  __syncthreads();
+  const float4 m4 = *reinterpret_cast<const float4*>(part + 16 * 64 + 4 * bi);
+  cm[0] = m4.x;
+  cm[1] = m4.y;
+  cm[2] = m4.z;
+  cm[3] = m4.w;
 }
 
 // Slices of a 4 x 4 block, each row r scaled by sc[r] and written as row row0 + r
@@ -202,9 +196,43 @@ __device__ __forceinline__ void write_block(uint8_t* A, const float2 (&x)[4][4],
   }
 }
 
+// Slices of a 4 x 4 block with one scale, written both as rows row_a + r (K =
+// c0..) and as rows row_b + c (K = r0..).
+__device__ __forceinline__ void write_block_both(uint8_t* A, const float2 (&x)[4][4], float sc, int row_a, int row_b,
+                                                 int r0, int c0) {
+  float s[4][4][kVS];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) slice4(__fmul_rn(x[r][c].x, sc), __fmul_rn(x[r][c].y, sc), s[r][c]);
+#pragma unroll
+  for (int k = 0; k < kVS; ++k) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      *reinterpret_cast<uint2*>(A + k * kTileA + quad_offset(row_a + r, c0)) =
+          make_uint2(pack_h2(s[r][0][k], s[r][1][k]), pack_h2(s[r][2][k], s[r][3][k]));
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      *reinterpret_cast<uint2*>(A + k * kTileA + quad_offset(row_b + c, r0)) =
+          make_uint2(pack_h2(s[0][c][k], s[1][c][k]), pack_h2(s[2][c][k], s[3][c][k]));
+  }
+}
+
+// maximum over the CTA (red: one float per warp); contains a __syncthreads
+__device__ __forceinline__ float cta_max(float m, float* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  m = red[0];
+#pragma unroll
+  for (int w = 1; w < kTcThreads / 32; ++w) m = fmaxf(m, red[w]);
+  return m;
+}
+
 // x and y contractions; out(y, x) = (Tx v + Ty v) as double-float pairs.  One
-// plane per batch: operand rows 0-63 are the plane's rows (each scaled by its own
-// maximum), rows 64-127 its columns (each scaled by its own maximum).  Two CTAs
+// plane per batch: operand rows 0-63 are the plane's rows, rows 64-127 its
+// columns, all with one scale per plane (each value is sliced once).  Two CTAs
 // per SM, 256 tensor-memory columns each.
 __global__ void __launch_bounds__(kTcThreads, 2) k_kin_xy_tc(KinTC a) {
   extern __shared__ uint8_t smraw[];
@@ -217,10 +245,11 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_kin_xy_tc(KinTC a) {
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_slot;
   __shared__ int failed;
-  __shared__ int e_row[128];
+  __shared__ int e_plane;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int nx = a.nx, ny = a.ny;
   const long long psz = (long long)ny * nx;
+  int plane_parity = 0;  // alternates the reduction slots of consecutive planes
   load_b(B, a.tslices);
   if (tid == 0) {
     failed = 0;
@@ -236,10 +265,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_kin_xy_tc(KinTC a) {
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   const int half = warp >> 2;
   const int bj = tid >> 4, bi = tid & 15;  // 4 x 4 block of the plane sliced by this thread
-  uint32_t phase = 0;
-  for (int plane = blockIdx.x; plane < a.nplanes; plane += gridDim.x) {
+  // this thread's 4 x 4 block of a plane, loaded one plane ahead (software pipeline)
+  auto load_block = [&](int plane, float2 (&x)[4][4]) {
     const float2* src = a.v + (long long)plane * psz;
-    float2 x[4][4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -247,23 +275,32 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_kin_xy_tc(KinTC a) {
         const int j = 4 * bj + r, i = 4 * bi + c;
         x[r][c] = (j < ny && i < nx) ? __ldg(src + (long long)j * nx + i) : make_float2(0.f, 0.f);
       }
-    const int nxt = plane + (int)gridDim.x;  // the next plane into L2
-    if (nxt < a.nplanes)
-      for (long long o = (long long)tid * 4; o < psz; o += kTcThreads * 4)
-        prefetch_l2(a.v + (long long)nxt * psz + o);
-    float rm[4], cm[4], sr[4], scl[4];
-    block_row_max(x, rm);
-    block_col_max(x, part, bj, bi, cm);
+  };
+  float2 xn[4][4];
+  if ((int)blockIdx.x < a.nplanes) load_block(blockIdx.x, xn);
+  uint32_t phase = 0;
+  for (int plane = blockIdx.x; plane < a.nplanes; plane += gridDim.x) {
+    float2 x[4][4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int er = plane_exponent(rm[u]), ec = plane_exponent(cm[u]);
-      sr[u] = pow2f(8 - er);
-      scl[u] = pow2f(8 - ec);
-      if (bi == 0) e_row[4 * bj + u] = er;
-      if (bj == 0) e_row[64 + 4 * bi + u] = ec;
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) x[r][c] = xn[r][c];
+    const int nxt = plane + (int)gridDim.x;
+    {  // the plane after next into L2
+      const int far = nxt + (int)gridDim.x;
+      if (far < a.nplanes)
+        for (long long o = (long long)tid * 4; o < psz; o += kTcThreads * 4) prefetch_l2(a.v + (long long)far * psz + o);
     }
-    write_block<true>(A, x, sr, 4 * bj, 4 * bi);
-    write_block<false>(A, x, scl, 64 + 4 * bi, 4 * bj);
+    // one scale per plane: every operand row keeps 36 bits relative to the plane maximum
+    float m = 0.f;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) m = fmaxf(m, fabsf(x[r][c].x));
+    const int e = plane_exponent(cta_max(m, part + 16 * 64 + (plane_parity ? 8 : 0)));
+    plane_parity ^= 1;
+    if (tid == 0) e_plane = e;
+    write_block_both(A, x, pow2f(8 - e), 4 * bj, 64 + 4 * bi, 4 * bj, 4 * bi);
     tc::fence_smem_to_async();
     tc::fence_before_sync();
     __syncthreads();
@@ -272,23 +309,24 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_kin_xy_tc(KinTC a) {
       issue_products(tmem, tc::smem_u32(A), tc::smem_u32(B));
       tc::mma_commit(&bar);
     }
+    if (nxt < a.nplanes) load_block(nxt, xn);  // in flight during the products and the epilogue
     if (!failed && !tc::mbar_wait(&bar, phase)) failed = 1;
     phase ^= 1u;
     tc::fence_after_sync();
     __syncthreads();
     if (failed) break;
     // epilogue: rows 0-63 (x part) and 64-127 (y part) to shared memory over A
-    const float scale = pow2f(e_row[lrow] + a.e_t - 16);
+    const float scale = pow2f(e_plane + a.e_t - 16);
 #pragma unroll 1
-    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 16) {
-      float2 v[16];
-      load_pairs(tmem + lane_base + (uint32_t)c0, scale, v);
+    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 8) {
+      float2 v[8];
+      load_pairs8(tmem + lane_base + (uint32_t)c0, scale, v);
       if (lrow < 64) {  // x part: row y = lrow, columns x
 #pragma unroll
-        for (int u = 0; u < 16; ++u) Xs[lrow * 64 + ((c0 + u) ^ (lrow & 31))] = v[u];
+        for (int u = 0; u < 8; ++u) Xs[lrow * 64 + ((c0 + u) ^ (lrow & 31))] = v[u];
       } else {          // y part: x = lrow - 64, columns y
 #pragma unroll
-        for (int u = 0; u < 16; ++u) Ys[(c0 + u) * 64 + (lrow - 64)] = v[u];
+        for (int u = 0; u < 8; ++u) Ys[(c0 + u) * 64 + (lrow - 64)] = v[u];
       }
     }
     tc::fence_before_sync();
@@ -296,8 +334,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_kin_xy_tc(KinTC a) {
     const int i = tid & 63;
     float2* dst = a.out + (long long)plane * psz;
     if (i < nx)
+#pragma unroll 2
       for (int j = tid >> 6; j < ny; j += kTcThreads / 64)
-        dst[(long long)j * nx + i] = df_add(Xs[j * 64 + (i ^ (j & 31))], Ys[j * 64 + i]);
+        dst[(long long)j * nx + i] = df_add_fast(Xs[j * 64 + (i ^ (j & 31))], Ys[j * 64 + i]);
     __syncthreads();  // A (under Xs, Ys) is sliced again next
   }
   if (failed && tid == 0) a.status[3] = 1;
@@ -341,38 +380,53 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_kin_z_tc(KinTC a) {
   auto plane_base = [&](int plane) {  // plane = s * ny + y
     return (long long)(plane / ny) * nz * pstride + (long long)(plane % ny) * nx;
   };
+  // this thread's 4 x 4 block of one plane (zeros beyond the planes)
+  auto load_block = [&](int plane, float2 (&x)[4][4]) {
+    const bool pv = plane < a.nplanes;
+    const float2* src = a.v + (pv ? plane_base(plane) : 0);
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int k = 4 * bk + r, i = 4 * bi + c;
+        x[r][c] = (pv && k < nz && i < nx) ? __ldg(src + k * pstride + i) : make_float2(0.f, 0.f);
+      }
+  };
+  auto slice_plane = [&](int pl, const float2 (&x)[4][4]) {
+    float cm[4], scl[4];
+    block_col_max(x, part, bk, bi, cm);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int ec = plane_exponent(cm[u]);
+      scl[u] = pow2f(8 - ec);
+      if (bk == 0) e_row[pl * 64 + 4 * bi + u] = ec;
+    }
+    write_block<false>(A, x, scl, pl * 64 + 4 * bi, 4 * bk);
+    __syncthreads();  // part[] is reused by the next plane
+  };
+  float2 xn[4][4];  // first plane of the next pair, loaded during the products (software pipeline)
+  if ((int)blockIdx.x < npairs) load_block(2 * blockIdx.x, xn);
   uint32_t phase = 0;
   for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x) {
-#pragma unroll 1
-    for (int pl = 0; pl < 2; ++pl) {
-      const int plane = 2 * pair + pl;
-      const bool pv = plane < a.nplanes;
-      const float2* src = a.v + (pv ? plane_base(plane) : 0);
-      float2 x[4][4];
+    {
+      float2 x0[4][4], x1[4][4];
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const int k = 4 * bk + r, i = 4 * bi + c;
-          x[r][c] = (pv && k < nz && i < nx) ? __ldg(src + k * pstride + i) : make_float2(0.f, 0.f);
-        }
-      float cm[4], scl[4];
-      block_col_max(x, part, bk, bi, cm);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int ec = plane_exponent(cm[u]);
-        scl[u] = pow2f(8 - ec);
-        if (bk == 0) e_row[pl * 64 + 4 * bi + u] = ec;
-      }
-      write_block<false>(A, x, scl, pl * 64 + 4 * bi, 4 * bk);
-      __syncthreads();  // part[] is reused by the next plane
+        for (int c = 0; c < 4; ++c) x0[r][c] = xn[r][c];
+      load_block(2 * pair + 1, x1);  // in flight while the first plane is sliced
+      slice_plane(0, x0);
+      slice_plane(1, x1);
     }
-    const int nxt = pair + (int)gridDim.x;  // the next pair's columns into L2
-    if (nxt < npairs) {
-      const int plane = 2 * nxt + (tid >> 7);
-      const int i = (tid & 127) * 4;
-      if (plane < a.nplanes && i < nx)
-        for (int k = 0; k < nz; ++k) prefetch_l2(a.v + plane_base(plane) + k * pstride + i);
+    const int nxt = pair + (int)gridDim.x;
+    {  // the pair after next into L2
+      const int far = nxt + (int)gridDim.x;
+      if (far < npairs) {
+        const int plane = 2 * far + (tid >> 7);
+        const int i = (tid & 127) * 4;
+        if (plane < a.nplanes && i < nx)
+          for (int k = 0; k < nz; ++k) prefetch_l2(a.v + plane_base(plane) + k * pstride + i);
+      }
     }
     tc::fence_smem_to_async();
     tc::fence_before_sync();
@@ -381,6 +435,16 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_kin_z_tc(KinTC a) {
     if (tid == 0 && !failed) {
       issue_products(tmem, tc::smem_u32(A), tc::smem_u32(B));
       tc::mma_commit(&bar);
+    }
+    if (nxt < npairs) load_block(2 * nxt, xn);
+    {  // this thread's epilogue targets into L1 while the products run
+      const int pl = lrow >> 6, i = lrow & 63;
+      const int plane = 2 * pair + pl;
+      if (plane < a.nplanes && i < nx) {
+        const long long ob = plane_base(plane) + i;
+        for (int k = half * 32; k < half * 32 + 32 && k < nz; ++k)
+          asm volatile("prefetch.global.L1 [%0];" ::"l"(a.out + ob + k * pstride));
+      }
     }
     if (!failed && !tc::mbar_wait(&bar, phase)) failed = 1;
     phase ^= 1u;
@@ -393,15 +457,15 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_kin_z_tc(KinTC a) {
     const long long ob = cv ? plane_base(plane) + i : 0;
     const float scale = pow2f(e_row[lrow] + a.e_t - 16);
 #pragma unroll 1
-    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 16) {
-      float2 v[16], u0[16];
+    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 8) {
+      float2 v[8], u0[8];
 #pragma unroll
-      for (int u = 0; u < 16; ++u)
+      for (int u = 0; u < 8; ++u)
         u0[u] = (cv && c0 + u < nz) ? a.out[ob + (c0 + u) * pstride] : make_float2(0.f, 0.f);
-      load_pairs(tmem + lane_base + (uint32_t)c0, scale, v);
+      load_pairs8(tmem + lane_base + (uint32_t)c0, scale, v);
 #pragma unroll
-      for (int u = 0; u < 16; ++u)
-        if (cv && c0 + u < nz) a.out[ob + (c0 + u) * pstride] = df_add(u0[u], v[u]);
+      for (int u = 0; u < 8; ++u)
+        if (cv && c0 + u < nz) a.out[ob + (c0 + u) * pstride] = df_add_fast(u0[u], v[u]);
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -413,7 +477,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_kin_z_tc(KinTC a) {
   if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
-constexpr size_t kSmemXY = kBatchA + kTS * kTileB + 16 * 64 * sizeof(float) + 1024;
+constexpr size_t kSmemXY = kBatchA + kTS * kTileB + 17 * 64 * sizeof(float) + 1024;
 constexpr size_t kSmemZ = kSmemXY;
 static_assert(2 * 64 * 64 * sizeof(float2) <= kBatchA, "x and y staging must fit over the operand tiles");
 static_assert(2 * (kSmemXY + 1024) <= 228 * 1024, "two CTAs per SM");

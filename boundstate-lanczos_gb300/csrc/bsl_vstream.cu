@@ -195,9 +195,9 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
               float hi, e, lo;
               two_sum(uk[u].x, a, hi, e);
               two_sum(hi, uk[u].y + e + __ldg(A.rot_lo + s) * vv[s], hi, lo);
-              const float2 r = df_fma(cc, make_float2(hi, lo), rr[u]);
+              const float2 r = df_fma_fast(cc, make_float2(hi, lo), rr[u]);
               Rp[s * npts + p] = r;
-              dacc = df_fma(make_float2(vv[s], vlo[s]), r, dacc);
+              dacc = df_fma_fast(make_float2(vv[s], vlo[s]), r, dacc);
             }
         }
       } else {

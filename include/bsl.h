@@ -221,6 +221,15 @@ int bsl_tm_eigenvectors(int niter, const double* alpha, const double* beta, cons
    layout, D = bsl_basis_size(h). */
 int bsl_ritz_vectors(bsl_handle* h, int niter, const double* evtr, int ngood, double* ritz);
 
+/* Result files in the reference's formats (lanczosEigenValuesVectors.cpp):
+   boundstates.txt + states_zpe.txt (:263-290), lv (:339-364, evtr column-major
+   [niter x ngood]) and eigVecFile.txt (:470-492, ritz[n * basis_size + row]),
+   written into `dir` with the simulation description sim_descr. */
+int bsl_write_boundstates(const char* dir, const char* sim_descr, int ngood, const double* eval, const double* err);
+int bsl_write_tm_vectors(const char* dir, const char* sim_descr, int niter, int ngood, const double* evtr);
+int bsl_write_ritz_vectors(const char* dir, const char* sim_descr, long long basis_size, int ngood,
+                           const double* ritz);
+
 /* Timing of the last bsl_lanczos_run: average device milliseconds per
    iteration, measured with CUDA events on the library's stream. */
 int bsl_last_run_ms_per_iter(const bsl_handle* h, double* ms);

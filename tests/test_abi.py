@@ -139,3 +139,65 @@ def test_tail_breakdown_free_on_tiny_matrix(bsl):
     w = np.linalg.eigvalsh(np.array([[1.5, 0.25], [0.25, -0.5]]))
     for e in ev:
         assert np.min(np.abs(w - e)) <= 1e-12
+
+
+def _lanczos_limits(d):
+    lines = open(os.path.join(d, "lanczos_input.txt")).read().split("\n")
+    vals = {l.split("=")[0]: l.split("=")[1].strip() for l in lines if "=" in l}
+    return float(vals["EigenvalueOpenLowerLimit(kJ/mol)"]), float(vals["EigenvalueClosedUpperLimit(kJ/mol)"])
+
+
+@pytest.mark.parametrize("name", ["cage11_n10_l3_all", "seed1_n6_l3_odd", "seed0_n5_l4_even", "iso_n20_l2_all",
+                                  "cpu_workload"])
+def test_boundstates_file_matches_reference(bsl, name, tmp_path):
+    """boundstates.txt written from the tail on the reference's alpha/beta has the
+    reference's layout, states and eigenvalues (the stored alpha/beta are the
+    reference's printed values, so the last digits can move: 1e-10 relative); the
+    error column depends on the random start of the inverse iteration and is
+    compared to a factor 10."""
+    d, man, _ = case_info(name)
+    ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))
+    b = np.concatenate([[0.0], ref["beta"]])
+    emin, emax = _lanczos_limits(d)
+    ev, er = bsl.good_eigenvalues(ref["alpha"], b, b * b, emin, emax)
+    rlines = open(os.path.join(d, "ref_boundstates.txt")).read().split("\n")
+    descr = rlines[1].split("simulation ", 1)[1]
+    bsl.write_boundstates(str(tmp_path), descr, ev, er)
+    mlines = open(os.path.join(tmp_path, "boundstates.txt")).read().split("\n")
+    assert len(mlines) == len(rlines)
+    assert mlines[:4] == rlines[:4]
+    for m, r in zip(mlines[4:], rlines[4:]):
+        mf, rf = m.split(), r.split()
+        assert mf[:1] == rf[:1]
+        if mf:
+            assert len(mf[1]) == len(rf[1]) and float(mf[1]) == pytest.approx(float(rf[1]), rel=1e-10, abs=1e-12)
+            em, erf = float(mf[2]), float(rf[2])
+            assert (em < 1e-12 and erf < 1e-12) or abs(np.log10(max(em, 1e-300) / max(erf, 1e-300))) < 1.0
+    zpe = open(os.path.join(tmp_path, "states_zpe.txt")).read().split("\n")
+    assert zpe[3] == "Zero Point Energy = %.15e kJ/mol" % ev[0]
+    assert float(zpe[-2].split()[1]) == pytest.approx(ev[-1] - ev[0], rel=1e-15)
+
+
+def test_lv_and_ritz_file_layout(bsl, tmp_path):
+    """lv and eigVecFile.txt follow the reference's layout (squared coefficients
+    with running norms; one row per basis index)."""
+    d, man, _ = case_info("seed1_n6_l3_odd")
+    ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))
+    a = ref["alpha"]
+    b = np.concatenate([[0.0], ref["beta"]])
+    ev, _ = bsl.good_eigenvalues(a, b, b * b)
+    rows = bsl.tm_eigenvectors(a, b, b * b, ev[:2])
+    bsl.write_tm_vectors(str(tmp_path), "case", rows)
+    lv = open(os.path.join(tmp_path, "lv")).read().split("\n")
+    assert lv[0] == "" and lv[2] == "Number of Eigenvectors: 2"
+    assert lv[3] == "Iteration | Coefficient Squared | Cumulative Norm "
+    body = [l.split() for l in lv[4:] if l.strip()]
+    assert len(body) == len(a)
+    last = np.array([float(x) for x in body[-1][1:]])
+    assert np.allclose(last[1::2], np.sum(rows ** 2, axis=1), rtol=1e-14)
+    ritz = np.random.default_rng(1).standard_normal((2, 7))
+    bsl.write_ritz_vectors(str(tmp_path), "case", ritz)
+    ev_lines = open(os.path.join(tmp_path, "eigVecFile.txt")).read().split("\n")
+    assert ev_lines[2] == "Number of Ritz vectors: 2"
+    assert ev_lines[4] == "0 %.15e %.15e " % (ritz[0, 0], ritz[1, 0])
+    assert len([l for l in ev_lines[4:] if l.strip()]) == 7
