@@ -464,6 +464,11 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
       (rc = dalloc(&d.ukin, D, "kinetic work")) || (rc = dalloc(&d.v32, D, "FP32 Lanczos copy")))
     return bail(rc);
   d.red_blocks = 1216;
+  {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
+    d.pair_blocks = 3 * (sms > 0 ? sms : 152);  // 3 resident 256-thread blocks per SM (80 registers)
+  }
   // one partial per block of the widest reducing launch (the per-point potential apply)
   const size_t nparts = std::max((size_t)d.red_blocks, (N + 63) / 64) + 64;
   if ((rc = dalloc(&d.partials, nparts, "reduction scratch")) ||

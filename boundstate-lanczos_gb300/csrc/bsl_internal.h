@@ -101,6 +101,7 @@ struct DeviceState {
   double* ritz = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int red_blocks = 0;
+  int pair_blocks = 0;  // grid of the double-float update: a few resident blocks per SM
 };
 
 }  // namespace bsl

@@ -715,7 +715,7 @@ int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s) {
 int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaStream_t s) {
   DeviceState& d = h->d;
   if (h->state_pairs == 1)
-    k_update_pair<<<d.red_blocks, kThreads, 0, s>>>(
+    k_update_pair<<<d.pair_blocks, kThreads, 0, s>>>(
         reinterpret_cast<const float2*>(V), reinterpret_cast<float2*>(R), L,
         h->kinetic_engine == BSL_KIN_TENSOR ? nullptr : d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
         d.hist_cap, j, d.status);

@@ -122,7 +122,11 @@ __device__ __forceinline__ void issue_products(uint32_t d, uint32_t a, uint32_t 
 }
 
 // the four class accumulators of 8 consecutive columns combined into
-// double-float pairs and multiplied by `scale` (a power of two)
+// double-float pairs and multiplied by `scale` (a power of two).  The classes
+// are exact integers below 2^24: the head is c0 + 2^-9 c1 with its rounding
+// error, the tail collects that error and the two smaller classes (its own
+// rounding is ~2^-33 of the head); the pair is left unnormalised (|lo| may
+// slightly exceed half an ulp of hi), which the double-float additions accept.
 __device__ __forceinline__ void load_pairs8(uint32_t taddr, float scale, float2 (&out)[8]) {
   float c0[8], c1[8], c2[8], c3[8];
   tc::tmem_ld8_nowait(taddr, c0);
@@ -132,11 +136,9 @@ __device__ __forceinline__ void load_pairs8(uint32_t taddr, float scale, float2 
   tc::tmem_wait_ld();
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
-    float h, e1, e2, l;
-    two_sum(c0[u], __fmul_rn(c1[u], 0x1p-9f), h, e1);
-    two_sum(h, __fmul_rn(c2[u], 0x1p-18f), h, e2);
-    l = __fadd_rn(__fadd_rn(e1, e2), __fmul_rn(c3[u], 0x1p-27f));
-    fast_two_sum(h, l, h, l);
+    float h, e;
+    two_sum(c0[u], __fmul_rn(c1[u], 0x1p-9f), h, e);
+    const float l = __fmaf_rn(c3[u], 0x1p-27f, __fmaf_rn(c2[u], 0x1p-18f, e));
     out[u] = make_float2(__fmul_rn(h, scale), __fmul_rn(l, scale));
   }
 }
