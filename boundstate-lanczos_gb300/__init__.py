@@ -49,7 +49,7 @@ class HvParams(C.Structure):
                 ("simulation_title", C.c_char * 256), ("ceiling_potential", C.c_double),
                 ("quadrature_study", C.c_int), ("symmetry", C.c_int), ("potential", C.c_int),
                 ("iso_mass", C.c_double), ("iso_frequency", C.c_double), ("iso_ceiling", C.c_double),
-                ("precision", C.c_int), ("device", C.c_int)]
+                ("precision", C.c_int), ("device", C.c_int), ("keep_potential_grid", C.c_int)]
 
 
 _lib = None
@@ -80,6 +80,8 @@ def lib():
     L.bsl_set_kinetic_engine.argtypes = [C.c_void_p, C.c_int]
     L.bsl_kinetic_engine.argtypes = [C.c_void_p]
     L.bsl_lanczos_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong, _P, _P, _P]
+    L.bsl_lanczos_run_batch.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_ulonglong,
+                                        C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]
     L.bsl_lanczos_step_host.argtypes = [C.c_void_p, _P, _P, _P, _P, _P]
     L.bsl_good_eigenvalues.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_int)]
     L.bsl_good_eigenvalues_unit.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, _P, _P,
@@ -87,6 +89,11 @@ def lib():
     L.bsl_write_boundstates.argtypes = [C.c_char_p, C.c_char_p, C.c_int, _P, _P]
     L.bsl_write_tm_vectors.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, _P]
     L.bsl_write_ritz_vectors.argtypes = [C.c_char_p, C.c_char_p, C.c_longlong, C.c_int, _P]
+    L.bsl_ritz_vectors_start.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong, _P, C.c_int, _P]
+    L.bsl_hv_prep_cage.argtypes = [C.POINTER(HvParams), C.c_int, _P, _P, _P, _P, C.POINTER(C.c_void_p)]
+    L.bsl_hf_gradient.argtypes = [C.c_void_p, C.c_int, _P, _P, _P, _P]
+    L.bsl_rigid_body_gradient.argtypes = [C.c_int, _P, _P, C.c_int, _P, _P, _P]
+    L.bsl_cage_sites.argtypes = [C.c_int, _P, _P, _P, _P, _P]
     L.bsl_tm_eigenvectors.argtypes = [C.c_int, _P, _P, _P, _P, C.c_int, _P]
     L.bsl_ritz_vectors.argtypes = [C.c_void_p, C.c_int, _P, C.c_int, _P]
     L.bsl_last_run_ms_per_iter.argtypes = [C.c_void_p, _P]
@@ -142,6 +149,42 @@ def tm_eigenvectors(alpha, beta, beta2, evals):
     return out.reshape(ngood, niter)  # row n = column n of the column-major evtr
 
 
+def lanczos_batch(hamiltonians, niter, start="uniform", seed=0):
+    """Loop 1 for several prepared problems at once (bsl_lanczos_run_batch);
+    returns a list of (alpha, beta, beta2)."""
+    n = len(hamiltonians)
+    out = [(np.zeros(niter), np.zeros(niter + 1), np.zeros(niter + 1)) for _ in range(n)]
+    hs = (C.c_void_p * n)(*[h.handle for h in hamiltonians])
+    arr = [(_P * n)(*[_ptr(o[k]) for o in out]) for k in range(3)]
+    _check(lib().bsl_lanczos_run_batch(hs, n, niter, START[start], seed, arr[0], arr[1], arr[2]))
+    return out
+
+
+def _f64(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+def cage_sites(cm_ang, euler, q_site=None):
+    """Site positions (nm, [3 nmol, 3]) and charges of rigid SPC/E waters."""
+    cm, ea = _f64(cm_ang).reshape(-1, 3), _f64(euler).reshape(-1, 3)
+    n = cm.shape[0]
+    xyz, q = np.zeros((3 * n, 3)), np.zeros(3 * n)
+    qs = None if q_site is None else _f64(q_site)
+    _check(lib().bsl_cage_sites(n, _ptr(cm), _ptr(ea), None if qs is None else _ptr(qs), _ptr(xyz), _ptr(q)))
+    return xyz, q
+
+
+def rigid_body_gradient(cm_ang, euler, dr_site):
+    """Chain rule dE/dr_site [nlev, 3 nmol, 3] -> (dE/dcm [nlev, nmol, 3] per Angstrom, dE/deuler)."""
+    cm, ea = _f64(cm_ang).reshape(-1, 3), _f64(euler).reshape(-1, 3)
+    n = cm.shape[0]
+    dr = _f64(dr_site).reshape(-1, 3 * n, 3)
+    nlev = dr.shape[0]
+    dcm, dea = np.zeros((nlev, n, 3)), np.zeros((nlev, n, 3))
+    _check(lib().bsl_rigid_body_gradient(n, _ptr(cm), _ptr(ea), nlev, _ptr(dr), _ptr(dcm), _ptr(dea)))
+    return dcm, dea
+
+
 def write_boundstates(directory, sim_descr, evals, errs):
     """boundstates.txt and states_zpe.txt in the reference's format."""
     evals, errs = (np.ascontiguousarray(x, dtype=np.float64) for x in (evals, errs))
@@ -183,6 +226,41 @@ class Hamiltonian:
         self.basis_size = L.bsl_basis_size(h)
         self.packed_size = L.bsl_packed_size(h)
         self.nn = L.bsl_packed_nn(h)
+
+    @classmethod
+    def from_cage(cls, params, cm_ang, euler, q_site=None, q_alavi=None, precision="fp64", device=0,
+                  keep_potential_grid=True):
+        """HvPrep for an Alavi SPC/E cage given as arrays (bsl_hv_prep_cage)."""
+        self = cls.__new__(cls)
+        L = lib()
+        p = HvParams()
+        C.pointer(p)[0] = params
+        p.potential = POT_ALAVI_SPCE
+        p.precision = PREC[precision]
+        p.device = device
+        p.keep_potential_grid = 1 if keep_potential_grid else 0
+        cm, ea = _f64(cm_ang).reshape(-1), _f64(euler).reshape(-1)
+        qs = None if q_site is None else _f64(q_site)
+        qa = None if q_alavi is None else _f64(q_alavi)
+        h = C.c_void_p()
+        self._h = None
+        _check(L.bsl_hv_prep_cage(C.byref(p), len(cm) // 3, _ptr(cm), _ptr(ea), None if qs is None else _ptr(qs),
+                                  None if qa is None else _ptr(qa), C.byref(h)))
+        self.params = p
+        self._h = h
+        self.basis_size = L.bsl_basis_size(h)
+        self.packed_size = L.bsl_packed_size(h)
+        self.nn = L.bsl_packed_nn(h)
+        return self
+
+    def hf_gradient(self, psi, natoms):
+        """Hellmann-Feynman derivatives of the levels of eigenvectors psi [nlev, basis_size]:
+        (dE/dq_site [nlev, natoms], dE/dr_site [nlev, natoms, 3], dE/dq_alavi [nlev, 2])."""
+        ps = _f64(psi).reshape(-1, self.basis_size)
+        nlev = ps.shape[0]
+        dq, dr, da = np.zeros((nlev, natoms)), np.zeros((nlev, natoms, 3)), np.zeros((nlev, 2))
+        _check(lib().bsl_hf_gradient(self._h, nlev, _ptr(ps), _ptr(dq), _ptr(dr), _ptr(da)))
+        return dq, dr, da
 
     def close(self):
         if self._h:
@@ -243,12 +321,16 @@ class Hamiltonian:
                                            C.cast(o + 16, _P)))
         return out[0], out[1], out[2]
 
-    def ritz(self, niter, evtr_rows):
-        """Ritz vectors (reference layout), evtr_rows[n] = T_m eigenvector n."""
+    def ritz(self, niter, evtr_rows, start=None, seed=0):
+        """Ritz vectors (reference layout), evtr_rows[n] = T_m eigenvector n; `start`
+        (and seed) as in the loop-1 run (default: the reference's uniform start)."""
         ng = evtr_rows.shape[0]
         ev = np.ascontiguousarray(evtr_rows, dtype=np.float64).reshape(-1)
         out = np.zeros(ng * self.basis_size)
-        _check(lib().bsl_ritz_vectors(self._h, niter, _ptr(ev), ng, _ptr(out)))
+        if start is None:
+            _check(lib().bsl_ritz_vectors(self._h, niter, _ptr(ev), ng, _ptr(out)))
+        else:
+            _check(lib().bsl_ritz_vectors_start(self._h, niter, START[start], seed, _ptr(ev), ng, _ptr(out)))
         return out.reshape(ng, self.basis_size)
 
     def vgrid(self):
@@ -291,3 +373,62 @@ def hv_interface_setup(calculator):
         storage.h.hv(vec, uec)
 
     return st, hv_prep, hv
+
+
+def read_cage_xyz(path):
+    """Molecules of a reference cage file: (centres of mass [nmol, 3] in Angstrom,
+    ZYZ Euler angles [nmol, 3]) (the reader of SPCE_AH2_EngRoutines.cpp:5-108)."""
+    with open(path) as f:
+        lines = f.read().split("\n")
+    nmol = int(lines[0].split()[0])
+    cm, ea = np.zeros((nmol, 3)), np.zeros((nmol, 3))
+    toks = " ".join(lines[2:]).split()
+    for m in range(nmol):
+        v = [float(x) for x in toks[7 * m + 1:7 * m + 7]]
+        cm[m] = v[0::2]
+        ea[m] = v[1::2]
+    return cm, ea
+
+
+def cage_levels_function():
+    """torch.autograd.Function: the lowest levels of H2 in an SPC/E cage as a
+    differentiable function of the cage (centres of mass [nmol, 3] in Angstrom,
+    Euler angles [nmol, 3], site charges [3 nmol], Alavi H2 charges [2]).
+    forward runs HvPrep, Lanczos loop 1, the eigen-tail, loop 2 (Ritz vectors)
+    and the Hellmann-Feynman derivatives on the GPU; backward contracts them."""
+    import torch
+
+    class CageLevels(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, cm, euler, q_site, q_alavi, setup):
+            precision = setup.get("precision", "fp64")
+            niter, nlev = setup["niter"], setup["nlev"]
+            cm_np, ea_np = cm.detach().cpu().double().numpy(), euler.detach().cpu().double().numpy()
+            h = Hamiltonian.from_cage(setup["params"], cm_np, ea_np, q_site.detach().cpu().double().numpy(),
+                                      q_alavi.detach().cpu().double().numpy(), precision=precision,
+                                      device=setup.get("device", 0))
+            try:
+                a, b, b2 = h.lanczos(niter, start="normal", seed=setup.get("seed", 0))
+                unit = MIXED_UNIT_ROUNDOFF if precision == "mixed" else None
+                ev, _ = good_eigenvalues(a, b, b2, setup.get("emin", -1e3), setup.get("emax", 1e3), unit)
+                if len(ev) < nlev:
+                    raise BslError(ERR_INPUT, "only %d good eigenvalues, %d requested" % (len(ev), nlev))
+                ev = ev[:nlev]
+                rows = tm_eigenvectors(a, b, b2, ev)
+                psi = h.ritz(niter, rows, start="normal", seed=setup.get("seed", 0))
+                dq, dr, da = h.hf_gradient(psi, 3 * cm_np.shape[0])
+            finally:
+                h.close()
+            dcm, dea = rigid_body_gradient(cm_np, ea_np, dr)
+            ctx.save_for_backward(torch.from_numpy(dcm), torch.from_numpy(dea), torch.from_numpy(dq),
+                                  torch.from_numpy(da))
+            return torch.from_numpy(np.ascontiguousarray(ev))
+
+        @staticmethod
+        def backward(ctx, gE):
+            dcm, dea, dq, da = ctx.saved_tensors
+            g = gE.to(torch.float64)
+            return (torch.einsum("n,nmk->mk", g, dcm), torch.einsum("n,nmk->mk", g, dea),
+                    torch.einsum("n,nw->w", g, dq), torch.einsum("n,na->a", g, da), None)
+
+    return CageLevels

@@ -221,6 +221,68 @@ int build_tables(const bsl_hv_params& p, Tables* t) {
   return BSL_OK;
 }
 
+namespace {
+// ZYZ rotation R(phi, theta, chi) and its derivatives with respect to each angle
+void zyz(const double* ea, double R[3][3], double dR[3][3][3]) {
+  const double cp = std::cos(ea[0]), sp = std::sin(ea[0]), ct = std::cos(ea[1]), st = std::sin(ea[1]),
+               cx = std::cos(ea[2]), sx = std::sin(ea[2]);
+  const double M[3][3] = {{(cp * ct * cx) - (sp * sx), (-1 * cp * ct * sx) - (sp * cx), cp * st},
+                          {(sp * ct * cx) + (cp * sx), (-1 * sp * ct * sx) + (cp * cx), sp * st},
+                          {-1 * st * cx, st * sx, ct}};
+  for (int r = 0; r < 3; ++r)
+    for (int k = 0; k < 3; ++k) R[r][k] = M[r][k];
+  if (!dR) return;
+  // d/dphi
+  const double Dp[3][3] = {{-sp * ct * cx - cp * sx, sp * ct * sx - cp * cx, -sp * st},
+                           {cp * ct * cx - sp * sx, -cp * ct * sx - sp * cx, cp * st},
+                           {0.0, 0.0, 0.0}};
+  // d/dtheta
+  const double Dt[3][3] = {{-cp * st * cx, cp * st * sx, cp * ct}, {-sp * st * cx, sp * st * sx, sp * ct},
+                           {-ct * cx, ct * sx, -st}};
+  // d/dchi
+  const double Dx[3][3] = {{-cp * ct * sx - sp * cx, -cp * ct * cx + sp * sx, 0.0},
+                           {-sp * ct * sx + cp * cx, -sp * ct * cx - cp * sx, 0.0},
+                           {st * sx, st * cx, 0.0}};
+  for (int r = 0; r < 3; ++r)
+    for (int k = 0; k < 3; ++k) {
+      dR[0][r][k] = Dp[r][k];
+      dR[1][r][k] = Dt[r][k];
+      dR[2][r][k] = Dx[r][k];
+    }
+}
+const double* body_site(int a) { return a == 0 ? kBodyO : (a == 1 ? kBodyH1 : kBodyH2); }
+}  // namespace
+
+void build_cage(int nmol, const double* cm_ang, const double* euler, const double* q_site, Cage* c) {
+  c->xyz.clear();
+  c->q.clear();
+  c->is_o.clear();
+  c->cm_ang.assign(cm_ang, cm_ang + 3 * (size_t)nmol);
+  c->euler.assign(euler, euler + 3 * (size_t)nmol);
+  const double qs[3] = {kQO, kQH, kQH};
+  for (int i = 0; i < nmol; ++i) {
+    double R[3][3];
+    zyz(euler + 3 * i, R, nullptr);
+    for (int a = 0; a < 3; ++a) {
+      const double* b = body_site(a);
+      for (int r = 0; r < 3; ++r) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s += R[r][k] * b[k];
+        c->xyz.push_back(s + kNmPerAngstrom * cm_ang[3 * i + r]);
+      }
+      c->q.push_back(q_site ? q_site[3 * i + a] : qs[a]);
+      c->is_o.push_back(a == 0 ? 1 : 0);
+    }
+  }
+}
+
+void site_angle_derivative(const Cage& c, int m, int a, int k, double* out) {
+  double R[3][3], dR[3][3][3];
+  zyz(&c.euler[3 * (size_t)m], R, dR);
+  const double* b = body_site(a);
+  for (int r = 0; r < 3; ++r) out[r] = dR[k][r][0] * b[0] + dR[k][r][1] * b[1] + dR[k][r][2] * b[2];
+}
+
 int read_cage(const std::string& path, Cage* c) {
   std::ifstream f(path);
   if (!f.is_open()) return fail(BSL_ERR_INPUT, "Atom geometry file '" + path + "' could not be opened.");
@@ -229,32 +291,14 @@ int read_cage(const std::string& path, Cage* c) {
   if (!(f >> nmol) || nmol <= 0) return fail(BSL_ERR_INPUT, "geometry file '" + path + "': bad molecule count");
   std::getline(f, line);
   std::getline(f, line);
-  c->xyz.clear();
-  c->q.clear();
-  c->is_o.clear();
+  std::vector<double> cm(3 * (size_t)nmol), ea(3 * (size_t)nmol);
   for (int i = 0; i < nmol; ++i) {
     std::string name;
-    double cm[3], ea[3];
-    if (!(f >> name >> cm[0] >> ea[0] >> cm[1] >> ea[1] >> cm[2] >> ea[2]))
+    if (!(f >> name >> cm[3 * i] >> ea[3 * i] >> cm[3 * i + 1] >> ea[3 * i + 1] >> cm[3 * i + 2] >> ea[3 * i + 2]))
       return fail(BSL_ERR_INPUT, "geometry file '" + path + "': expected " + std::to_string(nmol) +
                                      " molecules, read " + std::to_string(i));
-    const double cp = std::cos(ea[0]), sp = std::sin(ea[0]), ct = std::cos(ea[1]), st = std::sin(ea[1]),
-                 cx = std::cos(ea[2]), sx = std::sin(ea[2]);
-    const double R[3][3] = {{(cp * ct * cx) - (sp * sx), (-1 * cp * ct * sx) - (sp * cx), cp * st},
-                            {(sp * ct * cx) + (cp * sx), (-1 * sp * ct * sx) + (cp * cx), sp * st},
-                            {-1 * st * cx, st * sx, ct}};
-    const double* body[3] = {kBodyO, kBodyH1, kBodyH2};
-    const double qs[3] = {kQO, kQH, kQH};
-    for (int a = 0; a < 3; ++a) {
-      for (int r = 0; r < 3; ++r) {
-        double s = 0.0;
-        for (int k = 0; k < 3; ++k) s += R[r][k] * body[a][k];
-        c->xyz.push_back(s + kNmPerAngstrom * cm[r]);
-      }
-      c->q.push_back(qs[a]);
-      c->is_o.push_back(a == 0 ? 1 : 0);
-    }
   }
+  build_cage(nmol, cm.data(), ea.data(), nullptr, c);
   return BSL_OK;
 }
 
@@ -314,6 +358,110 @@ int validate(const bsl_hv_params& p) {
 }
 
 }  // namespace
+// HvPrep with the cage either from the geometry file (cage == null) or given
+int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
+  if (!params || !out) return fail(BSL_ERR_INPUT, "null argument");
+  *out = nullptr;
+  int rc = validate(*params);
+  if (rc) return rc;
+  bsl_handle* h = new bsl_handle();
+  h->p = *params;
+  h->precision = params->precision;
+  rc = build_tables(h->p, &h->t);
+  if (rc) { delete h; return rc; }
+  if (h->t.nn > kMaxNN) {
+    delete h;
+    return fail(BSL_ERR_UNSUPPORTED, "symmetry block with " + std::to_string(h->t.nn) + " (l,m) functions exceeds " +
+                                         std::to_string(kMaxNN));
+  }
+  if (h->p.potential == BSL_POT_ALAVI_SPCE) {
+    if (cage) {
+      h->cage = *cage;
+    } else {
+      rc = read_cage(h->p.geometry_filename, &h->cage);
+      if (rc) { delete h; return rc; }
+    }
+  }
+  auto bail = [&](int code) {
+    free_device(h->d);
+    delete h;
+    return code;
+  };
+  cudaError_t e = cudaSetDevice(h->p.device);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaSetDevice"));
+  DeviceState& d = h->d;
+  if ((e = cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaStreamCreate"));
+  if ((e = cudaEventCreate(&d.ev0)) != cudaSuccess || (e = cudaEventCreate(&d.ev1)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaEventCreate"));
+  const Tables& t = h->t;
+  std::vector<float> hi, lo;
+  if ((rc = upload(&d.tx, t.tx, "Tx")) || (rc = upload(&d.ty, t.ty, "Ty")) || (rc = upload(&d.tz, t.tz, "Tz")))
+    return bail(rc);
+  kinetic_split_tables(t.tx, t.nx, true, &hi, &lo);
+  if ((rc = upload(&d.kx_head, hi, "Tx")) || (rc = upload(&d.kx_band, lo, "Tx"))) return bail(rc);
+  kinetic_split_tables(t.ty, t.ny, false, &hi, &lo);
+  if ((rc = upload(&d.ky_head, hi, "Ty")) || (rc = upload(&d.ky_band, lo, "Ty"))) return bail(rc);
+  kinetic_split_tables(t.tz, t.nz, false, &hi, &lo);
+  if ((rc = upload(&d.kz_head, hi, "Tz")) || (rc = upload(&d.kz_band, lo, "Tz"))) return bail(rc);
+  if (kinetic_tc_supported(t)) {
+    std::vector<uint16_t> sl;
+    kinetic_f16_slices(t.tx, t.nx, &sl, &d.e_txy);
+    if ((rc = upload(&d.kxy_slices, sl, "Tx"))) return bail(rc);
+    kinetic_f16_slices(t.tz, t.nz, &sl, &d.e_tz);
+    if ((rc = upload(&d.kz_slices, sl, "Tz"))) return bail(rc);
+    h->kinetic_engine = BSL_KIN_TENSOR;
+  }
+  if ((rc = upload(&d.rot, t.rot, "rotor"))) return bail(rc);
+  {
+    std::vector<float> rh(t.rot.size()), rl(t.rot.size());
+    for (size_t i = 0; i < t.rot.size(); ++i) {
+      rh[i] = (float)t.rot[i];
+      rl[i] = (float)(t.rot[i] - (double)rh[i]);
+    }
+    if ((rc = upload(&d.rot_hi, rh, "rotor")) || (rc = upload(&d.rot_lo, rl, "rotor"))) return bail(rc);
+  }
+  if ((rc = upload(&d.full_of, t.full_of, "index map"))) return bail(rc);
+  const size_t N = (size_t)t.npts, D = N * t.nn;
+  const size_t ngrid = N * t.na * t.nb;
+  const size_t ntri = (size_t)t.nn * (t.nn + 1) / 2;
+  const size_t tp = (size_t)vstream_tile_points(), tiled = (N + tp - 1) / tp * tp;
+  if ((rc = dalloc(&d.v1, ngrid, "potential grid")) || (rc = dalloc(&d.v2, ngrid, "potential grid")) ||
+      (rc = dalloc(&d.vb64, ntri * N, "potential blocks")) || (rc = dalloc(&d.vb32, ntri * tiled, "potential blocks")) ||
+      (rc = dalloc(&d.vec, D + 1, "Lanczos vector")) || (rc = dalloc(&d.rvec, D + 1, "Lanczos vector")) ||
+      (rc = dalloc(&d.ukin, D, "kinetic work")) || (rc = dalloc(&d.v32, D, "FP32 Lanczos copy")))
+    return bail(rc);
+  d.red_blocks = 1216;
+  {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
+    d.pair_blocks = 3 * (sms > 0 ? sms : 152);  // 3 resident 256-thread blocks per SM (80 registers)
+  }
+  // one partial per block of the widest reducing launch (the per-point potential apply)
+  const size_t nparts = std::max((size_t)d.red_blocks, (N + 63) / 64) + 64;
+  if ((rc = dalloc(&d.partials, nparts, "reduction scratch")) ||
+      (rc = dalloc(&d.counter, 4, "reduction counter")) || (rc = dalloc(&d.scalars, 16, "scalars")) ||
+      (rc = dalloc(&d.status, 4, "status")))
+    return bail(rc);
+  if ((e = cudaMemset(d.counter, 0, 4 * sizeof(unsigned int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
+  if ((e = cudaMemset(d.status, 0, 4 * sizeof(int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
+  // zero the padding points of the last tile of the streamed FP32 blocks
+  if ((e = cudaMemset(d.vb32, 0, ntri * tiled * sizeof(float))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
+  rc = (h->p.potential == BSL_POT_ALAVI_SPCE) ? dev_potential_alavi(h) : dev_potential_iso(h);
+  if (rc) return bail(rc);
+  if ((rc = dev_vblocks(h))) return bail(rc);
+  if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return bail(cuda_fail(e, "HvPrep"));
+  // the potential grid is only needed to build the blocks; keep it for
+  // inspection (bsl_copy_vgrid) when it is small
+  if (ngrid > ((size_t)1 << 26) && !h->p.keep_potential_grid) {
+    cudaFree(d.v1);
+    cudaFree(d.v2);
+    d.v1 = d.v2 = nullptr;
+  }
+  *out = h;
+  return BSL_OK;
+}
+
 }  // namespace bsl
 
 using namespace bsl;
@@ -395,103 +543,54 @@ int bsl_calculator_potential(const char* calculator, int* potential) {
   return fail(BSL_ERR_INPUT, "HvCalculator '" + c + "' not recognized.");
 }
 
-int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) {
-  if (!params || !out) return fail(BSL_ERR_INPUT, "null argument");
-  *out = nullptr;
-  int rc = validate(*params);
-  if (rc) return rc;
-  bsl_handle* h = new bsl_handle();
-  h->p = *params;
-  h->precision = params->precision;
-  rc = build_tables(h->p, &h->t);
-  if (rc) { delete h; return rc; }
-  if (h->t.nn > kMaxNN) {
-    delete h;
-    return fail(BSL_ERR_UNSUPPORTED, "symmetry block with " + std::to_string(h->t.nn) + " (l,m) functions exceeds " +
-                                         std::to_string(kMaxNN));
-  }
-  if (h->p.potential == BSL_POT_ALAVI_SPCE) {
-    rc = read_cage(h->p.geometry_filename, &h->cage);
-    if (rc) { delete h; return rc; }
-  }
-  auto bail = [&](int code) {
-    free_device(h->d);
-    delete h;
-    return code;
-  };
-  cudaError_t e = cudaSetDevice(h->p.device);
-  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaSetDevice"));
-  DeviceState& d = h->d;
-  if ((e = cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking)) != cudaSuccess)
-    return bail(cuda_fail(e, "cudaStreamCreate"));
-  if ((e = cudaEventCreate(&d.ev0)) != cudaSuccess || (e = cudaEventCreate(&d.ev1)) != cudaSuccess)
-    return bail(cuda_fail(e, "cudaEventCreate"));
-  const Tables& t = h->t;
-  std::vector<float> hi, lo;
-  if ((rc = upload(&d.tx, t.tx, "Tx")) || (rc = upload(&d.ty, t.ty, "Ty")) || (rc = upload(&d.tz, t.tz, "Tz")))
-    return bail(rc);
-  kinetic_split_tables(t.tx, t.nx, true, &hi, &lo);
-  if ((rc = upload(&d.kx_head, hi, "Tx")) || (rc = upload(&d.kx_band, lo, "Tx"))) return bail(rc);
-  kinetic_split_tables(t.ty, t.ny, false, &hi, &lo);
-  if ((rc = upload(&d.ky_head, hi, "Ty")) || (rc = upload(&d.ky_band, lo, "Ty"))) return bail(rc);
-  kinetic_split_tables(t.tz, t.nz, false, &hi, &lo);
-  if ((rc = upload(&d.kz_head, hi, "Tz")) || (rc = upload(&d.kz_band, lo, "Tz"))) return bail(rc);
-  if (kinetic_tc_supported(t)) {
-    std::vector<uint16_t> sl;
-    kinetic_f16_slices(t.tx, t.nx, &sl, &d.e_txy);
-    if ((rc = upload(&d.kxy_slices, sl, "Tx"))) return bail(rc);
-    kinetic_f16_slices(t.tz, t.nz, &sl, &d.e_tz);
-    if ((rc = upload(&d.kz_slices, sl, "Tz"))) return bail(rc);
-    h->kinetic_engine = BSL_KIN_TENSOR;
-  }
-  if ((rc = upload(&d.rot, t.rot, "rotor"))) return bail(rc);
-  {
-    std::vector<float> rh(t.rot.size()), rl(t.rot.size());
-    for (size_t i = 0; i < t.rot.size(); ++i) {
-      rh[i] = (float)t.rot[i];
-      rl[i] = (float)(t.rot[i] - (double)rh[i]);
-    }
-    if ((rc = upload(&d.rot_hi, rh, "rotor")) || (rc = upload(&d.rot_lo, rl, "rotor"))) return bail(rc);
-  }
-  if ((rc = upload(&d.full_of, t.full_of, "index map"))) return bail(rc);
-  const size_t N = (size_t)t.npts, D = N * t.nn;
-  const size_t ngrid = N * t.na * t.nb;
-  const size_t ntri = (size_t)t.nn * (t.nn + 1) / 2;
-  const size_t tp = (size_t)vstream_tile_points(), tiled = (N + tp - 1) / tp * tp;
-  if ((rc = dalloc(&d.v1, ngrid, "potential grid")) || (rc = dalloc(&d.v2, ngrid, "potential grid")) ||
-      (rc = dalloc(&d.vb64, ntri * N, "potential blocks")) || (rc = dalloc(&d.vb32, ntri * tiled, "potential blocks")) ||
-      (rc = dalloc(&d.vec, D + 1, "Lanczos vector")) || (rc = dalloc(&d.rvec, D + 1, "Lanczos vector")) ||
-      (rc = dalloc(&d.ukin, D, "kinetic work")) || (rc = dalloc(&d.v32, D, "FP32 Lanczos copy")))
-    return bail(rc);
-  d.red_blocks = 1216;
-  {
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
-    d.pair_blocks = 3 * (sms > 0 ? sms : 152);  // 3 resident 256-thread blocks per SM (80 registers)
-  }
-  // one partial per block of the widest reducing launch (the per-point potential apply)
-  const size_t nparts = std::max((size_t)d.red_blocks, (N + 63) / 64) + 64;
-  if ((rc = dalloc(&d.partials, nparts, "reduction scratch")) ||
-      (rc = dalloc(&d.counter, 4, "reduction counter")) || (rc = dalloc(&d.scalars, 16, "scalars")) ||
-      (rc = dalloc(&d.status, 4, "status")))
-    return bail(rc);
-  if ((e = cudaMemset(d.counter, 0, 4 * sizeof(unsigned int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
-  if ((e = cudaMemset(d.status, 0, 4 * sizeof(int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
-  // zero the padding points of the last tile of the streamed FP32 blocks
-  if ((e = cudaMemset(d.vb32, 0, ntri * tiled * sizeof(float))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
-  rc = (h->p.potential == BSL_POT_ALAVI_SPCE) ? dev_potential_alavi(h) : dev_potential_iso(h);
-  if (rc) return bail(rc);
-  if ((rc = dev_vblocks(h))) return bail(rc);
-  if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return bail(cuda_fail(e, "HvPrep"));
-  // the potential grid is only needed to build the blocks; keep it for
-  // inspection (bsl_copy_vgrid) when it is small
-  if (ngrid > ((size_t)1 << 26)) {
-    cudaFree(d.v1);
-    cudaFree(d.v2);
-    d.v1 = d.v2 = nullptr;
-  }
-  *out = h;
+int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) { return hv_prep(params, nullptr, out); }
+
+int bsl_cage_sites(int nmol, const double* cm_ang, const double* euler, const double* q_site, double* xyz, double* q) {
+  if (nmol < 1 || !cm_ang || !euler || !xyz || !q) return fail(BSL_ERR_INPUT, "bad arguments");
+  Cage c;
+  build_cage(nmol, cm_ang, euler, q_site, &c);
+  std::copy(c.xyz.begin(), c.xyz.end(), xyz);
+  std::copy(c.q.begin(), c.q.end(), q);
   return BSL_OK;
+}
+
+int bsl_rigid_body_gradient(int nmol, const double* cm_ang, const double* euler, int nlev, const double* dr_site,
+                            double* d_cm, double* d_euler) {
+  if (nmol < 1 || nlev < 1 || !cm_ang || !euler || !dr_site || !d_cm || !d_euler)
+    return fail(BSL_ERR_INPUT, "bad arguments");
+  Cage c;
+  build_cage(nmol, cm_ang, euler, nullptr, &c);
+  for (int n = 0; n < nlev; ++n)
+    for (int m = 0; m < nmol; ++m) {
+      double gc[3] = {0, 0, 0}, ge[3] = {0, 0, 0};
+      for (int a = 0; a < 3; ++a) {
+        const double* g = dr_site + ((size_t)n * 3 * nmol + 3 * m + a) * 3;
+        for (int k = 0; k < 3; ++k) gc[k] += kNmPerAngstrom * g[k];  // site = R body + 0.1 cm
+        for (int k = 0; k < 3; ++k) {
+          double dsite[3];
+          site_angle_derivative(c, m, a, k, dsite);
+          ge[k] += g[0] * dsite[0] + g[1] * dsite[1] + g[2] * dsite[2];
+        }
+      }
+      for (int k = 0; k < 3; ++k) {
+        d_cm[((size_t)n * nmol + m) * 3 + k] = gc[k];
+        d_euler[((size_t)n * nmol + m) * 3 + k] = ge[k];
+      }
+    }
+  return BSL_OK;
+}
+
+int bsl_hv_prep_cage(const bsl_hv_params* params, int nmol, const double* cm_ang, const double* euler,
+                     const double* q_site, const double* q_alavi, bsl_handle** out) {
+  if (!params || !out || nmol < 1 || !cm_ang || !euler) return fail(BSL_ERR_INPUT, "bad arguments");
+  if (params->potential != BSL_POT_ALAVI_SPCE) return fail(BSL_ERR_INPUT, "a cage needs the Alavi SPC/E potential");
+  Cage c;
+  build_cage(nmol, cm_ang, euler, q_site, &c);
+  if (q_alavi) {
+    c.q_h2_h = q_alavi[0];
+    c.q_h2_cm = q_alavi[1];
+  }
+  return hv_prep(params, &c, out);
 }
 
 void bsl_destroy(bsl_handle* h) {

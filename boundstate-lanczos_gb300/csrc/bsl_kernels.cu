@@ -37,9 +37,9 @@ struct AtomSet {
   const double* q;
   const int* is_o;
   int n;
+  double q_h, q_cm;   // Alavi H2 charges: each H, centre of mass
 };
 
-constexpr double kQ_H2_H = 0.4932, kQ_H2_CM = -0.9864;   // Alavi_Parameters.h:5-6
 constexpr double kA_LJ = 1.364e-06, kB_LJ = 1.533e-3;    // SPCE_AH2_EngRoutines.h:37-38
 constexpr int kMaxAtoms = 512;
 
@@ -75,7 +75,7 @@ __global__ void k_potential_cm(AtomSet atoms, const double* xg, const double* yg
   if (p >= npts) return;
   const int i = (int)(p % nx), j = (int)((p / nx) % ny), k = (int)(p / ((long long)nx * ny));
   const double x = xg[i], y = yg[j], z = zg[k];
-  double e = coulomb(sxyz, sq, atoms.n, kQ_H2_CM, x, y, z);
+  double e = coulomb(sxyz, sq, atoms.n, atoms.q_cm, x, y, z);
   double lj = 0.0;
   for (int a = 0; a < atoms.n; ++a) {
     if (!so[a]) continue;
@@ -108,8 +108,8 @@ __global__ void k_potential_alavi(AtomSet atoms, const double* xg, const double*
 #pragma unroll
   for (int half = 0; half < 2; ++half) {
     const double hyh = half ? -1.0 * hy : hy;
-    double v = coulomb(sxyz, sq, atoms.n, kQ_H2_H, __dadd_rn(x, hx), __dadd_rn(y, hyh), __dadd_rn(z, hz));
-    v = __dadd_rn(v, coulomb(sxyz, sq, atoms.n, kQ_H2_H, __dsub_rn(x, hx), __dsub_rn(y, hyh), __dsub_rn(z, hz)));
+    double v = coulomb(sxyz, sq, atoms.n, atoms.q_h, __dadd_rn(x, hx), __dadd_rn(y, hyh), __dadd_rn(z, hz));
+    v = __dadd_rn(v, coulomb(sxyz, sq, atoms.n, atoms.q_h, __dsub_rn(x, hx), __dsub_rn(y, hyh), __dsub_rn(z, hz)));
     v = __dadd_rn(v, c);
     if (v >= ceiling) v = ceiling;
     (half ? v2 : v1)[t] = v;
@@ -598,7 +598,7 @@ int dev_potential_alavi(bsl_handle* h) {
     cleanup();
     return cuda_fail(e, "potential upload");
   }
-  AtomSet atoms{dxyz, dq, dis_o, natoms};
+  AtomSet atoms{dxyz, dq, dis_o, natoms, h->cage.q_h2_h, h->cage.q_h2_cm};
   const long long N = t.npts;
   const int nab = t.na * t.nb;
   double* cm = d.ukin;  // scratch of >= N doubles

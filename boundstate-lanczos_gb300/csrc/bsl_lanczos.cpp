@@ -153,6 +153,45 @@ int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed
   return check_status(h);
 }
 
+int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned long long seed, double** alpha,
+                          double** beta, double** beta2) {
+  if (!hs || n < 1 || niter < 1 || !alpha || !beta || !beta2) return fail(BSL_ERR_INPUT, "bad arguments");
+  for (int b = 0; b < n; ++b) {
+    if (!hs[b] || !alpha[b] || !beta[b] || !beta2[b]) return fail(BSL_ERR_INPUT, "null handle or output in the batch");
+    for (int c = 0; c < b; ++c)
+      if (hs[c] == hs[b]) return fail(BSL_ERR_INPUT, "a handle appears twice in the batch");
+  }
+  int rc;
+  for (int b = 0; b < n; ++b) {
+    cudaSetDevice(hs[b]->p.device);
+    if ((rc = ensure_hist(hs[b], niter)) || (rc = init_state(hs[b], start, seed))) return rc;
+  }
+  // iteration j of every problem before iteration j + 1 of any: each problem
+  // runs on its own stream, so the kernels of different problems overlap
+  for (int j = 1; j <= niter; ++j)
+    for (int b = 0; b < n; ++b) {
+      cudaSetDevice(hs[b]->p.device);
+      if ((rc = dev_lanczos_iteration(hs[b], j, hs[b]->d.stream))) return rc;
+    }
+  for (int b = 0; b < n; ++b) {
+    bsl_handle* h = hs[b];
+    cudaSetDevice(h->p.device);
+    DeviceState& d = h->d;
+    BSL_CUDA(cudaStreamSynchronize(d.stream));
+    std::vector<double> hist(3 * (size_t)d.hist_cap);
+    BSL_CUDA(cudaMemcpy(hist.data(), d.hist, hist.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int j = 0; j < niter; ++j) alpha[b][j] = hist[j];
+    beta[b][0] = 0.0;
+    beta2[b][0] = 0.0;
+    for (int j = 1; j <= niter; ++j) {
+      beta[b][j] = hist[d.hist_cap + j];
+      beta2[b][j] = hist[2 * (size_t)d.hist_cap + j];
+    }
+    if ((rc = check_status(h))) return rc;
+  }
+  return BSL_OK;
+}
+
 int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alpha_j, double* beta_j,
                           double* beta2_j) {
   if (!h || !vec || !rvec) return fail(BSL_ERR_INPUT, "null argument");
@@ -184,12 +223,17 @@ int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alph
 }
 
 int bsl_ritz_vectors(bsl_handle* h, int niter, const double* evtr, int ngood, double* ritz) {
+  return bsl_ritz_vectors_start(h, niter, BSL_START_UNIFORM, 0, evtr, ngood, ritz);
+}
+
+int bsl_ritz_vectors_start(bsl_handle* h, int niter, int start, unsigned long long seed, const double* evtr, int ngood,
+                           double* ritz) {
   if (!h || niter < 1 || ngood < 1 || !evtr || !ritz) return fail(BSL_ERR_INPUT, "bad arguments");
   cudaSetDevice(h->p.device);
   DeviceState& d = h->d;
   const long long D = bsl_packed_size(h), Df = bsl_basis_size(h), L = D + 1;
   int rc;
-  if ((rc = ensure_hist(h, niter)) || (rc = init_state(h, BSL_START_UNIFORM, 0))) return rc;
+  if ((rc = ensure_hist(h, niter)) || (rc = init_state(h, start, seed))) return rc;
   // coefficient schedule with the reference's cumulative-norm cut-off
   std::vector<double> coef((size_t)niter * ngood);
   std::vector<int> active((size_t)niter * ngood);

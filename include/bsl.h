@@ -97,6 +97,9 @@ typedef struct bsl_hv_params {
   /* execution */
   int precision; /* BSL_PREC_* */
   int device;    /* CUDA device ordinal */
+  int keep_potential_grid; /* keep V(x,y,z,theta,phi) on the device after HvPrep
+                              (needed by bsl_hf_gradient; otherwise released when
+                              larger than 2^26 values) */
 } bsl_hv_params;
 
 typedef struct bsl_handle bsl_handle;
@@ -120,6 +123,15 @@ int bsl_calculator_potential(const char* calculator, int* potential);
 /* HvPrep: build grids, tables and the potential on the device.  Replaces
    Hv_Prep_linRotCartSph_NoQuad (linRotCartSphHvFullVPrepRoutines.cpp:798-805). */
 int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out);
+
+/* HvPrep with the cage given as arrays instead of the geometry file (for
+   parameter derivatives): nmol rigid SPC/E waters, centres of mass in
+   Angstrom cm_ang[3 nmol] and ZYZ Euler angles euler[3 nmol] in the file's
+   order (SPCE_AH2_EngRoutines.cpp:5-108); q_site[3 nmol] (O, H1, H2 per
+   molecule) replaces the SPC/E charges when not NULL, q_alavi[2] (each H,
+   centre of mass) the Alavi H2 charges when not NULL.  Alavi SPC/E only. */
+int bsl_hv_prep_cage(const bsl_hv_params* params, int nmol, const double* cm_ang, const double* euler,
+                     const double* q_site, const double* q_alavi, bsl_handle** out);
 
 void bsl_destroy(bsl_handle* h);
 
@@ -158,6 +170,16 @@ int bsl_hv_apply_device(bsl_handle* h, const double* d_v, double* d_u, void* str
    vanishes or alpha/beta stop being finite. */
 int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed, double* alpha, double* beta,
                     double* beta2);
+
+/* bsl_lanczos_run for n independent problems (different cages, symmetry
+   blocks or grids, each prepared by its own bsl_hv_prep) in one call: iteration
+   j of every problem is queued before iteration j + 1 of any, each problem on
+   its own stream, so the kernels of small problems that do not fill the GPU
+   overlap.  alpha[b], beta[b], beta2[b] as in bsl_lanczos_run for problem b;
+   the results are bit-identical to separate bsl_lanczos_run calls.  No
+   counterpart in the reference (one problem per process there). */
+int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned long long seed, double** alpha,
+                          double** beta, double** beta2);
 
 /* One iteration of the reference loop body (lanczosEigenValuesVectors.cpp:191-238)
    with the Lanczos state on the host in the reference layout: on return vec
@@ -229,6 +251,33 @@ int bsl_write_boundstates(const char* dir, const char* sim_descr, int ngood, con
 int bsl_write_tm_vectors(const char* dir, const char* sim_descr, int niter, int ngood, const double* evtr);
 int bsl_write_ritz_vectors(const char* dir, const char* sim_descr, long long basis_size, int ngood,
                            const double* ritz);
+
+/* Hellmann-Feynman derivatives dE_n/dtheta = <psi_n| dV/dtheta |psi_n> of nlev
+   levels with respect to the cage (Alavi SPC/E potential, the grid kept with
+   keep_potential_grid): psi[n * basis_size + row] eigenvectors in the reference
+   layout (any normalisation; e.g. from bsl_ritz_vectors); outputs
+   dq_site[n * natoms + w] (kJ/mol per e), dr_site[(n * natoms + w) * 3 + k]
+   (kJ/mol per nm), dq_alavi[2 n + {0, 1}] (the H and centre-of-mass charges of
+   H2).  Sites are O, H1, H2 per molecule in file order.  No counterpart in the
+   reference. */
+int bsl_hf_gradient(bsl_handle* h, int nlev, const double* psi, double* dq_site, double* dr_site,
+                    double* dq_alavi);
+
+/* Chain rule from site positions to the rigid-body coordinates of the cage
+   (centre of mass in Angstrom, ZYZ Euler angles in rad; SPCE_AH2_EngRoutines.cpp:5-108):
+   dr_site[(n * 3 nmol + site) * 3 + k] -> d_cm[(n * nmol + m) * 3 + k],
+   d_euler[(n * nmol + m) * 3 + k].  Host only. */
+int bsl_rigid_body_gradient(int nmol, const double* cm_ang, const double* euler, int nlev, const double* dr_site,
+                            double* d_cm, double* d_euler);
+
+/* Site positions (nm) and charges of a cage of rigid SPC/E waters: xyz[3 * 3 nmol],
+   q[3 nmol] (q_site NULL: the SPC/E charges).  Host only. */
+int bsl_cage_sites(int nmol, const double* cm_ang, const double* euler, const double* q_site, double* xyz, double* q);
+
+/* bsl_ritz_vectors from the start vector of a bsl_lanczos_run(start, seed)
+   (bsl_ritz_vectors itself restarts from BSL_START_UNIFORM, as the reference). */
+int bsl_ritz_vectors_start(bsl_handle* h, int niter, int start, unsigned long long seed, const double* evtr, int ngood,
+                           double* ritz);
 
 /* Timing of the last bsl_lanczos_run: average device milliseconds per
    iteration, measured with CUDA events on the library's stream. */

@@ -201,3 +201,39 @@ def test_lv_and_ritz_file_layout(bsl, tmp_path):
     assert ev_lines[2] == "Number of Ritz vectors: 2"
     assert ev_lines[4] == "0 %.15e %.15e " % (ritz[0, 0], ritz[1, 0])
     assert len([l for l in ev_lines[4:] if l.strip()]) == 7
+
+
+def test_rigid_body_chain_rule_matches_finite_differences(bsl):
+    """bsl_rigid_body_gradient: d(g . sites)/d(centre, angles) against central
+    differences of bsl_cage_sites (host only)."""
+    cm, ea = bsl.read_cage_xyz(os.path.join(case_info("seed1_n6_l3_odd")[0], "cage_seed1.xyz"))
+    rng = np.random.default_rng(2)
+    g = rng.standard_normal((2, 3 * cm.shape[0], 3))
+    dcm, dea = bsl.rigid_body_gradient(cm, ea, g)
+
+    def f(c, e, n):
+        return float(np.sum(g[n] * bsl.cage_sites(c, e)[0]))
+
+    h = 1e-6
+    for n in range(2):
+        for m, k in [(0, 0), (3, 1), (7, 2), (19, 0)]:
+            cp, cq = cm.copy(), cm.copy()
+            cp[m, k] += h
+            cq[m, k] -= h
+            assert (f(cp, ea, n) - f(cq, ea, n)) / (2 * h) == pytest.approx(dcm[n, m, k], rel=1e-6, abs=1e-9)
+            ep, eq = ea.copy(), ea.copy()
+            ep[m, k] += h
+            eq[m, k] -= h
+            assert (f(cm, ep, n) - f(cm, eq, n)) / (2 * h) == pytest.approx(dea[n, m, k], rel=1e-6, abs=1e-9)
+
+
+def test_cage_sites_charges(bsl):
+    cm, ea = bsl.read_cage_xyz(os.path.join(case_info("seed1_n6_l3_odd")[0], "cage_seed1.xyz"))
+    xyz, q = bsl.cage_sites(cm, ea)
+    assert xyz.shape == (60, 3) and np.allclose(q[:3], [-0.8476, 0.4238, 0.4238])
+    assert abs(q.sum()) < 1e-12
+    # the O-H distance of SPC/E (1 A) in every molecule
+    for m in range(20):
+        assert np.linalg.norm(xyz[3 * m + 1] - xyz[3 * m]) == pytest.approx(0.1, rel=1e-8)
+    qs = np.arange(60, dtype=float)
+    assert np.array_equal(bsl.cage_sites(cm, ea, qs)[1], qs)

@@ -266,3 +266,18 @@ def test_ritz_vectors_mixed_are_eigenvectors(bsl):
         keep[s * npts:(s + 1) * npts] = True
     assert np.linalg.norm(u[keep] - em * xm[keep]) <= 1e-4
     h.close()
+
+
+def test_lanczos_batch_matches_separate_runs(bsl):
+    """Three problems (two grids and symmetry blocks, both precisions' default
+    engines) in one batched call give bit-identical alpha/beta to separate runs."""
+    names = ["seed1_n6_l3_odd", "seed0_n5_l4_even", "cpu_workload"]
+    hs = [make(bsl, n)[0] for n in names]
+    hs[2].set_precision("mixed")
+    niter = 60
+    sep = [h.lanczos(niter, start="normal", seed=3) for h in hs]
+    bat = bsl.lanczos_batch(hs, niter, start="normal", seed=3)
+    for (a, b, b2), (ab, bb, b2b) in zip(sep, bat):
+        assert np.array_equal(a, ab) and np.array_equal(b, bb) and np.array_equal(b2, b2b)
+    for h in hs:
+        h.close()
