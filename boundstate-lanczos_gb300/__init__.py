@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(HERE, "libbsl_gb300.so")
 
 OK, ERR_INPUT, ERR_CUDA, ERR_STATE, ERR_BREAKDOWN, ERR_UNSUPPORTED, ERR_NOMEM = range(7)
 SYM = {"All": 0, "Even": 1, "Odd": 2}
-POT_ALAVI_SPCE, POT_ISOHARMOSC = 0, 1
+POT_ALAVI_SPCE, POT_ISOHARMOSC, POT_ALAVI_TIP4P = 0, 1, 2
 PREC = {"fp64": 0, "mixed": 1}
 START = {"uniform": 0, "normal": 1}
 KINETIC = {"simt": 0, "tensor": 1}
@@ -29,6 +29,8 @@ CALCULATORS = {
     "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE": POT_ALAVI_SPCE,
     "linRotCartSph_NoQuad_IsoHarmOsc": POT_ISOHARMOSC,
     "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE_GB300": POT_ALAVI_SPCE,
+    "linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P": POT_ALAVI_TIP4P,
+    "linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P_GB300": POT_ALAVI_TIP4P,
     "linRotCartSph_NoQuad_IsoHarmOsc_GB300": POT_ISOHARMOSC,
 }
 
@@ -92,8 +94,8 @@ def lib():
     L.bsl_ritz_vectors_start.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong, _P, C.c_int, _P]
     L.bsl_hv_prep_cage.argtypes = [C.POINTER(HvParams), C.c_int, _P, _P, _P, _P, C.POINTER(C.c_void_p)]
     L.bsl_hf_gradient.argtypes = [C.c_void_p, C.c_int, _P, _P, _P, _P]
-    L.bsl_rigid_body_gradient.argtypes = [C.c_int, _P, _P, C.c_int, _P, _P, _P]
-    L.bsl_cage_sites.argtypes = [C.c_int, _P, _P, _P, _P, _P]
+    L.bsl_rigid_body_gradient.argtypes = [C.c_int, C.c_int, _P, _P, C.c_int, _P, _P, _P]
+    L.bsl_cage_sites.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P]
     L.bsl_tm_eigenvectors.argtypes = [C.c_int, _P, _P, _P, _P, C.c_int, _P]
     L.bsl_ritz_vectors.argtypes = [C.c_void_p, C.c_int, _P, C.c_int, _P]
     L.bsl_last_run_ms_per_iter.argtypes = [C.c_void_p, _P]
@@ -164,24 +166,29 @@ def _f64(x):
     return np.ascontiguousarray(x, dtype=np.float64)
 
 
-def cage_sites(cm_ang, euler, q_site=None):
-    """Site positions (nm, [3 nmol, 3]) and charges of rigid SPC/E waters."""
+def sites_per_molecule(potential):
+    return 4 if potential == POT_ALAVI_TIP4P else 3
+
+
+def cage_sites(cm_ang, euler, q_site=None, potential=POT_ALAVI_SPCE):
+    """Site positions (nm, [S nmol, 3]) and charges of rigid SPC/E (S = 3) or TIP4P (S = 4) waters."""
     cm, ea = _f64(cm_ang).reshape(-1, 3), _f64(euler).reshape(-1, 3)
-    n = cm.shape[0]
-    xyz, q = np.zeros((3 * n, 3)), np.zeros(3 * n)
+    n, S = cm.shape[0], sites_per_molecule(potential)
+    xyz, q = np.zeros((S * n, 3)), np.zeros(S * n)
     qs = None if q_site is None else _f64(q_site)
-    _check(lib().bsl_cage_sites(n, _ptr(cm), _ptr(ea), None if qs is None else _ptr(qs), _ptr(xyz), _ptr(q)))
+    _check(lib().bsl_cage_sites(potential, n, _ptr(cm), _ptr(ea), None if qs is None else _ptr(qs), _ptr(xyz),
+                                _ptr(q)))
     return xyz, q
 
 
-def rigid_body_gradient(cm_ang, euler, dr_site):
-    """Chain rule dE/dr_site [nlev, 3 nmol, 3] -> (dE/dcm [nlev, nmol, 3] per Angstrom, dE/deuler)."""
+def rigid_body_gradient(cm_ang, euler, dr_site, potential=POT_ALAVI_SPCE):
+    """Chain rule dE/dr_site [nlev, S nmol, 3] -> (dE/dcm [nlev, nmol, 3] per Angstrom, dE/deuler)."""
     cm, ea = _f64(cm_ang).reshape(-1, 3), _f64(euler).reshape(-1, 3)
-    n = cm.shape[0]
-    dr = _f64(dr_site).reshape(-1, 3 * n, 3)
+    n, S = cm.shape[0], sites_per_molecule(potential)
+    dr = _f64(dr_site).reshape(-1, S * n, 3)
     nlev = dr.shape[0]
     dcm, dea = np.zeros((nlev, n, 3)), np.zeros((nlev, n, 3))
-    _check(lib().bsl_rigid_body_gradient(n, _ptr(cm), _ptr(ea), nlev, _ptr(dr), _ptr(dcm), _ptr(dea)))
+    _check(lib().bsl_rigid_body_gradient(potential, n, _ptr(cm), _ptr(ea), nlev, _ptr(dr), _ptr(dcm), _ptr(dea)))
     return dcm, dea
 
 
@@ -229,13 +236,13 @@ class Hamiltonian:
 
     @classmethod
     def from_cage(cls, params, cm_ang, euler, q_site=None, q_alavi=None, precision="fp64", device=0,
-                  keep_potential_grid=True):
-        """HvPrep for an Alavi SPC/E cage given as arrays (bsl_hv_prep_cage)."""
+                  keep_potential_grid=True, potential=POT_ALAVI_SPCE):
+        """HvPrep for an Alavi SPC/E or TIP4P cage given as arrays (bsl_hv_prep_cage)."""
         self = cls.__new__(cls)
         L = lib()
         p = HvParams()
         C.pointer(p)[0] = params
-        p.potential = POT_ALAVI_SPCE
+        p.potential = potential
         p.precision = PREC[precision]
         p.device = device
         p.keep_potential_grid = 1 if keep_potential_grid else 0
@@ -404,9 +411,10 @@ def cage_levels_function():
             precision = setup.get("precision", "fp64")
             niter, nlev = setup["niter"], setup["nlev"]
             cm_np, ea_np = cm.detach().cpu().double().numpy(), euler.detach().cpu().double().numpy()
+            pot = setup.get("potential", POT_ALAVI_SPCE)
             h = Hamiltonian.from_cage(setup["params"], cm_np, ea_np, q_site.detach().cpu().double().numpy(),
                                       q_alavi.detach().cpu().double().numpy(), precision=precision,
-                                      device=setup.get("device", 0))
+                                      device=setup.get("device", 0), potential=pot)
             try:
                 a, b, b2 = h.lanczos(niter, start="normal", seed=setup.get("seed", 0))
                 unit = MIXED_UNIT_ROUNDOFF if precision == "mixed" else None
@@ -416,10 +424,10 @@ def cage_levels_function():
                 ev = ev[:nlev]
                 rows = tm_eigenvectors(a, b, b2, ev)
                 psi = h.ritz(niter, rows, start="normal", seed=setup.get("seed", 0))
-                dq, dr, da = h.hf_gradient(psi, 3 * cm_np.shape[0])
+                dq, dr, da = h.hf_gradient(psi, sites_per_molecule(pot) * cm_np.shape[0])
             finally:
                 h.close()
-            dcm, dea = rigid_body_gradient(cm_np, ea_np, dr)
+            dcm, dea = rigid_body_gradient(cm_np, ea_np, dr, setup.get("potential", POT_ALAVI_SPCE))
             ctx.save_for_backward(torch.from_numpy(dcm), torch.from_numpy(dea), torch.from_numpy(dq),
                                   torch.from_numpy(da))
             return torch.from_numpy(np.ascontiguousarray(ev))

@@ -8,9 +8,9 @@
 //   psi(p, a, b, half) = sum_s psi_s(p) L_s(a) T^half_{m_s}(b)
 // (the quadrature of the potential blocks, ContinuousAngularGrid/
 // linRotCartSphHvContGridRoutines.cpp:7-152), with V the Alavi SPC/E potential
-// of Alavi_ContGrid_H2_Routines.cpp:6-147: the two H charges at p +- d u(a, b)
-// and the centre-of-mass charge at p interact with every site by Coulomb, the
-// centre of mass with every oxygen by Lennard-Jones, and V is clipped at the
+// of Alavi_ContGrid_H2_Routines.cpp:6-147 with SPC/E or TIP4P water: the two H
+// charges at p +- d u(a, b) and the centre-of-mass charge at p interact with
+// every site by Coulomb, the centre of mass with every oxygen by Lennard-Jones, and V is clipped at the
 // ceiling (no derivative where the ceiling applies).
 //
 // One CTA per grid point (persistent over points), one thread per site.  The
@@ -29,7 +29,6 @@ constexpr int kGThreads = 64;     // sites per pass
 constexpr int kChunk = 256;       // (a, b, half) nodes per chunk
 constexpr int kMaxLev = 8;        // levels per pass
 constexpr int kVals = 6;          // per (level, site): dE/dq, dE/dr (3), q_H part, q_CM part
-constexpr double kA_LJ = 1.364e-06, kB_LJ = 1.533e-3;  // SPCE_AH2_EngRoutines.h:37-38
 
 struct GradArgs {
   const float* psi;       // [lev][nn][N] packed eigenvectors (normalised), FP32
@@ -43,7 +42,7 @@ struct GradArgs {
   const int* is_o;
   int natoms, nx, ny, nn, na, nb, nlev;
   long long npts;
-  double ceiling, q_h, q_cm;
+  double ceiling, q_h, q_cm, lj_a, lj_b;
   double* part;           // [gridDim][nlev][natoms][kVals]
 };
 
@@ -162,7 +161,7 @@ __global__ void __launch_bounds__(kGThreads) k_hf_gradient(GradArgs g) {
         double f = kCoulombK * g.q_cm * qw * inv3;  // dV/dr_w = f (p - r_w)
         if (oxy) {
           const double i2 = inv * inv, i6 = i2 * i2 * i2, i8 = i6 * i2, i14 = i6 * i6 * i2;
-          f += 12.0 * kA_LJ * i14 - 6.0 * kB_LJ * i8;
+          f += 12.0 * g.lj_a * i14 - 6.0 * g.lj_b * i8;
         }
 #pragma unroll
         for (int n = 0; n < kMaxLev; ++n) {
@@ -203,7 +202,7 @@ using namespace bsl;
 extern "C" int bsl_hf_gradient(bsl_handle* h, int nlev, const double* psi, double* dq_site, double* dr_site,
                                double* dq_alavi) {
   if (!h || nlev < 1 || !psi || !dq_site || !dr_site || !dq_alavi) return fail(BSL_ERR_INPUT, "bad arguments");
-  if (h->p.potential != BSL_POT_ALAVI_SPCE) return fail(BSL_ERR_INPUT, "derivatives need the Alavi SPC/E potential");
+  if (h->p.potential == BSL_POT_ISOHARMOSC) return fail(BSL_ERR_INPUT, "derivatives need an Alavi potential");
   if (!h->d.v1) return fail(BSL_ERR_STATE, "the potential grid was released after HvPrep (keep_potential_grid = 0)");
   cudaSetDevice(h->p.device);
   const Tables& t = h->t;
@@ -285,7 +284,7 @@ extern "C" int bsl_hf_gradient(bsl_handle* h, int nlev, const double* psi, doubl
       return cuda_fail(e, "eigenvector upload");
     }
     GradArgs g{dpsi, dY, h->d.v1, h->d.v2, dh, dx, dy, dz, dxyz, dq, dio, natoms, t.nx, t.ny, nn, t.na, t.nb, L, N,
-               h->p.ceiling_potential, h->cage.q_h2_h, h->cage.q_h2_cm, dpart};
+               h->p.ceiling_potential, h->cage.q_h2_h, h->cage.q_h2_cm, h->cage.lj_a, h->cage.lj_b, dpart};
     k_hf_gradient<<<blocks, kGThreads>>>(g);
     const int count = L * natoms * kVals;
     k_hf_reduce<<<(count + 255) / 256, 256>>>(dpart, blocks, count, dout);

@@ -36,6 +36,13 @@ const double kBodyO[3] = {0.0, 0.0, 0.006461408220};
 const double kBodyH1[3] = {-8.164965810E-2, 0.0, -0.05127361870};
 const double kBodyH2[3] = {8.164965810E-2, 0.0, -0.05127361870};
 const double kQO = -0.8476, kQH = 0.4238;
+// TIP4P body frame (nm), charges and O-H2 Lennard-Jones, TIP4P_AH2_EngRoutines.h
+const double kT4O[3] = {0.0, 0.0, 0.00655538};
+const double kT4H1[3] = {-0.075695, 0.0, -0.0520326};
+const double kT4H2[3] = {0.075695, 0.0, -0.0520326};
+const double kT4M[3] = {0.0, 0.0, -0.00844462};
+const double kT4QH = 0.520, kT4QM = -1.040;
+const double kT4A = 1.362e-06, kT4B = 1.532e-3;
 
 double factorial(int n) {
   double f = 1.0;
@@ -250,27 +257,35 @@ void zyz(const double* ea, double R[3][3], double dR[3][3][3]) {
       dR[2][r][k] = Dx[r][k];
     }
 }
-const double* body_site(int a) { return a == 0 ? kBodyO : (a == 1 ? kBodyH1 : kBodyH2); }
+const double* body_site(int model, int a) {
+  if (model == BSL_POT_ALAVI_TIP4P) return a == 0 ? kT4O : (a == 1 ? kT4H1 : (a == 2 ? kT4H2 : kT4M));
+  return a == 0 ? kBodyO : (a == 1 ? kBodyH1 : kBodyH2);
+}
 }  // namespace
 
-void build_cage(int nmol, const double* cm_ang, const double* euler, const double* q_site, Cage* c) {
+void build_cage(int model, int nmol, const double* cm_ang, const double* euler, const double* q_site, Cage* c) {
+  const bool t4 = model == BSL_POT_ALAVI_TIP4P;
+  c->model = t4 ? BSL_POT_ALAVI_TIP4P : BSL_POT_ALAVI_SPCE;
+  c->sites = t4 ? 4 : 3;
+  c->lj_a = t4 ? kT4A : 1.364e-06;  // SPCE_AH2_EngRoutines.h:37-38
+  c->lj_b = t4 ? kT4B : 1.533e-3;
   c->xyz.clear();
   c->q.clear();
   c->is_o.clear();
   c->cm_ang.assign(cm_ang, cm_ang + 3 * (size_t)nmol);
   c->euler.assign(euler, euler + 3 * (size_t)nmol);
-  const double qs[3] = {kQO, kQH, kQH};
+  const double qs[4] = {t4 ? 0.0 : kQO, t4 ? kT4QH : kQH, t4 ? kT4QH : kQH, kT4QM};
   for (int i = 0; i < nmol; ++i) {
     double R[3][3];
     zyz(euler + 3 * i, R, nullptr);
-    for (int a = 0; a < 3; ++a) {
-      const double* b = body_site(a);
+    for (int a = 0; a < c->sites; ++a) {
+      const double* b = body_site(c->model, a);
       for (int r = 0; r < 3; ++r) {
         double s = 0.0;
         for (int k = 0; k < 3; ++k) s += R[r][k] * b[k];
         c->xyz.push_back(s + kNmPerAngstrom * cm_ang[3 * i + r]);
       }
-      c->q.push_back(q_site ? q_site[3 * i + a] : qs[a]);
+      c->q.push_back(q_site ? q_site[c->sites * i + a] : qs[a]);
       c->is_o.push_back(a == 0 ? 1 : 0);
     }
   }
@@ -279,11 +294,11 @@ void build_cage(int nmol, const double* cm_ang, const double* euler, const doubl
 void site_angle_derivative(const Cage& c, int m, int a, int k, double* out) {
   double R[3][3], dR[3][3][3];
   zyz(&c.euler[3 * (size_t)m], R, dR);
-  const double* b = body_site(a);
+  const double* b = body_site(c.model, a);
   for (int r = 0; r < 3; ++r) out[r] = dR[k][r][0] * b[0] + dR[k][r][1] * b[1] + dR[k][r][2] * b[2];
 }
 
-int read_cage(const std::string& path, Cage* c) {
+int read_cage(const std::string& path, int model, Cage* c) {
   std::ifstream f(path);
   if (!f.is_open()) return fail(BSL_ERR_INPUT, "Atom geometry file '" + path + "' could not be opened.");
   int nmol = 0;
@@ -298,7 +313,7 @@ int read_cage(const std::string& path, Cage* c) {
       return fail(BSL_ERR_INPUT, "geometry file '" + path + "': expected " + std::to_string(nmol) +
                                      " molecules, read " + std::to_string(i));
   }
-  build_cage(nmol, cm.data(), ea.data(), nullptr, c);
+  build_cage(model, nmol, cm.data(), ea.data(), nullptr, c);
   return BSL_OK;
 }
 
@@ -350,7 +365,7 @@ int validate(const bsl_hv_params& p) {
   if (p.symmetry < BSL_SYM_ALL || p.symmetry > BSL_SYM_ODD)
     return fail(BSL_ERR_INPUT, "ERROR: Symmeterizer Flag not recognized.");
   if (p.symmetry == BSL_SYM_ODD && p.l_max < 1) return fail(BSL_ERR_INPUT, "Odd symmetry needs l_max >= 1");
-  if (p.potential != BSL_POT_ALAVI_SPCE && p.potential != BSL_POT_ISOHARMOSC)
+  if (p.potential != BSL_POT_ALAVI_SPCE && p.potential != BSL_POT_ISOHARMOSC && p.potential != BSL_POT_ALAVI_TIP4P)
     return fail(BSL_ERR_INPUT, "unknown potential");
   if (p.precision != BSL_PREC_FP64 && p.precision != BSL_PREC_MIXED)
     return fail(BSL_ERR_INPUT, "unknown precision");
@@ -374,11 +389,11 @@ int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
     return fail(BSL_ERR_UNSUPPORTED, "symmetry block with " + std::to_string(h->t.nn) + " (l,m) functions exceeds " +
                                          std::to_string(kMaxNN));
   }
-  if (h->p.potential == BSL_POT_ALAVI_SPCE) {
+  if (h->p.potential != BSL_POT_ISOHARMOSC) {
     if (cage) {
       h->cage = *cage;
     } else {
-      rc = read_cage(h->p.geometry_filename, &h->cage);
+      rc = read_cage(h->p.geometry_filename, h->p.potential, &h->cage);
       if (rc) { delete h; return rc; }
     }
   }
@@ -447,7 +462,7 @@ int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
   if ((e = cudaMemset(d.status, 0, 4 * sizeof(int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
   // zero the padding points of the last tile of the streamed FP32 blocks
   if ((e = cudaMemset(d.vb32, 0, ntri * tiled * sizeof(float))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
-  rc = (h->p.potential == BSL_POT_ALAVI_SPCE) ? dev_potential_alavi(h) : dev_potential_iso(h);
+  rc = (h->p.potential == BSL_POT_ISOHARMOSC) ? dev_potential_iso(h) : dev_potential_alavi(h);
   if (rc) return bail(rc);
   if ((rc = dev_vblocks(h))) return bail(rc);
   if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return bail(cuda_fail(e, "HvPrep"));
@@ -536,6 +551,10 @@ int bsl_calculator_potential(const char* calculator, int* potential) {
     *potential = BSL_POT_ALAVI_SPCE;
     return BSL_OK;
   }
+  if (c == "linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P" || c == "linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P_GB300") {
+    *potential = BSL_POT_ALAVI_TIP4P;
+    return BSL_OK;
+  }
   if (c == "linRotCartSph_NoQuad_IsoHarmOsc" || c == "linRotCartSph_NoQuad_IsoHarmOsc_GB300") {
     *potential = BSL_POT_ISOHARMOSC;
     return BSL_OK;
@@ -545,26 +564,28 @@ int bsl_calculator_potential(const char* calculator, int* potential) {
 
 int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out) { return hv_prep(params, nullptr, out); }
 
-int bsl_cage_sites(int nmol, const double* cm_ang, const double* euler, const double* q_site, double* xyz, double* q) {
+int bsl_cage_sites(int potential, int nmol, const double* cm_ang, const double* euler, const double* q_site,
+                   double* xyz, double* q) {
   if (nmol < 1 || !cm_ang || !euler || !xyz || !q) return fail(BSL_ERR_INPUT, "bad arguments");
   Cage c;
-  build_cage(nmol, cm_ang, euler, q_site, &c);
+  build_cage(potential, nmol, cm_ang, euler, q_site, &c);
   std::copy(c.xyz.begin(), c.xyz.end(), xyz);
   std::copy(c.q.begin(), c.q.end(), q);
   return BSL_OK;
 }
 
-int bsl_rigid_body_gradient(int nmol, const double* cm_ang, const double* euler, int nlev, const double* dr_site,
-                            double* d_cm, double* d_euler) {
+int bsl_rigid_body_gradient(int potential, int nmol, const double* cm_ang, const double* euler, int nlev,
+                            const double* dr_site, double* d_cm, double* d_euler) {
   if (nmol < 1 || nlev < 1 || !cm_ang || !euler || !dr_site || !d_cm || !d_euler)
     return fail(BSL_ERR_INPUT, "bad arguments");
   Cage c;
-  build_cage(nmol, cm_ang, euler, nullptr, &c);
+  build_cage(potential, nmol, cm_ang, euler, nullptr, &c);
+  const int S = c.sites;
   for (int n = 0; n < nlev; ++n)
     for (int m = 0; m < nmol; ++m) {
       double gc[3] = {0, 0, 0}, ge[3] = {0, 0, 0};
-      for (int a = 0; a < 3; ++a) {
-        const double* g = dr_site + ((size_t)n * 3 * nmol + 3 * m + a) * 3;
+      for (int a = 0; a < S; ++a) {
+        const double* g = dr_site + ((size_t)n * S * nmol + S * m + a) * 3;
         for (int k = 0; k < 3; ++k) gc[k] += kNmPerAngstrom * g[k];  // site = R body + 0.1 cm
         for (int k = 0; k < 3; ++k) {
           double dsite[3];
@@ -583,9 +604,9 @@ int bsl_rigid_body_gradient(int nmol, const double* cm_ang, const double* euler,
 int bsl_hv_prep_cage(const bsl_hv_params* params, int nmol, const double* cm_ang, const double* euler,
                      const double* q_site, const double* q_alavi, bsl_handle** out) {
   if (!params || !out || nmol < 1 || !cm_ang || !euler) return fail(BSL_ERR_INPUT, "bad arguments");
-  if (params->potential != BSL_POT_ALAVI_SPCE) return fail(BSL_ERR_INPUT, "a cage needs the Alavi SPC/E potential");
+  if (params->potential == BSL_POT_ISOHARMOSC) return fail(BSL_ERR_INPUT, "a cage needs an Alavi potential");
   Cage c;
-  build_cage(nmol, cm_ang, euler, q_site, &c);
+  build_cage(params->potential, nmol, cm_ang, euler, q_site, &c);
   if (q_alavi) {
     c.q_h2_h = q_alavi[0];
     c.q_h2_cm = q_alavi[1];

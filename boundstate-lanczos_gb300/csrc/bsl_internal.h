@@ -57,20 +57,25 @@ struct Cage {
   std::vector<double> q;
   std::vector<int> is_o;
   // rigid-body description: per molecule the centre of mass (Angstrom) and the
-  // ZYZ Euler angles (rad); three sites O, H1, H2 per molecule
+  // ZYZ Euler angles (rad); `sites` sites per molecule (SPC/E: O, H1, H2;
+  // TIP4P: O, H1, H2, M)
   std::vector<double> cm_ang, euler;
+  int model = BSL_POT_ALAVI_SPCE, sites = 3;
+  // Lennard-Jones A / r^12 - B / r^6 between the H2 centre of mass and each O
+  double lj_a = 1.364e-06, lj_b = 1.533e-3;
   // Alavi H2 charges on each H and on the centre of mass (Alavi_Parameters.h:5-6)
   double q_h2_h = 0.4932, q_h2_cm = -0.9864;
 };
 
-// Sites of a cage of rigid SPC/E waters (SPCE_AH2_EngRoutines.cpp:5-108,
-// rotmat.cpp:6-32); q_site (3 per molecule) may be null for the SPC/E charges.
-void build_cage(int nmol, const double* cm_ang, const double* euler, const double* q_site, Cage* c);
-// d site / d (Euler angle k) for molecule m, site a (0 = O, 1 = H1, 2 = H2): out[3]
+// Sites of a cage of rigid waters (SPC/E: SPCE_AH2_EngRoutines.cpp:5-108; TIP4P:
+// TIP4P_AH2_EngRoutines.cpp getTIP4Patoms; rotmat.cpp:6-32); q_site (one per
+// site) may be null for the model's charges.
+void build_cage(int model, int nmol, const double* cm_ang, const double* euler, const double* q_site, Cage* c);
+// d site / d (Euler angle k) for molecule m, site a of the model: out[3]
 void site_angle_derivative(const Cage& c, int m, int a, int k, double* out);
 
 int build_tables(const bsl_hv_params& p, Tables* t);
-int read_cage(const std::string& path, Cage* c);
+int read_cage(const std::string& path, int model, Cage* c);
 
 // Device-resident state of one prepared Hamiltonian.
 struct DeviceState {

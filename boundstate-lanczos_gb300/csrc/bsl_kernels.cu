@@ -38,9 +38,9 @@ struct AtomSet {
   const int* is_o;
   int n;
   double q_h, q_cm;   // Alavi H2 charges: each H, centre of mass
+  double lj_a, lj_b;  // centre of mass - O Lennard-Jones A / r^12 - B / r^6 of the water model
 };
 
-constexpr double kA_LJ = 1.364e-06, kB_LJ = 1.533e-3;    // SPCE_AH2_EngRoutines.h:37-38
 constexpr int kMaxAtoms = 512;
 
 __device__ __forceinline__ double dist(const double* a, double x, double y, double z) {
@@ -80,7 +80,7 @@ __global__ void k_potential_cm(AtomSet atoms, const double* xg, const double* yg
   for (int a = 0; a < atoms.n; ++a) {
     if (!so[a]) continue;
     const double r = dist(sxyz + 3 * a, x, y, z);
-    lj = __dadd_rn(lj, __dsub_rn(__ddiv_rn(kA_LJ, pow(r, 12.0)), __ddiv_rn(kB_LJ, pow(r, 6.0))));
+    lj = __dadd_rn(lj, __dsub_rn(__ddiv_rn(atoms.lj_a, pow(r, 12.0)), __ddiv_rn(atoms.lj_b, pow(r, 6.0))));
   }
   cm[p] = __dadd_rn(e, lj);
 }
@@ -598,7 +598,7 @@ int dev_potential_alavi(bsl_handle* h) {
     cleanup();
     return cuda_fail(e, "potential upload");
   }
-  AtomSet atoms{dxyz, dq, dis_o, natoms, h->cage.q_h2_h, h->cage.q_h2_cm};
+  AtomSet atoms{dxyz, dq, dis_o, natoms, h->cage.q_h2_h, h->cage.q_h2_cm, h->cage.lj_a, h->cage.lj_b};
   const long long N = t.npts;
   const int nab = t.na * t.nb;
   double* cm = d.ukin;  // scratch of >= N doubles

@@ -46,6 +46,7 @@ extern "C" {
 /* potential selected by the HvCalculator string */
 #define BSL_POT_ALAVI_SPCE 0  /* linRotCartSph_NoQuad_ContGrid_Alavi_SPCE */
 #define BSL_POT_ISOHARMOSC 1  /* linRotCartSph_NoQuad_IsoHarmOsc */
+#define BSL_POT_ALAVI_TIP4P 2 /* linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P */
 
 /* arithmetic of the Hv application */
 #define BSL_PREC_FP64 0  /* every step in FP64 */
@@ -129,7 +130,8 @@ int bsl_hv_prep(const bsl_hv_params* params, bsl_handle** out);
    Angstrom cm_ang[3 nmol] and ZYZ Euler angles euler[3 nmol] in the file's
    order (SPCE_AH2_EngRoutines.cpp:5-108); q_site[3 nmol] (O, H1, H2 per
    molecule) replaces the SPC/E charges when not NULL, q_alavi[2] (each H,
-   centre of mass) the Alavi H2 charges when not NULL.  Alavi SPC/E only. */
+   centre of mass) the Alavi H2 charges when not NULL.  Alavi SPC/E or TIP4P
+   (params->potential; TIP4P: q_site[4 nmol], O, H1, H2, M per molecule). */
 int bsl_hv_prep_cage(const bsl_hv_params* params, int nmol, const double* cm_ang, const double* euler,
                      const double* q_site, const double* q_alavi, bsl_handle** out);
 
@@ -258,21 +260,23 @@ int bsl_write_ritz_vectors(const char* dir, const char* sim_descr, long long bas
    layout (any normalisation; e.g. from bsl_ritz_vectors); outputs
    dq_site[n * natoms + w] (kJ/mol per e), dr_site[(n * natoms + w) * 3 + k]
    (kJ/mol per nm), dq_alavi[2 n + {0, 1}] (the H and centre-of-mass charges of
-   H2).  Sites are O, H1, H2 per molecule in file order.  No counterpart in the
-   reference. */
+   H2).  Sites are O, H1, H2 (SPC/E) or O, H1, H2, M (TIP4P) per molecule in file
+   order.  No counterpart in the reference. */
 int bsl_hf_gradient(bsl_handle* h, int nlev, const double* psi, double* dq_site, double* dr_site,
                     double* dq_alavi);
 
 /* Chain rule from site positions to the rigid-body coordinates of the cage
-   (centre of mass in Angstrom, ZYZ Euler angles in rad; SPCE_AH2_EngRoutines.cpp:5-108):
-   dr_site[(n * 3 nmol + site) * 3 + k] -> d_cm[(n * nmol + m) * 3 + k],
-   d_euler[(n * nmol + m) * 3 + k].  Host only. */
-int bsl_rigid_body_gradient(int nmol, const double* cm_ang, const double* euler, int nlev, const double* dr_site,
-                            double* d_cm, double* d_euler);
+   (centre of mass in Angstrom, ZYZ Euler angles in rad; SPCE_AH2_EngRoutines.cpp:5-108,
+   TIP4P_AH2_EngRoutines.cpp): potential = BSL_POT_ALAVI_SPCE (3 sites per
+   molecule) or BSL_POT_ALAVI_TIP4P (4); dr_site[(n * S nmol + site) * 3 + k] ->
+   d_cm[(n * nmol + m) * 3 + k], d_euler[(n * nmol + m) * 3 + k].  Host only. */
+int bsl_rigid_body_gradient(int potential, int nmol, const double* cm_ang, const double* euler, int nlev,
+                            const double* dr_site, double* d_cm, double* d_euler);
 
-/* Site positions (nm) and charges of a cage of rigid SPC/E waters: xyz[3 * 3 nmol],
-   q[3 nmol] (q_site NULL: the SPC/E charges).  Host only. */
-int bsl_cage_sites(int nmol, const double* cm_ang, const double* euler, const double* q_site, double* xyz, double* q);
+/* Site positions (nm) and charges of a cage of rigid waters of the given model:
+   xyz[3 * S nmol], q[S nmol] (q_site NULL: the model's charges).  Host only. */
+int bsl_cage_sites(int potential, int nmol, const double* cm_ang, const double* euler, const double* q_site,
+                   double* xyz, double* q);
 
 /* bsl_ritz_vectors from the start vector of a bsl_lanczos_run(start, seed)
    (bsl_ritz_vectors itself restarts from BSL_START_UNIFORM, as the reference). */

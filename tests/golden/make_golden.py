@@ -8,7 +8,10 @@ reference's own stored runs (Compilation/SmallBasisTest2_*), so that the tests
 can pin the oracle restatement and the GPU path where the reference tree is
 absent.
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py [REFERENCE_ROOT [CASE ...]]
+
+With case names, only those cases are (re)generated and merged into the
+existing manifest.
 """
 import ctypes as C
 import glob
@@ -26,6 +29,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ONLY = set(sys.argv[2:])
 REF_LIB = os.path.join(REPO, "oracle", "_ref", "libref_hv.so")
 REF_BIN = os.path.join(REPO, "oracle", "_ref", "ref_lanczos")
 
@@ -35,6 +39,7 @@ inputs = importlib.util.module_from_spec(_spec)
 _spec.loader.exec_module(inputs)
 
 CONTGRID = "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE"
+CONTGRID_TIP4P = "linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P"
 ISO = "linRotCartSph_NoQuad_IsoHarmOsc"
 
 # name: (calculator, n, x_max, l_max, theta, phi, sym, geometry, niter, hv_full, iso)
@@ -49,6 +54,8 @@ CASES = {
     "iso_n20_l2_all": (ISO, 20, 0.3, 2, 4, 4, "All", "NULL", 300, True, (2.015650064, 24.1, 100.0)),
     # the CPU workload itself: 15^3 even l<=4 12 x 24, cage seed 0, 600 iterations
     "cpu_workload": (CONTGRID, 15, 0.08, 4, 12, 12, "Even", "cage_seed0.xyz", 600, False, None),
+    # the same continuous-grid path with TIP4P water
+    "tip4p_seed1_n6_l3_odd": (CONTGRID_TIP4P, 6, 0.08, 3, 8, 7, "Odd", "cage_seed1.xyz", 200, True, None),
 }
 
 
@@ -87,7 +94,12 @@ def main():
     for seed in (0, 1):
         inputs.write_cage_xyz(os.path.join(HERE, "cage_seed%d.xyz" % seed), inputs.dodecahedral_cage(seed))
     manifest = {}
+    if ONLY:
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest = json.load(f)
     for name, (calc, n, xm, lmax, th, ph, sym, geo, niter, full, iso) in CASES.items():
+        if ONLY and name not in ONLY:
+            continue
         d = os.path.join(HERE, name)
         os.makedirs(d, exist_ok=True)
         if geo != "NULL":
@@ -122,6 +134,10 @@ def main():
         np.savez(os.path.join(d, "ref_alpha_beta.npz"), alpha=alpha, beta=beta)
         manifest[name] = rec
         print(name, rec)
+    if ONLY:
+        with open(os.path.join(HERE, "manifest.json"), "w") as f:
+            json.dump(manifest, f, indent=1)
+        return
     # the reference's own stored 2013 runs that the final tree reproduces
     stored = {}
     for run in ("SmallBasisTest2_2013-09-03_18_36_00", "SmallBasisTest2_2013-09-03_19_06_47"):

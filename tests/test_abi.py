@@ -77,7 +77,7 @@ def test_parse_errors(bsl, tmp_path, in_case_dir):
 
 
 @pytest.mark.parametrize("name", ["cage11_n10_l3_all", "seed1_n6_l3_odd", "seed0_n5_l4_even", "iso_n20_l2_all",
-                                  "cpu_workload"])
+                                  "cpu_workload", "tip4p_seed1_n6_l3_odd"])
 def test_tail_matches_oracle(bsl, name):
     d, man, _ = case_info(name)
     ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))
@@ -148,7 +148,7 @@ def _lanczos_limits(d):
 
 
 @pytest.mark.parametrize("name", ["cage11_n10_l3_all", "seed1_n6_l3_odd", "seed0_n5_l4_even", "iso_n20_l2_all",
-                                  "cpu_workload"])
+                                  "cpu_workload", "tip4p_seed1_n6_l3_odd"])
 def test_boundstates_file_matches_reference(bsl, name, tmp_path):
     """boundstates.txt written from the tail on the reference's alpha/beta has the
     reference's layout, states and eigenvalues (the stored alpha/beta are the

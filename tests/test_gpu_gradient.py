@@ -132,3 +132,46 @@ def test_autograd_function(bsl):
     assert np.allclose(tcm.grad.numpy(), np.einsum("n,nmk->mk", wn, dcm), rtol=1e-10, atol=1e-12)
     assert np.allclose(tea.grad.numpy(), np.einsum("n,nmk->mk", wn, dea), rtol=1e-10, atol=1e-12)
     assert np.allclose(tqa.grad.numpy(), wn @ da, rtol=1e-10, atol=1e-12)
+
+
+def test_hf_gradient_tip4p(bsl):
+    """The same derivatives with TIP4P water (4 sites per molecule, charge on M,
+    Lennard-Jones on O): central differences on an M charge, an H charge, a
+    centre and an angle."""
+    d, p, cm, ea, q, qa = setup_case(bsl)
+    T4 = bsl.POT_ALAVI_TIP4P
+    q4 = bsl.cage_sites(cm, ea, potential=T4)[1]
+    assert q4.shape == (80,) and abs(q4.sum()) < 1e-12
+
+    def lev(cm_, ea_, q_, grads=False):
+        h = bsl.Hamiltonian.from_cage(p, cm_, ea_, q_, qa, potential=T4)
+        try:
+            a, b, b2 = h.lanczos(NITER, start="normal", seed=1)
+            ev, _ = bsl.good_eigenvalues(a, b, b2, -10.0, 10.0)
+            ev = ev[:NLEV]
+            if not grads:
+                return ev, None
+            rows = bsl.tm_eigenvectors(a, b, b2, ev)
+            return ev, h.hf_gradient(h.ritz(NITER, rows, start="normal", seed=1), 80)
+        finally:
+            h.close()
+
+    ev, (dq, dr, da) = lev(cm, ea, q4, grads=True)
+    dcm, dea = bsl.rigid_body_gradient(cm, ea, dr, potential=T4)
+    h = 1e-4
+    for w in (3, 9):  # M site of molecule 0, H site of molecule 2
+        qp, qm = q4.copy(), q4.copy()
+        qp[w] += h
+        qm[w] -= h
+        f = (lev(cm, ea, qp)[0] - lev(cm, ea, qm)[0]) / (2 * h)
+        assert np.allclose(dq[:, w], f, rtol=2e-4, atol=2e-5), (dq[:, w], f)
+    cp, cq = cm.copy(), cm.copy()
+    cp[6, 1] += h
+    cq[6, 1] -= h
+    f = (lev(cp, ea, q4)[0] - lev(cq, ea, q4)[0]) / (2 * h)
+    assert np.allclose(dcm[:, 6, 1], f, rtol=2e-4, atol=2e-5), (dcm[:, 6, 1], f)
+    ep, eq = ea.copy(), ea.copy()
+    ep[9, 2] += h
+    eq[9, 2] -= h
+    f = (lev(cm, ep, q4)[0] - lev(cm, eq, q4)[0]) / (2 * h)
+    assert np.allclose(dea[:, 9, 2], f, rtol=2e-4, atol=2e-5), (dea[:, 9, 2], f)

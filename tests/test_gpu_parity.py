@@ -9,7 +9,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import CASES, OracleModel, case_info, load_package, oracle_lancbis, read_boundstates
+from conftest import CASES, REF_ONLY_CASES, OracleModel, case_info, load_package, oracle_lancbis, read_boundstates
 
 pytestmark = pytest.mark.gpu
 KJ_TO_CM = 83.5935
@@ -37,7 +37,7 @@ def rel(a, b):
     return np.max(np.abs(a - b)) / np.max(np.abs(b))
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", CASES + REF_ONLY_CASES)
 def test_hv_fp64_matches_reference(bsl, name):
     h, d, man, _ = make(bsl, name)
     assert h.basis_size == man["basis_size"]
@@ -70,7 +70,7 @@ def test_hv_cpu_workload_fp64_and_mixed(bsl):
     h.close()
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", CASES + REF_ONLY_CASES)
 def test_hv_mixed_engines_match_fp64(bsl, name):
     """Both kinetic engines of the mixed path against the FP64 path (2e-6 relative)."""
     h, d, man, _ = make(bsl, name)
@@ -130,7 +130,7 @@ def stable_levels(alpha, beta, drop=40, tol=1e-10, emax=10.0):
     return np.array([e for e in ev if np.min(np.abs(ev2 - e)) <= tol])
 
 
-@pytest.mark.parametrize("name", CASES + ["cpu_workload"])
+@pytest.mark.parametrize("name", CASES + REF_ONLY_CASES + ["cpu_workload"])
 def test_lanczos_fp64_eigenvalues_match_reference(bsl, name):
     h, d, man, _ = make(bsl, name)
     ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))
