@@ -307,6 +307,23 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = world * args.e2e_steps / e2e_s
+    # the transfer floor of that path: the same bytes between pinned host memory
+    # and the device through torch, each direction on its own
+    dv = torch.empty(Df, dtype=torch.float64, device="cuda")
+    tv, tr = torch.from_numpy(vec), torch.from_numpy(rvec)
+    ev0, ev1, ev2 = torch.cuda.Event(True), torch.cuda.Event(True), torch.cuda.Event(True)
+    torch.cuda.synchronize()
+    ev0.record()
+    for _ in range(5):
+        dv.copy_(tv, non_blocking=True)
+        dv.copy_(tr, non_blocking=True)
+    ev1.record()
+    for _ in range(5):
+        tv.copy_(dv, non_blocking=True)
+        tr.copy_(dv, non_blocking=True)
+    ev2.record()
+    torch.cuda.synchronize()
+    h2d_ms, d2h_ms = ev0.elapsed_time(ev1) / 5, ev1.elapsed_time(ev2) / 5
 
     # ---- FP64 GPU path ----
     h.set_precision("fp64")
@@ -370,6 +387,7 @@ def main():
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (generated SPC/E cage, seed 1)",
         "config": dict(config_record(cfg, D, Df), kinetic_engine=kinetic_engine),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * Df * 8, "d2h_bytes_per_step": 2 * Df * 8,
+                "ms_per_step": 1000.0 / e2e_value * world, "h2d_ms_per_step": h2d_ms, "d2h_ms_per_step": d2h_ms,
                 "path": "bsl_lanczos_step_host: reference loop body with host (pinned) vec/rvec in the reference "
                         "layout, H2D + Hv + recurrence + D2H per step"},
         "roofline": {"bound": "hbm", "kernel": stage_names[dom] if stage_names else None,

@@ -323,12 +323,14 @@ void free_device(DeviceState& d) {
   void* ptrs[] = {d.tx, d.ty, d.tz, d.kx_head, d.ky_head, d.kz_head, d.kx_band, d.ky_band, d.kz_band, d.rot,
                   d.v1, d.v2, d.vb64, d.vb32, d.vec, d.rvec, d.ukin, d.v32, d.rot_hi, d.rot_lo, d.partials,
                   d.counter,
-                  d.scalars, d.status, d.hist, d.ref_vec, d.ref_out, d.full_of, d.ritz};
+                  d.scalars, d.status, d.hist, d.ref_vec, d.ref_out, d.full_of, d.packed_of, d.ritz};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (d.vpair) cudaFree(d.vpair);
   if (d.kxy_slices) cudaFree(d.kxy_slices);
   if (d.kz_slices) cudaFree(d.kz_slices);
+  if (d.copy_done) cudaEventDestroy(d.copy_done);
+  if (d.copy_stream) cudaStreamDestroy(d.copy_stream);
   if (d.ev0) cudaEventDestroy(d.ev0);
   if (d.ev1) cudaEventDestroy(d.ev1);
   if (d.stream) cudaStreamDestroy(d.stream);
@@ -437,6 +439,11 @@ int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
     if ((rc = upload(&d.rot_hi, rh, "rotor")) || (rc = upload(&d.rot_lo, rl, "rotor"))) return bail(rc);
   }
   if ((rc = upload(&d.full_of, t.full_of, "index map"))) return bail(rc);
+  {
+    std::vector<int> pof(t.nn_full, -1);
+    for (int s2 = 0; s2 < t.nn; ++s2) pof[t.full_of[s2]] = s2;
+    if ((rc = upload(&d.packed_of, pof, "index map"))) return bail(rc);
+  }
   const size_t N = (size_t)t.npts, D = N * t.nn;
   const size_t ngrid = N * t.na * t.nb;
   const size_t ntri = (size_t)t.nn * (t.nn + 1) / 2;

@@ -114,6 +114,9 @@ struct DeviceState {
   // host-layout staging
   double *ref_vec = nullptr, *ref_out = nullptr;  // full reference layout
   int* full_of = nullptr;                          // packed -> full index
+  int* packed_of = nullptr;                        // full (l, m) index -> packed, -1 outside the block
+  cudaStream_t copy_stream = nullptr;              // host-state step: second copy-in stream
+  cudaEvent_t copy_done = nullptr;
   double* ritz = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int red_blocks = 0;
@@ -149,6 +152,8 @@ int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_
 const char* dev_stage_name(bsl_handle* h, int i);
 int dev_fill_start(bsl_handle* h, int start, unsigned long long seed, cudaStream_t s);
 int dev_gather_packed(bsl_handle* h, const double* full, double* packed, cudaStream_t s);
+int dev_hv_full(bsl_handle* h, const double* full, double* out, cudaStream_t s);
+int dev_full_step_fused(bsl_handle* h, double* v, double* r, long long L, const double* hv, int j, cudaStream_t s);
 int dev_scatter_full(bsl_handle* h, const double* packed, double* full_accum, cudaStream_t s);
 int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, int ngood, double* ritz,
                         cudaStream_t s);

@@ -245,16 +245,30 @@ __global__ void k_kin_z_f64(const double* __restrict__ vec, double* __restrict__
   }
 }
 
-// ---------------------------------------------------------------------------
-// Lanczos vector kernels over L entries (packed block plus the extra
-// coordinate, or the whole reference layout)
-// ---------------------------------------------------------------------------
-// alpha = v . r
-__global__ void k_dot_alpha(const double* __restrict__ v, const double* __restrict__ r, long long L, double* partials,
-                            unsigned int* counter, double* scalars, double* hist, int j) {
+// Full-layout step of the host-state loop body (lanczosEigenValuesVectors.cpp:
+// 195-238), three passes in the reference's per-element FP64 arithmetic:
+//   1. r_i += (H v)_i on the symmetry block (packed_of: full function -> packed, -1
+//      outside), alpha = v . r
+//   2. beta^2 = |r - alpha v|^2 (nothing written)
+//   3. v <- (r - alpha v) / beta, r <- -beta v
+__global__ void k_scatter_dot(const double* __restrict__ v, double* __restrict__ r, long long L,
+                              const double* __restrict__ hv, const int* __restrict__ packed_of, long long npts,
+                              int nfull, double* partials, unsigned int* counter, double* scalars, double* hist,
+                              int j) {
+  __shared__ int pof[1024];
+  for (int f = threadIdx.x; f < nfull && f < 1024; f += blockDim.x) pof[f] = packed_of[f];
+  __syncthreads();
   double acc = 0.0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x)
-    acc += v[i] * r[i];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x) {
+    const long long f = i / npts;
+    const int s = pof[f];
+    double ri = r[i];
+    if (s >= 0) {
+      ri = ri + hv[(long long)s * npts + (i - f * npts)];
+      r[i] = ri;
+    }
+    acc += v[i] * ri;
+  }
   double total;
   if (reduce_grid(acc, partials, counter, &total) && threadIdx.x == 0) {
     scalars[0] = total;
@@ -262,15 +276,13 @@ __global__ void k_dot_alpha(const double* __restrict__ v, const double* __restri
   }
 }
 
-// r -= alpha v ; beta^2 = r . r ; beta = sqrt(beta^2)
-__global__ void k_update_beta(const double* __restrict__ v, double* __restrict__ r, long long L, double* partials,
-                              unsigned int* counter, double* scalars, double* hist, int hist_stride, int j,
-                              int* status) {
+__global__ void k_beta_only(const double* __restrict__ v, const double* __restrict__ r, long long L, double* partials,
+                            unsigned int* counter, double* scalars, double* hist, int hist_stride, int j,
+                            int* status) {
   const double alpha = scalars[0];
   double acc = 0.0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x) {
     const double x = r[i] - alpha * v[i];
-    r[i] = x;
     acc += x * x;
   }
   double total;
@@ -288,15 +300,28 @@ __global__ void k_update_beta(const double* __restrict__ v, double* __restrict__
   }
 }
 
-// v_{j+1} = r / beta ; r_{j+1} = -beta v_j  (the reference's scale-then-swap)
-__global__ void k_normalize_swap(double* __restrict__ v, double* __restrict__ r, long long L,
-                                 const double* __restrict__ scalars) {
-  const double b = scalars[1], inv = scalars[3];
+__global__ void k_normalize_fused(double* __restrict__ v, double* __restrict__ r, long long L,
+                                  const double* __restrict__ scalars) {
+  const double alpha = scalars[0], b = scalars[1], inv = scalars[3];
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x) {
     const double vi = v[i];
-    v[i] = inv * r[i];
+    const double x = r[i] - alpha * vi;
+    v[i] = inv * x;
     r[i] = (-b) * vi;
   }
+}
+
+// packed FP32 copy and double-float pairs of a full-layout FP64 vector
+__global__ void k_gather_mixed(const double* __restrict__ full, float* __restrict__ v32, float2* __restrict__ vpair,
+                               const int* __restrict__ full_of, long long npts, int nn) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= npts * nn) return;
+  const int s = (int)(e / npts);
+  const long long p = e - (long long)s * npts;
+  const double x = full[(long long)full_of[s] * npts + p];
+  const float2 d = df_of(x);
+  v32[e] = d.x;
+  if (vpair) vpair[e] = d;
 }
 
 // Folded-scale update of the packed loop.  The logical vectors are v = sv V and
@@ -817,13 +842,33 @@ int dev_scatter_full(bsl_handle* h, const double* packed, double* full_accum, cu
   return BSL_OK;
 }
 
-// Full-layout Lanczos step on device buffers v, r (length L) after r += H v.
-int dev_full_step(bsl_handle* h, double* v, double* r, long long L, int j, cudaStream_t s) {
+// H v of a full-layout FP64 vector into packed FP64 `out` (mode 0), without a
+// packed FP64 copy on the mixed path.
+int dev_hv_full(bsl_handle* h, const double* full, double* out, cudaStream_t s) {
+  DeviceState& d = h->d;
+  const long long N = h->t.npts, D = bsl_packed_size(h);
+  if (h->precision != BSL_PREC_MIXED) {
+    k_gather<<<grid_for(N * h->t.nn), kThreads, 0, s>>>(full, d.vec, d.full_of, N, h->t.nn);
+    BSL_CUDA(cudaGetLastError());
+    return dev_hv(h, d.vec, out, s);
+  }
+  const bool tc = h->kinetic_engine == BSL_KIN_TENSOR;
+  if (tc && !d.vpair) BSL_CUDA(cudaMalloc(&d.vpair, (size_t)D * sizeof(float2)));
+  k_gather_mixed<<<grid_for(D), kThreads, 0, s>>>(full, d.v32, tc ? d.vpair : nullptr, d.full_of, N, h->t.nn);
+  BSL_CUDA(cudaGetLastError());
+  int rc = launch_kinetic(h, nullptr, d.vpair, s);
+  if (rc) return rc;
+  return launch_vapply(h, nullptr, out, 0, 0, s);
+}
+
+// The full-layout host step after H v: r += S H v, alpha, beta, normalise and swap.
+int dev_full_step_fused(bsl_handle* h, double* v, double* r, long long L, const double* hv, int j, cudaStream_t s) {
   DeviceState& d = h->d;
   const int g = d.red_blocks;
-  k_dot_alpha<<<g, kThreads, 0, s>>>(v, r, L, d.partials, d.counter, d.scalars, d.hist, j);
-  k_update_beta<<<g, kThreads, 0, s>>>(v, r, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j, d.status);
-  k_normalize_swap<<<g, kThreads, 0, s>>>(v, r, L, d.scalars);
+  k_scatter_dot<<<g, kThreads, 0, s>>>(v, r, L, hv, d.packed_of, h->t.npts, h->t.nn_full, d.partials, d.counter,
+                                       d.scalars, d.hist, j);
+  k_beta_only<<<g, kThreads, 0, s>>>(v, r, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j, d.status);
+  k_normalize_fused<<<g, kThreads, 0, s>>>(v, r, L, d.scalars);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }

@@ -25,7 +25,6 @@ namespace bsl {
 int dev_fill(double* x, long long L, double val, cudaStream_t s);
 int dev_to_f32(const double* x, float* y, long long n, cudaStream_t s);
 int dev_to_pair(double* x, long long n, cudaStream_t s);
-int dev_full_step(bsl_handle* h, double* v, double* r, long long L, int j, cudaStream_t s);
 
 namespace {
 
@@ -42,6 +41,10 @@ int ensure_hist(bsl_handle* h, int niter) {
 
 int ensure_staging(bsl_handle* h) {
   DeviceState& d = h->d;
+  if (!d.copy_stream) {
+    BSL_CUDA(cudaStreamCreateWithFlags(&d.copy_stream, cudaStreamNonBlocking));
+    BSL_CUDA(cudaEventCreateWithFlags(&d.copy_done, cudaEventDisableTiming));
+  }
   if (d.ref_vec) return BSL_OK;
   const size_t Df = (size_t)bsl_basis_size(h);
   BSL_CUDA(cudaMalloc(&d.ref_vec, Df * sizeof(double) + 16));
@@ -201,16 +204,18 @@ int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alph
   if ((rc = ensure_hist(h, 1)) || (rc = ensure_staging(h))) return rc;
   const size_t Df = (size_t)bsl_basis_size(h);
   cudaStream_t s = d.stream;
+  // vec feeds H v at once; rvec is copied in on a second stream meanwhile and
+  // only waited for where r += H v needs it
   BSL_CUDA(cudaMemcpyAsync(d.ref_vec, vec, Df * sizeof(double), cudaMemcpyHostToDevice, s));
-  BSL_CUDA(cudaMemcpyAsync(d.ref_out, rvec, Df * sizeof(double), cudaMemcpyHostToDevice, s));
+  BSL_CUDA(cudaMemcpyAsync(d.ref_out, rvec, Df * sizeof(double), cudaMemcpyHostToDevice, d.copy_stream));
+  BSL_CUDA(cudaEventRecord(d.copy_done, d.copy_stream));
   BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
   // r += S H v: H on the packed block, nothing elsewhere (the device Lanczos
   // vectors serve as packed scratch)
   h->state_pairs = -1;
-  if ((rc = dev_gather_packed(h, d.ref_vec, d.vec, s))) return rc;
-  if ((rc = dev_hv(h, d.vec, d.rvec, s))) return rc;
-  if ((rc = dev_scatter_full(h, d.rvec, d.ref_out, s))) return rc;
-  if ((rc = dev_full_step(h, d.ref_vec, d.ref_out, (long long)Df, 1, s))) return rc;
+  if ((rc = dev_hv_full(h, d.ref_vec, d.rvec, s))) return rc;
+  BSL_CUDA(cudaStreamWaitEvent(s, d.copy_done, 0));
+  if ((rc = dev_full_step_fused(h, d.ref_vec, d.ref_out, (long long)Df, d.rvec, 1, s))) return rc;
   BSL_CUDA(cudaMemcpyAsync(vec, d.ref_vec, Df * sizeof(double), cudaMemcpyDeviceToHost, s));
   BSL_CUDA(cudaMemcpyAsync(rvec, d.ref_out, Df * sizeof(double), cudaMemcpyDeviceToHost, s));
   double sc[3];
