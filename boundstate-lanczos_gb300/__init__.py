@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(HERE, "libbsl_gb300.so")
 OK, ERR_INPUT, ERR_CUDA, ERR_STATE, ERR_BREAKDOWN, ERR_UNSUPPORTED, ERR_NOMEM = range(7)
 SYM = {"All": 0, "Even": 1, "Odd": 2}
 POT_ALAVI_SPCE, POT_ISOHARMOSC, POT_ALAVI_TIP4P = 0, 1, 2
+POT_POINT_ALAVI_SPCE, POT_POINT_ALAVI_TIP4P, POT_COULOMB = 3, 4, 5
 PREC = {"fp64": 0, "mixed": 1}
 START = {"uniform": 0, "normal": 1}
 KINETIC = {"simt": 0, "tensor": 1}
@@ -32,6 +33,12 @@ CALCULATORS = {
     "linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P": POT_ALAVI_TIP4P,
     "linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P_GB300": POT_ALAVI_TIP4P,
     "linRotCartSph_NoQuad_IsoHarmOsc_GB300": POT_ISOHARMOSC,
+    "linRotCartSph_NoQuad_Alavi_SPCE": POT_POINT_ALAVI_SPCE,
+    "linRotCartSph_NoQuad_Alavi_SPCE_GB300": POT_POINT_ALAVI_SPCE,
+    "linRotCartSph_NoQuad_Alavi_TIP4P": POT_POINT_ALAVI_TIP4P,
+    "linRotCartSph_NoQuad_Alavi_TIP4P_GB300": POT_POINT_ALAVI_TIP4P,
+    "linRotCartSph_NoQuad_Coulomb": POT_COULOMB,
+    "linRotCartSph_NoQuad_Coulomb_GB300": POT_COULOMB,
 }
 
 
@@ -51,7 +58,9 @@ class HvParams(C.Structure):
                 ("simulation_title", C.c_char * 256), ("ceiling_potential", C.c_double),
                 ("quadrature_study", C.c_int), ("symmetry", C.c_int), ("potential", C.c_int),
                 ("iso_mass", C.c_double), ("iso_frequency", C.c_double), ("iso_ceiling", C.c_double),
-                ("precision", C.c_int), ("device", C.c_int), ("keep_potential_grid", C.c_int)]
+                ("precision", C.c_int), ("device", C.c_int), ("keep_potential_grid", C.c_int),
+                ("coulomb_centre_charge", C.c_double), ("coulomb_mol_charge", C.c_double),
+                ("coulomb_ceiling", C.c_double)]
 
 
 _lib = None
@@ -103,6 +112,7 @@ def lib():
     L.bsl_copy_vblocks.argtypes = [C.c_void_p, _P]
     L.bsl_parse_hv_input.argtypes = [C.c_char_p, C.POINTER(HvParams)]
     L.bsl_parse_isoharmosc_input.argtypes = [C.c_char_p, C.POINTER(HvParams)]
+    L.bsl_parse_coulomb_input.argtypes = [C.c_char_p, C.POINTER(HvParams)]
     L.bsl_calculator_potential.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
     _lib = L
     return L
@@ -167,7 +177,7 @@ def _f64(x):
 
 
 def sites_per_molecule(potential):
-    return 4 if potential == POT_ALAVI_TIP4P else 3
+    return 4 if potential in (POT_ALAVI_TIP4P, POT_POINT_ALAVI_TIP4P) else 3
 
 
 def cage_sites(cm_ang, euler, q_site=None, potential=POT_ALAVI_SPCE):
@@ -224,6 +234,8 @@ class Hamiltonian:
         p.potential = pot.value
         if p.potential == POT_ISOHARMOSC:
             _check(L.bsl_parse_isoharmosc_input(extra_input.encode(), C.byref(p)))
+        if p.potential == POT_COULOMB:
+            _check(L.bsl_parse_coulomb_input(extra_input.encode(), C.byref(p)))
         p.precision = PREC[precision]
         p.device = device
         self.params = p

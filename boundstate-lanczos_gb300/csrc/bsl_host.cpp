@@ -264,7 +264,7 @@ const double* body_site(int model, int a) {
 }  // namespace
 
 void build_cage(int model, int nmol, const double* cm_ang, const double* euler, const double* q_site, Cage* c) {
-  const bool t4 = model == BSL_POT_ALAVI_TIP4P;
+  const bool t4 = cage_model(model) == BSL_POT_ALAVI_TIP4P;
   c->model = t4 ? BSL_POT_ALAVI_TIP4P : BSL_POT_ALAVI_SPCE;
   c->sites = t4 ? 4 : 3;
   c->lj_a = t4 ? kT4A : 1.364e-06;  // SPCE_AH2_EngRoutines.h:37-38
@@ -330,6 +330,7 @@ void free_device(DeviceState& d) {
   if (d.kxy_slices) cudaFree(d.kxy_slices);
   if (d.kz_slices) cudaFree(d.kz_slices);
   if (d.copy_done) cudaEventDestroy(d.copy_done);
+  if (d.vec_in) cudaEventDestroy(d.vec_in);
   if (d.copy_stream) cudaStreamDestroy(d.copy_stream);
   if (d.ev0) cudaEventDestroy(d.ev0);
   if (d.ev1) cudaEventDestroy(d.ev1);
@@ -367,7 +368,7 @@ int validate(const bsl_hv_params& p) {
   if (p.symmetry < BSL_SYM_ALL || p.symmetry > BSL_SYM_ODD)
     return fail(BSL_ERR_INPUT, "ERROR: Symmeterizer Flag not recognized.");
   if (p.symmetry == BSL_SYM_ODD && p.l_max < 1) return fail(BSL_ERR_INPUT, "Odd symmetry needs l_max >= 1");
-  if (p.potential != BSL_POT_ALAVI_SPCE && p.potential != BSL_POT_ISOHARMOSC && p.potential != BSL_POT_ALAVI_TIP4P)
+  if (p.potential < BSL_POT_ALAVI_SPCE || p.potential > BSL_POT_COULOMB)
     return fail(BSL_ERR_INPUT, "unknown potential");
   if (p.precision != BSL_PREC_FP64 && p.precision != BSL_PREC_MIXED)
     return fail(BSL_ERR_INPUT, "unknown precision");
@@ -391,7 +392,7 @@ int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
     return fail(BSL_ERR_UNSUPPORTED, "symmetry block with " + std::to_string(h->t.nn) + " (l,m) functions exceeds " +
                                          std::to_string(kMaxNN));
   }
-  if (h->p.potential != BSL_POT_ISOHARMOSC) {
+  if (has_cage(h->p.potential)) {
     if (cage) {
       h->cage = *cage;
     } else {
@@ -469,7 +470,13 @@ int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
   if ((e = cudaMemset(d.status, 0, 4 * sizeof(int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
   // zero the padding points of the last tile of the streamed FP32 blocks
   if ((e = cudaMemset(d.vb32, 0, ntri * tiled * sizeof(float))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
-  rc = (h->p.potential == BSL_POT_ISOHARMOSC) ? dev_potential_iso(h) : dev_potential_alavi(h);
+  switch (h->p.potential) {
+    case BSL_POT_ISOHARMOSC: rc = dev_potential_iso(h); break;
+    case BSL_POT_COULOMB: rc = dev_potential_coulomb(h); break;
+    case BSL_POT_POINT_ALAVI_SPCE:
+    case BSL_POT_POINT_ALAVI_TIP4P: rc = dev_potential_point_alavi(h); break;
+    default: rc = dev_potential_alavi(h);
+  }
   if (rc) return bail(rc);
   if ((rc = dev_vblocks(h))) return bail(rc);
   if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return bail(cuda_fail(e, "HvPrep"));
@@ -551,9 +558,37 @@ int bsl_parse_isoharmosc_input(const char* path, bsl_hv_params* inout) {
   return BSL_OK;
 }
 
+int bsl_parse_coulomb_input(const char* path, bsl_hv_params* inout) {
+  if (!path || !inout) return fail(BSL_ERR_INPUT, "null argument");
+  std::ifstream f(path);
+  if (!f.is_open())
+    return fail(BSL_ERR_INPUT, std::string("Coulomb Potential input file '") + path + "' could not be opened.");
+  std::string line;
+  std::getline(f, line);
+  std::getline(f, line);
+  std::vector<std::string> v;
+  if (!read_token_pairs(f, &v, 3)) return fail(BSL_ERR_INPUT, "Coulomb input file is truncated");
+  if (!(to_double(v[0], &inout->coulomb_centre_charge) && to_double(v[1], &inout->coulomb_mol_charge) &&
+        to_double(v[2], &inout->coulomb_ceiling)))
+    return fail(BSL_ERR_INPUT, "Coulomb input file: malformed number");
+  inout->potential = BSL_POT_COULOMB;
+  return BSL_OK;
+}
+
 int bsl_calculator_potential(const char* calculator, int* potential) {
   if (!calculator || !potential) return fail(BSL_ERR_INPUT, "null argument");
   std::string c(calculator);
+  static const struct {
+    const char* name;
+    int potential;
+  } kPointGrid[] = {{"linRotCartSph_NoQuad_Alavi_SPCE", BSL_POT_POINT_ALAVI_SPCE},
+                    {"linRotCartSph_NoQuad_Alavi_TIP4P", BSL_POT_POINT_ALAVI_TIP4P},
+                    {"linRotCartSph_NoQuad_Coulomb", BSL_POT_COULOMB}};
+  for (const auto& e : kPointGrid)
+    if (c == e.name || c == std::string(e.name) + "_GB300") {
+      *potential = e.potential;
+      return BSL_OK;
+    }
   if (c == "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE" || c == "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE_GB300") {
     *potential = BSL_POT_ALAVI_SPCE;
     return BSL_OK;
@@ -611,7 +646,7 @@ int bsl_rigid_body_gradient(int potential, int nmol, const double* cm_ang, const
 int bsl_hv_prep_cage(const bsl_hv_params* params, int nmol, const double* cm_ang, const double* euler,
                      const double* q_site, const double* q_alavi, bsl_handle** out) {
   if (!params || !out || nmol < 1 || !cm_ang || !euler) return fail(BSL_ERR_INPUT, "bad arguments");
-  if (params->potential == BSL_POT_ISOHARMOSC) return fail(BSL_ERR_INPUT, "a cage needs an Alavi potential");
+  if (!has_cage(params->potential)) return fail(BSL_ERR_INPUT, "a cage needs an Alavi potential");
   Cage c;
   build_cage(params->potential, nmol, cm_ang, euler, q_site, &c);
   if (q_alavi) {

@@ -67,6 +67,16 @@ struct Cage {
   double q_h2_h = 0.4932, q_h2_cm = -0.9864;
 };
 
+// water model of the cage a potential reads (BSL_POT_ALAVI_SPCE or BSL_POT_ALAVI_TIP4P)
+inline int cage_model(int potential) {
+  return (potential == BSL_POT_ALAVI_TIP4P || potential == BSL_POT_POINT_ALAVI_TIP4P) ? BSL_POT_ALAVI_TIP4P
+                                                                                      : BSL_POT_ALAVI_SPCE;
+}
+inline bool has_cage(int potential) { return potential != BSL_POT_ISOHARMOSC && potential != BSL_POT_COULOMB; }
+inline bool point_grid_alavi(int potential) {
+  return potential == BSL_POT_POINT_ALAVI_SPCE || potential == BSL_POT_POINT_ALAVI_TIP4P;
+}
+
 // Sites of a cage of rigid waters (SPC/E: SPCE_AH2_EngRoutines.cpp:5-108; TIP4P:
 // TIP4P_AH2_EngRoutines.cpp getTIP4Patoms; rotmat.cpp:6-32); q_site (one per
 // site) may be null for the model's charges.
@@ -117,6 +127,7 @@ struct DeviceState {
   int* packed_of = nullptr;                        // full (l, m) index -> packed, -1 outside the block
   cudaStream_t copy_stream = nullptr;              // host-state step: second copy-in stream
   cudaEvent_t copy_done = nullptr;
+  cudaEvent_t vec_in = nullptr;                    // host-state step: vec is on the device
   double* ritz = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int red_blocks = 0;
@@ -143,6 +154,8 @@ namespace bsl {
 // ---- kernel launchers (bsl_kernels.cu) -----------------------------------
 int dev_potential_alavi(bsl_handle* h);
 int dev_potential_iso(bsl_handle* h);
+int dev_potential_point_alavi(bsl_handle* h);
+int dev_potential_coulomb(bsl_handle* h);
 int dev_vblocks(bsl_handle* h);
 int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s);
 // One Lanczos iteration on the packed state (vec, rvec) with the device

@@ -2,7 +2,9 @@
 //
 //   potential grid     V(x,y,z,theta,phi) for the Alavi H2 model in an SPC/E cage
 //                      (reference: potentialCalc/Alavi/AlaviGeneric/Alavi_ContGrid_H2_Routines.cpp:6-147)
-//                      or the isotropic oscillator (IsoHarmOsc_Routines.cpp:6-31), FP64
+//                      or the isotropic oscillator (IsoHarmOsc_Routines.cpp:6-31), FP64;
+//                      the point-grid Alavi H2 (Alavi_H2_Routines.cpp:5-276) and the
+//                      origin point charge (Coulomb_Routines.cpp:6-33)
 //   potential blocks   <lm|V|l'm'>(x,y,z) by the angular quadrature, sum-factorised over phi
 //                      (reference: HvCalc/NoQuadOnTheFly/ContinuousAngularGrid/linRotCartSphHvContGridRoutines.cpp:7-152)
 //   kinetic            sinc-DVR contractions along x, y (one plane per CTA) and z
@@ -18,6 +20,7 @@
 // consecutive threads (consecutive p) read consecutive addresses.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -59,8 +62,14 @@ __device__ __forceinline__ double coulomb(const double* sxyz, const double* sq, 
   return e;
 }
 
-__global__ void k_potential_cm(AtomSet atoms, const double* xg, const double* yg, const double* zg, int nx, int ny,
-                               long long npts, double* cm) {
+// Energy of one Alavi H2 charge site at every point of a grid (x fastest):
+// Coulomb with the site charge qsite, plus the Lennard-Jones term to the
+// oxygens for the centre of mass (with_lj).  The continuous-grid calculators
+// evaluate it at the basis grid (the centre of mass), the point-grid ones at
+// every point of the potential universe for both the centre of mass and the
+// H atoms (Alavi_SiteSite_Eng, Alavi_H2_Routines.cpp:197-276).
+__global__ void k_site_energy(AtomSet atoms, const double* xg, const double* yg, const double* zg, int nx, int ny,
+                              long long npts, double qsite, int with_lj, double* out) {
   __shared__ double sxyz[3 * kMaxAtoms], sq[kMaxAtoms];
   __shared__ int so[kMaxAtoms];
   for (int i = threadIdx.x; i < atoms.n; i += blockDim.x) {
@@ -75,14 +84,93 @@ __global__ void k_potential_cm(AtomSet atoms, const double* xg, const double* yg
   if (p >= npts) return;
   const int i = (int)(p % nx), j = (int)((p / nx) % ny), k = (int)(p / ((long long)nx * ny));
   const double x = xg[i], y = yg[j], z = zg[k];
-  double e = coulomb(sxyz, sq, atoms.n, atoms.q_cm, x, y, z);
-  double lj = 0.0;
-  for (int a = 0; a < atoms.n; ++a) {
-    if (!so[a]) continue;
-    const double r = dist(sxyz + 3 * a, x, y, z);
-    lj = __dadd_rn(lj, __dsub_rn(__ddiv_rn(atoms.lj_a, pow(r, 12.0)), __ddiv_rn(atoms.lj_b, pow(r, 6.0))));
+  double e = coulomb(sxyz, sq, atoms.n, qsite, x, y, z);
+  if (with_lj) {
+    double lj = 0.0;
+    for (int a = 0; a < atoms.n; ++a) {
+      if (!so[a]) continue;
+      const double r = dist(sxyz + 3 * a, x, y, z);
+      lj = __dadd_rn(lj, __dsub_rn(__ddiv_rn(atoms.lj_a, pow(r, 12.0)), __ddiv_rn(atoms.lj_b, pow(r, 6.0))));
+    }
+    e = __dadd_rn(e, lj);
   }
-  cm[p] = __dadd_rn(e, lj);
+  out[p] = e;
+}
+
+// The potential universe of the point-grid calculators (generateGrid,
+// potentialCalc/CommonRoutines/gridFcns.cpp:6-56): n[j] points with spacing
+// d[j] = grid_max / (n - 1) from gmin[j] = -grid_max / 2, x fastest (disp, :58-84).
+struct PointGrid {
+  int n[3];
+  double d[3], gmin[3];
+};
+
+// index of the universe point nearest to the numerator's coordinate: C round
+// (halves away from zero) of numerator / d, kept inside the universe
+// (AlaviMapH2GridToHGrid, Alavi_H2_Routines.cpp:5-52)
+__device__ __forceinline__ int nearest_index(double numerator, double d, int n) {
+  const int i = (int)round(__ddiv_rn(numerator, d));
+  return i <= 0 ? 0 : (i >= n ? n - 1 : i);
+}
+
+// Point-grid Alavi H2 (Alavi_H2_Eng_Point, Alavi_H2_Routines.cpp:136-195, in
+// calc_Vlmlpmp_NoQuad, HvCalc/NoQuadOnTheFly/linRotCartSphHvFullVPrepRoutines.cpp:126-177):
+// V = CM(nearest to the centre) + H(nearest to centre + d e) + H(nearest to
+// centre - d e), clipped at the ceiling; e = (sin t cos p, sin t sin p, cos t)
+// of each quadrature direction, both phi halves (edir: [half][a*nb+b][3]).
+// One thread per (point, theta_a, phi_b).
+__global__ void k_potential_point(const double* xg, const double* yg, const double* zg, int nx, int ny,
+                                  long long npts, int nab, PointGrid u, const double* edir, const double* cmpot,
+                                  const double* hpot, double hz, double ceiling, double* v1, double* v2) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npts * nab) return;
+  const long long p = t / nab;
+  const int ab = (int)(t % nab);
+  const int i = (int)(p % nx), j = (int)((p / nx) % ny), k = (int)(p / ((long long)nx * ny));
+  const double c[3] = {xg[i], yg[j], zg[k]};
+  int icm[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) icm[q] = nearest_index(__dsub_rn(c[q], u.gmin[q]), u.d[q], u.n[q]);
+  const double vcm = cmpot[icm[0] + (long long)u.n[0] * (icm[1] + (long long)u.n[1] * icm[2])];
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    const double* e = edir + ((long long)half * nab + ab) * 3;
+    double v = vcm;
+#pragma unroll
+    for (int site = 0; site < 2; ++site) {  // H1 at +d, H2 at -d along the axis
+      const double dist_h = site ? -hz : hz;
+      int ih[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        ih[q] = nearest_index(__dsub_rn(__dadd_rn(c[q], __dmul_rn(e[q], dist_h)), u.gmin[q]), u.d[q], u.n[q]);
+      v = __dadd_rn(v, hpot[ih[0] + (long long)u.n[0] * (ih[1] + (long long)u.n[1] * ih[2])]);
+    }
+    if (v >= ceiling) v = ceiling;
+    (half ? v2 : v1)[t] = v;
+  }
+}
+
+// Point charge at the origin seen by one on the H2 centre of mass
+// (CoulombPotential, potentialCalc/CoulombPotential/Coulomb_Routines.cpp:6-33,
+// CoulombEng, CommonRoutines/energyRoutines.cpp:5-26): V = (K q_c q_m) / |r|,
+// |V| > |c_ceil| -> c_ceil, then the HvInputFile ceiling; orientation
+// independent.
+__global__ void k_potential_coulomb(const double* xg, const double* yg, const double* zg, int nx, int ny,
+                                    long long npts, int nab, double kqq, double coulomb_ceiling, double ceiling,
+                                    double* v1, double* v2) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npts * nab) return;
+  const long long p = t / nab;
+  const int i = (int)(p % nx), j = (int)((p / nx) % ny), k = (int)(p / ((long long)nx * ny));
+  const double x = xg[i], y = yg[j], z = zg[k];
+  double s = __dmul_rn(x, x);
+  s = __dadd_rn(s, __dmul_rn(y, y));
+  s = __dadd_rn(s, __dmul_rn(z, z));
+  double v = __ddiv_rn(kqq, __dsqrt_rn(s));
+  if (fabs(v) > fabs(coulomb_ceiling)) v = coulomb_ceiling;
+  if (v >= ceiling) v = ceiling;
+  v1[t] = v;
+  v2[t] = v;
 }
 
 // one thread per (point, theta_a, phi_b): both phi halves
@@ -627,7 +715,7 @@ int dev_potential_alavi(bsl_handle* h) {
   const long long N = t.npts;
   const int nab = t.na * t.nb;
   double* cm = d.ukin;  // scratch of >= N doubles
-  k_potential_cm<<<grid_for(N), kThreads, 0, d.stream>>>(atoms, dx, dy, dz, t.nx, t.ny, N, cm);
+  k_site_energy<<<grid_for(N), kThreads, 0, d.stream>>>(atoms, dx, dy, dz, t.nx, t.ny, N, atoms.q_cm, 1, cm);
   k_potential_alavi<<<grid_for(N * nab), kThreads, 0, d.stream>>>(atoms, dx, dy, dz, t.nx, t.ny, N, nab, dh, cm,
                                                                   h->p.ceiling_potential, d.v1, d.v2);
   e = cudaGetLastError();
@@ -660,6 +748,106 @@ int dev_potential_iso(bsl_handle* h) {
   cudaFree(dz);
   if (e != cudaSuccess) return cuda_fail(e, "isotropic oscillator kernel launch");
   if (e2 != cudaSuccess) return cuda_fail(e2, "isotropic oscillator kernel");
+  return BSL_OK;
+}
+
+namespace {
+// device copies of host arrays, freed together
+struct Uploads {
+  std::vector<void*> ptrs;
+  ~Uploads() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  cudaError_t put(T** dst, const std::vector<T>& src) {
+    *dst = nullptr;
+    cudaError_t e = cudaMalloc((void**)dst, std::max<size_t>(1, src.size()) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    ptrs.push_back(*dst);
+    return src.empty() ? cudaSuccess : cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+  }
+};
+}  // namespace
+
+int dev_potential_point_alavi(bsl_handle* h) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  const bsl_hv_params& p = h->p;
+  const int natoms = (int)h->cage.q.size();
+  if (natoms > kMaxAtoms) return fail(BSL_ERR_UNSUPPORTED, "cage has more than 512 atoms");
+  // the potential universe (generateGrid, gridFcns.cpp:6-56)
+  PointGrid u;
+  const int un[3] = {p.pnx, p.pny, p.pnz};
+  const double umax[3] = {p.px_max, p.py_max, p.pz_max};
+  std::vector<double> ucoord[3];
+  long long usize = 1;
+  for (int q = 0; q < 3; ++q) {
+    u.n[q] = un[q];
+    u.d[q] = umax[q] / double(un[q] - 1);
+    u.gmin[q] = (-0.5) * umax[q];
+    usize *= un[q];
+    ucoord[q].resize(un[q]);
+    for (int i = 0; i < un[q]; ++i) ucoord[q][i] = (double(i) * u.d[q]) - (umax[q] / 2.0);
+  }
+  // H-H axis of every quadrature direction, phi in [0, pi) then [pi, 2 pi)
+  const int nab = t.na * t.nb;
+  std::vector<double> edir((size_t)2 * nab * 3);
+  for (int half = 0; half < 2; ++half)
+    for (int a = 0; a < t.na; ++a)
+      for (int b = 0; b < t.nb; ++b) {
+        const double ph = half ? t.phi2[b] : t.phi[b];
+        double* o = &edir[(((size_t)half * t.na + a) * t.nb + b) * 3];
+        o[0] = sin(t.theta[a]) * cos(ph);
+        o[1] = sin(t.theta[a]) * sin(ph);
+        o[2] = cos(t.theta[a]);
+      }
+  Uploads up;
+  double *dxyz, *dq, *de, *dx, *dy, *dz, *ux, *uy, *uz, *cm, *hp;
+  int* dis_o;
+  cudaError_t e;
+  if ((e = up.put(&dxyz, h->cage.xyz)) != cudaSuccess || (e = up.put(&dq, h->cage.q)) != cudaSuccess ||
+      (e = up.put(&dis_o, h->cage.is_o)) != cudaSuccess || (e = up.put(&de, edir)) != cudaSuccess ||
+      (e = up.put(&dx, t.xg)) != cudaSuccess || (e = up.put(&dy, t.yg)) != cudaSuccess ||
+      (e = up.put(&dz, t.zg)) != cudaSuccess || (e = up.put(&ux, ucoord[0])) != cudaSuccess ||
+      (e = up.put(&uy, ucoord[1])) != cudaSuccess || (e = up.put(&uz, ucoord[2])) != cudaSuccess ||
+      (e = up.put(&cm, std::vector<double>((size_t)usize))) != cudaSuccess ||
+      (e = up.put(&hp, std::vector<double>((size_t)usize))) != cudaSuccess)
+    return cuda_fail(e, "point-grid potential upload");
+  AtomSet atoms{dxyz, dq, dis_o, natoms, h->cage.q_h2_h, h->cage.q_h2_cm, h->cage.lj_a, h->cage.lj_b};
+  k_site_energy<<<grid_for(usize), kThreads, 0, d.stream>>>(atoms, ux, uy, uz, u.n[0], u.n[1], usize, atoms.q_cm, 1,
+                                                            cm);
+  k_site_energy<<<grid_for(usize), kThreads, 0, d.stream>>>(atoms, ux, uy, uz, u.n[0], u.n[1], usize, atoms.q_h, 0,
+                                                            hp);
+  const long long N = t.npts;
+  const double hz = 0.03707;  // H2_H1_Z = -H2_H2_Z, Alavi_Parameters.h:10-14, nm
+  k_potential_point<<<grid_for(N * nab), kThreads, 0, d.stream>>>(dx, dy, dz, t.nx, t.ny, N, nab, u, de, cm, hp, hz,
+                                                                  p.ceiling_potential, d.v1, d.v2);
+  e = cudaGetLastError();
+  const cudaError_t e2 = cudaStreamSynchronize(d.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "point-grid potential launch");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "point-grid potential kernel");
+  return BSL_OK;
+}
+
+int dev_potential_coulomb(bsl_handle* h) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  Uploads up;
+  double *dx, *dy, *dz;
+  cudaError_t e;
+  if ((e = up.put(&dx, t.xg)) != cudaSuccess || (e = up.put(&dy, t.yg)) != cudaSuccess ||
+      (e = up.put(&dz, t.zg)) != cudaSuccess)
+    return cuda_fail(e, "Coulomb potential upload");
+  const double kqq = kCoulombK * h->p.coulomb_centre_charge * h->p.coulomb_mol_charge;
+  const long long N = t.npts;
+  const int nab = t.na * t.nb;
+  k_potential_coulomb<<<grid_for(N * nab), kThreads, 0, d.stream>>>(dx, dy, dz, t.nx, t.ny, N, nab, kqq,
+                                                                    h->p.coulomb_ceiling, h->p.ceiling_potential,
+                                                                    d.v1, d.v2);
+  e = cudaGetLastError();
+  const cudaError_t e2 = cudaStreamSynchronize(d.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "Coulomb potential launch");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "Coulomb potential kernel");
   return BSL_OK;
 }
 

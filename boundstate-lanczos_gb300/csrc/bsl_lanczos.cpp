@@ -44,6 +44,7 @@ int ensure_staging(bsl_handle* h) {
   if (!d.copy_stream) {
     BSL_CUDA(cudaStreamCreateWithFlags(&d.copy_stream, cudaStreamNonBlocking));
     BSL_CUDA(cudaEventCreateWithFlags(&d.copy_done, cudaEventDisableTiming));
+    BSL_CUDA(cudaEventCreateWithFlags(&d.vec_in, cudaEventDisableTiming));
   }
   if (d.ref_vec) return BSL_OK;
   const size_t Df = (size_t)bsl_basis_size(h);
@@ -204,9 +205,14 @@ int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alph
   if ((rc = ensure_hist(h, 1)) || (rc = ensure_staging(h))) return rc;
   const size_t Df = (size_t)bsl_basis_size(h);
   cudaStream_t s = d.stream;
-  // vec feeds H v at once; rvec is copied in on a second stream meanwhile and
-  // only waited for where r += H v needs it
+  // vec feeds H v at once; rvec is copied in on a second stream while H v runs
+  // and only waited for where r += H v needs it.  The rvec copy starts after
+  // the vec copy has finished: both share the host link's bandwidth in one
+  // direction, and running them side by side would delay H v until both had
+  // arrived.
   BSL_CUDA(cudaMemcpyAsync(d.ref_vec, vec, Df * sizeof(double), cudaMemcpyHostToDevice, s));
+  BSL_CUDA(cudaEventRecord(d.vec_in, s));
+  BSL_CUDA(cudaStreamWaitEvent(d.copy_stream, d.vec_in, 0));
   BSL_CUDA(cudaMemcpyAsync(d.ref_out, rvec, Df * sizeof(double), cudaMemcpyHostToDevice, d.copy_stream));
   BSL_CUDA(cudaEventRecord(d.copy_done, d.copy_stream));
   BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));

@@ -24,8 +24,9 @@ struct GB300Storage {
 
 generalStor* bsl_reference_storage(const std::string& calculator) {
   int pot = 0;
-  if (calculator != "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE_GB300" &&
-      calculator != "linRotCartSph_NoQuad_IsoHarmOsc_GB300")
+  const std::string suffix = "_GB300";
+  if (calculator.size() <= suffix.size() ||
+      calculator.compare(calculator.size() - suffix.size(), suffix.size(), suffix) != 0)
     return nullptr;
   if (bsl_calculator_potential(calculator.c_str(), &pot) != BSL_OK) return nullptr;
   GB300Storage* s = new GB300Storage();
@@ -43,6 +44,10 @@ void Hv_Prep_linRotCartSph_NoQuad_GB300(int argc, char** argv, generalStor* gene
   if (p.potential == BSL_POT_ISOHARMOSC) {
     if (argc < 4) die("the oscillator needs argv[3]");
     if (bsl_parse_isoharmosc_input(argv[3], &p) != BSL_OK) die("IsoHarmOsc input");
+  }
+  if (p.potential == BSL_POT_COULOMB) {
+    if (argc < 4) die("the Coulomb potential needs argv[3]");
+    if (bsl_parse_coulomb_input(argv[3], &p) != BSL_OK) die("Coulomb input");
   }
   const char* prec = std::getenv("BSL_PRECISION");
   p.precision = (prec && std::strcmp(prec, "mixed") == 0) ? BSL_PREC_MIXED : BSL_PREC_FP64;

@@ -80,9 +80,12 @@ HV_KEYS = ["nx", "x_max(nm)", "ny", "y_max(nm)", "nz", "z_max(nm)", "l_max", "th
 
 
 def hv_fields(n, x_max, l_max, theta_points, phi_points, geometry, title, sym,
-              total_mass=2.01588, rot_const=0.709648713, ceiling=18.0):
-    """Field values in HvInputFile order for a cubic grid."""
-    return [n, x_max, n, x_max, n, x_max, l_max, theta_points, phi_points, n, x_max, n, x_max, n, x_max,
+              total_mass=2.01588, rot_const=0.709648713, ceiling=18.0, point_grid=None):
+    """Field values in HvInputFile order for a cubic grid.  point_grid = (points,
+    width) of the potential universe the point-grid calculators tabulate the H2
+    site energies on (default: the basis grid itself)."""
+    pn, pmax = point_grid if point_grid else (n, x_max)
+    return [n, x_max, n, x_max, n, x_max, l_max, theta_points, phi_points, pn, pmax, pn, pmax, pn, pmax,
             total_mass, rot_const, geometry, title, ceiling, "FALSE", sym]
 
 
@@ -110,6 +113,16 @@ def write_isoharmosc_input(path, mass, frequency, max_energy):
     with open(path, "w") as f:
         f.write("#\n#IsoHarmOsc input\n")
         f.write("mass(g/mol)= %r\nfrequency(1/ps)= %r\nmaxEnergy(kJ/mol)= %r\n" % (mass, frequency, max_energy))
+
+
+def write_coulomb_input(path, centre_charge, mol_charge, ceiling):
+    """Potential file read as argv[3] by the Coulomb calculator
+    (Coulomb_Routines.cpp:36-85): two comment lines, then the charge at the
+    origin, the charge on the H2 centre of mass (e) and the |V| ceiling (kJ/mol)."""
+    with open(path, "w") as f:
+        f.write("#\n#Coulomb input\n")
+        f.write("centreCharge(e)= %r\nmolCharge(e)= %r\ncoulombPotentialCeiling(kJ/mol)= %r\n"
+                % (centre_charge, mol_charge, ceiling))
 
 
 # The two workloads: a CPU-sized parity case and the full-size metric case.

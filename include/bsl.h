@@ -47,6 +47,13 @@ extern "C" {
 #define BSL_POT_ALAVI_SPCE 0  /* linRotCartSph_NoQuad_ContGrid_Alavi_SPCE */
 #define BSL_POT_ISOHARMOSC 1  /* linRotCartSph_NoQuad_IsoHarmOsc */
 #define BSL_POT_ALAVI_TIP4P 2 /* linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P */
+/* point-grid calculators: the H2 site energies are tabulated on the potential
+   universe grid (pointPotential_* fields) and read at the grid point nearest
+   to each site (Alavi_H2_Routines.cpp:136-195) */
+#define BSL_POT_POINT_ALAVI_SPCE 3  /* linRotCartSph_NoQuad_Alavi_SPCE */
+#define BSL_POT_POINT_ALAVI_TIP4P 4 /* linRotCartSph_NoQuad_Alavi_TIP4P */
+#define BSL_POT_COULOMB 5           /* linRotCartSph_NoQuad_Coulomb: a point charge at the
+                                       origin and one on the H2 centre of mass */
 
 /* arithmetic of the Hv application */
 #define BSL_PREC_FP64 0  /* every step in FP64 */
@@ -101,6 +108,9 @@ typedef struct bsl_hv_params {
   int keep_potential_grid; /* keep V(x,y,z,theta,phi) on the device after HvPrep
                               (needed by bsl_hf_gradient; otherwise released when
                               larger than 2^26 values) */
+  double coulomb_centre_charge; /* Coulomb input file (argv[3]), e */
+  double coulomb_mol_charge;
+  double coulomb_ceiling;       /* |V| > |ceiling| -> ceiling, kJ/mol */
 } bsl_hv_params;
 
 typedef struct bsl_handle bsl_handle;
@@ -116,6 +126,11 @@ int bsl_parse_hv_input(const char* path, bsl_hv_params* out);
 
 /* Parse the IsoHarmOsc potential file (IsoHarmOsc_Routines.cpp:41-58). */
 int bsl_parse_isoharmosc_input(const char* path, bsl_hv_params* inout);
+
+/* Parse the Coulomb potential file read as argv[3]: two comment lines, then
+   centreCharge, molCharge and the potential ceiling as key/value pairs
+   (potentialCalc/CoulombPotential/Coulomb_Routines.cpp:36-85). */
+int bsl_parse_coulomb_input(const char* path, bsl_hv_params* inout);
 
 /* Map an HvCalculator string (headLoop/InterfaceCode/interface.cpp:3-250) to
    BSL_POT_*; unknown names give BSL_ERR_INPUT. */

@@ -26,8 +26,13 @@ struct generalStor {
 };
 #endif
 
-/* Storage for one of the GB300 HvCalculators:
+/* Storage for one of the GB300 HvCalculators, the reference's NoQuad names
+   with the suffix "_GB300":
      "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE_GB300"
+     "linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P_GB300"
+     "linRotCartSph_NoQuad_Alavi_SPCE_GB300"
+     "linRotCartSph_NoQuad_Alavi_TIP4P_GB300"
+     "linRotCartSph_NoQuad_Coulomb_GB300"
      "linRotCartSph_NoQuad_IsoHarmOsc_GB300"
    Returns NULL for any other name.  The arithmetic is chosen by the
    environment variable BSL_PRECISION ("fp64", the default, or "mixed") and
@@ -36,7 +41,8 @@ generalStor* bsl_reference_storage(const std::string& calculator);
 
 /* Replaces Hv_Prep_linRotCartSph_NoQuad
    (Hv-calculators/linRotor/cartSphBasis/HvCalc/NoQuadOnTheFly/linRotCartSphHvFullVPrepRoutines.cpp:798-805):
-   reads argv[2] (HvInputFile) and, for the oscillator, argv[3]; sets
+   reads argv[2] (HvInputFile) and, for the oscillator and the Coulomb
+   potential, argv[3]; sets
    total_basis_size, sim_descr and sim_descr_short.  Errors print to cerr and
    exit(1), as the reference does. */
 void Hv_Prep_linRotCartSph_NoQuad_GB300(int argc, char** argv, generalStor* general_data, lanczosStor* lanczos_data);

@@ -175,7 +175,8 @@ double factorial(int n) {
 
 struct Model {
   HvInput in;
-  int potential_kind = 0;  // 0 Alavi SPC/E continuous grid, 1 IsoHarmOsc, 2 synthetic blocks
+  int potential_kind = 0;  // 0 Alavi SPC/E continuous grid, 1 IsoHarmOsc, 2 synthetic blocks,
+                           // 3 Alavi SPC/E point grid, 4 Coulomb
   double iso_factor = 0, iso_ceil = 0;
   int nn = 0;              // (l_max+1)^2
   std::vector<int> ql, qm; // n -> l, m
@@ -349,6 +350,101 @@ void build_potential_alavi(Model& M, int nthreads) {
       }
 }
 
+// calc_Vlmlpmp_NoQuad (HvCalc/NoQuadOnTheFly/linRotCartSphHvFullVPrepRoutines.cpp:126-177)
+// with Alavi_H2_Eng_Point (potentialCalc/Alavi/AlaviGeneric/Alavi_H2_Routines.cpp:136-195):
+// the centre-of-mass and H-atom site energies are tabulated on the potential
+// universe (preCalcPotential_Alavi / Alavi_SiteSite_Eng, :197-310; generateGrid,
+// CommonRoutines/gridFcns.cpp:6-56) and read at the universe point nearest to
+// each site (AlaviMapH2GridToHGrid, :5-52: round half away from zero, clamped).
+void build_potential_point_alavi(Model& M, int nthreads) {
+  HvInput& in = M.in;
+  int ni = in.nx, nj = in.ny, nk = in.nz, na = in.theta_points, nb = in.phi_points;
+  size_t np = (size_t)ni * nj * nk;
+  const int un[3] = {in.pnx, in.pny, in.pnz};
+  const double gm[3] = {in.px_max, in.py_max, in.pz_max};
+  double du[3];
+  for (int q = 0; q < 3; ++q) du[q] = gm[q] / (double(un[q] - 1));
+  size_t usize = (size_t)un[0] * un[1] * un[2];
+  std::vector<double> cmpot(usize), hpot(usize);
+#pragma omp parallel for schedule(guided) num_threads(nthreads)
+  for (long u = 0; u < (long)usize; ++u) {
+    const int ix = u % un[0], iy = (u / un[0]) % un[1], iz = u / ((size_t)un[0] * un[1]);
+    double g[3] = {(double(ix) * du[0]) - (gm[0] / 2.0), (double(iy) * du[1]) - (gm[1] / 2.0),
+                   (double(iz) * du[2]) - (gm[2] / 2.0)};
+    double c = 0.0;
+    c += coulomb_sum(g, kQ_H2_CM, M.cage);
+    c += lj_sum(g, M.cage);
+    cmpot[u] = c;
+    double h = 0.0;
+    h += coulomb_sum(g, kQ_H2_H, M.cage);
+    hpot[u] = h;
+  }
+  auto nearest = [&](double numerator, int q) {
+    int i = (int)round(numerator / du[q]);
+    if (i <= 0) i = 0;
+    else if (i >= un[q]) i = un[q] - 1;
+    return i;
+  };
+  auto at = [&](const int* idx) { return (size_t)idx[0] + (size_t)un[0] * (idx[1] + (size_t)un[1] * idx[2]); };
+  M.V1.assign(np * na * nb, 0.0);
+  M.V2.assign(np * na * nb, 0.0);
+  double ceil_v = in.ceiling;
+#pragma omp parallel for schedule(guided) num_threads(nthreads)
+  for (long p = 0; p < (long)np; ++p) {
+    int i = p / ((size_t)nj * nk), j = (p / nk) % nj, k = p % nk;
+    const double c[3] = {M.xgrid[i], M.ygrid[j], M.zgrid[k]};
+    for (int a = 0; a < na; a++)
+      for (int b = 0; b < nb; b++)
+        for (int half = 0; half < 2; ++half) {
+          const double th = M.theta[a], ph = half ? M.phi2[b] : M.phi[b];
+          const double e[3] = {sin(th) * cos(ph), sin(th) * sin(ph), cos(th)};
+          int icm[3], ih1[3], ih2[3];
+          for (int q = 0; q < 3; ++q) {
+            const double grid_min = (-0.5) * gm[q];
+            icm[q] = nearest(c[q] - grid_min, q);
+            ih1[q] = nearest(c[q] + e[q] * kH2_H1_Z - grid_min, q);
+            ih2[q] = nearest(c[q] + e[q] * (-kH2_H1_Z) - grid_min, q);
+          }
+          double v = 0.0;
+          v += cmpot[at(icm)];
+          v += hpot[at(ih1)];
+          v += hpot[at(ih2)];
+          if (v >= ceil_v) v = ceil_v;
+          (half ? M.V2 : M.V1)[((size_t)p * na + a) * nb + b] = v;
+        }
+  }
+}
+
+// calc_Vlmlpmp_NoQuad with CoulombPotential
+// (potentialCalc/CoulombPotential/Coulomb_Routines.cpp:6-33, CoulombEng,
+// CommonRoutines/energyRoutines.cpp:5-26): V = K q_c q_m / |r| for a charge at
+// the origin, |V| > |c| -> c, then the HvInputFile ceiling.
+void build_potential_coulomb(Model& M, double qc, double qm, double c_ceil) {
+  HvInput& in = M.in;
+  int ni = in.nx, nj = in.ny, nk = in.nz, na = in.theta_points, nb = in.phi_points;
+  size_t np = (size_t)ni * nj * nk;
+  M.V1.assign(np * na * nb, 0.0);
+  M.V2.assign(np * na * nb, 0.0);
+  for (int i = 0; i < ni; ++i)
+    for (int j = 0; j < nj; ++j)
+      for (int k = 0; k < nk; ++k) {
+        double x = M.xgrid[i], y = M.ygrid[j], z = M.zgrid[k];
+        double d2 = 0.;
+        d2 += x * x;
+        d2 += y * y;
+        d2 += z * z;
+        double v = kK * qc * qm / sqrt(d2);
+        if (fabs(v) > fabs(c_ceil)) v = c_ceil;
+        if (v >= in.ceiling) v = in.ceiling;
+        size_t p = ((size_t)i * nj + j) * nk + k;
+        for (int a = 0; a < na; ++a)
+          for (int b = 0; b < nb; ++b) {
+            M.V1[(p * na + a) * nb + b] = v;
+            M.V2[(p * na + a) * nb + b] = v;
+          }
+      }
+}
+
 // calc_Vlmlpmp_NoQuad with IsoHarmOscEng: V = 0.5 m w^2 |r|^2, clipped first by
 // the oscillator's own ceiling (|V| > |c| -> c) and then by the HvInputFile
 // ceiling (V >= c -> c).
@@ -456,8 +552,10 @@ extern "C" {
 
 const char* orc_last_error() { return g_err.c_str(); }
 
-// calculator: "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE" or
-// "linRotCartSph_NoQuad_IsoHarmOsc".  extra_input: IsoHarmOsc parameter file.
+// calculator: "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE",
+// "linRotCartSph_NoQuad_Alavi_SPCE", "linRotCartSph_NoQuad_Coulomb" or
+// "linRotCartSph_NoQuad_IsoHarmOsc".  extra_input: the IsoHarmOsc or Coulomb
+// parameter file (argv[3]).
 void* orc_create(const char* calculator, const char* hv_input, const char* extra_input, int nthreads) {
   Model* M = new Model();
   if (!read_hv_input(hv_input, &M->in)) { delete M; return nullptr; }
@@ -467,6 +565,20 @@ void* orc_create(const char* calculator, const char* hv_input, const char* extra
     if (!read_cage(M->in.geometry, &M->cage)) { delete M; return nullptr; }
     M->potential_kind = 0;
     build_potential_alavi(*M, nthreads);
+  } else if (calc == "linRotCartSph_NoQuad_Alavi_SPCE") {
+    if (!read_cage(M->in.geometry, &M->cage)) { delete M; return nullptr; }
+    M->potential_kind = 3;
+    build_potential_point_alavi(*M, nthreads);
+  } else if (calc == "linRotCartSph_NoQuad_Coulomb") {
+    std::ifstream f(extra_input ? extra_input : "");
+    if (!f.is_open()) { g_err = "cannot open Coulomb input"; delete M; return nullptr; }
+    std::string line, junk;
+    double qc, qm, c_ceil;
+    std::getline(f, line);
+    std::getline(f, line);
+    f >> junk >> qc >> junk >> qm >> junk >> c_ceil;
+    M->potential_kind = 4;
+    build_potential_coulomb(*M, qc, qm, c_ceil);
   } else if (calc == "linRotCartSph_NoQuad_IsoHarmOsc") {
     std::ifstream f(extra_input ? extra_input : "");
     if (!f.is_open()) { g_err = "cannot open IsoHarmOsc input"; delete M; return nullptr; }

@@ -127,17 +127,21 @@ def read_boundstates(path):
     return np.array([[float(x) for x in l.split()[1:3]] for l in lines if l.strip()])
 
 
-CASES = ["cage11_n10_l3_all", "seed1_n6_l3_odd", "seed0_n5_l4_even", "iso_n20_l2_all"]
+CASES = ["cage11_n10_l3_all", "seed1_n6_l3_odd", "seed0_n5_l4_even", "iso_n20_l2_all", "point_cage11_n10_l2_odd",
+         "coulomb_n9_l2_all"]
 # cases whose fixtures come from the compiled reference but that the CPU oracle
 # restatement does not cover (other water models of the same path)
-REF_ONLY_CASES = ["tip4p_seed1_n6_l3_odd"]
+REF_ONLY_CASES = ["tip4p_seed1_n6_l3_odd", "point_tip4p_seed1_n6_l3_odd"]
 
 
 def case_info(name):
     import json
     man = json.load(open(os.path.join(GOLDEN, "manifest.json")))[name]
     d = os.path.join(GOLDEN, name)
-    extra = "iso_input.txt" if os.path.exists(os.path.join(d, "iso_input.txt")) else None
+    extra = None
+    for f in ("iso_input.txt", "coulomb_input.txt"):  # the potential file the reference reads as argv[3]
+        if os.path.exists(os.path.join(d, f)):
+            extra = f
     return d, man, extra
 
 

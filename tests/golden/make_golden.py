@@ -41,8 +41,13 @@ _spec.loader.exec_module(inputs)
 CONTGRID = "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE"
 CONTGRID_TIP4P = "linRotCartSph_NoQuad_ContGrid_Alavi_TIP4P"
 ISO = "linRotCartSph_NoQuad_IsoHarmOsc"
+POINT = "linRotCartSph_NoQuad_Alavi_SPCE"
+POINT_TIP4P = "linRotCartSph_NoQuad_Alavi_TIP4P"
+COULOMB = "linRotCartSph_NoQuad_Coulomb"
 
 # name: (calculator, n, x_max, l_max, theta, phi, sym, geometry, niter, hv_full, iso)
+# iso: the IsoHarmOsc file values, or ("coulomb", centre charge, molecule charge, ceiling),
+# or ("point", universe points, universe width) for the point-grid calculators
 CASES = {
     # the stored 2013-09-03 10^3 l3 runs (inputs identical to the reference's own)
     "cage11_n10_l3_all": (CONTGRID, 10, 0.4, 3, 10, 10, "All", "cage11.xyz", 300, True, None),
@@ -56,6 +61,13 @@ CASES = {
     "cpu_workload": (CONTGRID, 15, 0.08, 4, 12, 12, "Even", "cage_seed0.xyz", 600, False, None),
     # the same continuous-grid path with TIP4P water
     "tip4p_seed1_n6_l3_odd": (CONTGRID_TIP4P, 6, 0.08, 3, 8, 7, "Odd", "cage_seed1.xyz", 200, True, None),
+    # point-grid Alavi SPC/E with the inputs of the reference's stored 2013-08-30 15:06 run
+    "point_cage11_n10_l2_odd": (POINT, 10, 0.4, 2, 10, 10, "Odd", "cage11.xyz", 300, True, ("point", 20, 0.48)),
+    # point-grid Alavi TIP4P, universe finer than the basis grid
+    "point_tip4p_seed1_n6_l3_odd": (POINT_TIP4P, 6, 0.08, 3, 8, 7, "Odd", "cage_seed1.xyz", 200, True,
+                                    ("point", 13, 0.1)),
+    # charge at the origin (an odd grid has a point there: 1/0 is clipped)
+    "coulomb_n9_l2_all": (COULOMB, 9, 0.3, 2, 4, 4, "All", "NULL", 300, True, ("coulomb", 0.1, -0.1, -20.0)),
 }
 
 
@@ -78,7 +90,7 @@ def run_ref_lanczos(case_dir, calc, extra):
     lz = os.path.join(tmp, "lanczos_input.txt")
     txt = open(lz).read().replace("OutputDirectoryPath= ./", "OutputDirectoryPath= %s/out_" % tmp)
     open(lz, "w").write(txt)
-    args = [REF_BIN, "lanczos_input.txt", "hv_input.txt"] + (["iso_input.txt"] if extra else [])
+    args = [REF_BIN, "lanczos_input.txt", "hv_input.txt"] + ([extra] if extra else [])
     log = subprocess.run(args, cwd=tmp, capture_output=True, text=True, check=True).stdout
     ab = [l.split() for l in log.splitlines() if re.match(r"^\d+ \S+ \S+$", l)]
     alpha = np.array([float(x[1]) for x in ab])
@@ -104,19 +116,24 @@ def main():
         os.makedirs(d, exist_ok=True)
         if geo != "NULL":
             shutil.copy(os.path.join(HERE, geo), os.path.join(d, geo))
-        if calc == CONTGRID and name.startswith("cage11"):
-            vals = inputs.hv_fields(n, xm, lmax, th, ph, geo, "SmallBasisTest2", sym, rot_const=0.7096487130193394)
+        point = iso[1:] if iso and iso[0] == "point" else None
+        if name.startswith("cage11") or name == "point_cage11_n10_l2_odd":
+            vals = inputs.hv_fields(n, xm, lmax, th, ph, geo, "SmallBasisTest2", sym, rot_const=0.7096487130193394,
+                                    point_grid=point)
         else:
-            vals = inputs.hv_fields(n, xm, lmax, th, ph, geo, name, sym)
-        if iso:
+            vals = inputs.hv_fields(n, xm, lmax, th, ph, geo, name, sym, point_grid=point)
+        if calc == ISO:
             vals[16] = 0.709652722117881
             vals[19] = 100.0
         inputs.write_hv_input(os.path.join(d, "hv_input.txt"), vals)
         inputs.write_lanczos_input(os.path.join(d, "lanczos_input.txt"), niter, calc)
         extra = None
-        if iso:
+        if calc == ISO:
             inputs.write_isoharmosc_input(os.path.join(d, "iso_input.txt"), *iso)
             extra = "iso_input.txt"
+        elif calc == COULOMB:
+            inputs.write_coulomb_input(os.path.join(d, "coulomb_input.txt"), *iso[1:])
+            extra = "coulomb_input.txt"
         cwd = os.getcwd()
         os.chdir(d)
         try:
@@ -140,7 +157,8 @@ def main():
         return
     # the reference's own stored 2013 runs that the final tree reproduces
     stored = {}
-    for run in ("SmallBasisTest2_2013-09-03_18_36_00", "SmallBasisTest2_2013-09-03_19_06_47"):
+    for run in ("SmallBasisTest2_2013-09-03_18_36_00", "SmallBasisTest2_2013-09-03_19_06_47",
+                "SmallBasisTest2_2013-08-30_15_06_49"):
         lines = open(os.path.join(REF, "Compilation", run, "boundstates.txt")).read().split("\n")[4:]
         vals = [[float(x) for x in l.split()[1:3]] for l in lines if l.strip()]
         niter = int(re.search(r"numberOfIterations= (\d+)",

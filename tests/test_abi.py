@@ -76,8 +76,33 @@ def test_parse_errors(bsl, tmp_path, in_case_dir):
         bsl.hv_interface_setup("linRotCartSph_NoSuchCalculator")
 
 
+def test_calculator_strings_and_coulomb_input(bsl, tmp_path):
+    """Every NoQuad HvCalculator string of the reference registry
+    (interface.cpp:90-246), with and without the _GB300 suffix, maps to its
+    potential; the Coulomb potential file (argv[3]) is read in token order."""
+    import ctypes as C
+    L = bsl.lib()
+    for name, pot in bsl.CALCULATORS.items():
+        out = C.c_int(-1)
+        assert L.bsl_calculator_potential(name.encode(), C.byref(out)) == bsl.OK, name
+        assert out.value == pot, name
+    for base, pot in (("linRotCartSph_NoQuad_Alavi_SPCE", bsl.POT_POINT_ALAVI_SPCE),
+                      ("linRotCartSph_NoQuad_Alavi_TIP4P", bsl.POT_POINT_ALAVI_TIP4P),
+                      ("linRotCartSph_NoQuad_Coulomb", bsl.POT_COULOMB)):
+        assert bsl.CALCULATORS[base] == bsl.CALCULATORS[base + "_GB300"] == pot
+    d, man, extra = case_info("coulomb_n9_l2_all")
+    p = bsl.HvParams()
+    assert L.bsl_parse_coulomb_input(os.path.join(d, extra).encode(), C.byref(p)) == bsl.OK
+    assert (p.coulomb_centre_charge, p.coulomb_mol_charge, p.coulomb_ceiling) == (0.1, -0.1, -20.0)
+    assert p.potential == bsl.POT_COULOMB
+    bad = tmp_path / "c.txt"
+    bad.write_text("#\n#\ncentreCharge= 1.0\n")
+    assert L.bsl_parse_coulomb_input(str(bad).encode(), C.byref(p)) == bsl.ERR_INPUT
+
+
 @pytest.mark.parametrize("name", ["cage11_n10_l3_all", "seed1_n6_l3_odd", "seed0_n5_l4_even", "iso_n20_l2_all",
-                                  "cpu_workload", "tip4p_seed1_n6_l3_odd"])
+                                  "cpu_workload", "tip4p_seed1_n6_l3_odd", "point_cage11_n10_l2_odd",
+                                  "point_tip4p_seed1_n6_l3_odd", "coulomb_n9_l2_all"])
 def test_tail_matches_oracle(bsl, name):
     d, man, _ = case_info(name)
     ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))
@@ -148,7 +173,8 @@ def _lanczos_limits(d):
 
 
 @pytest.mark.parametrize("name", ["cage11_n10_l3_all", "seed1_n6_l3_odd", "seed0_n5_l4_even", "iso_n20_l2_all",
-                                  "cpu_workload", "tip4p_seed1_n6_l3_odd"])
+                                  "cpu_workload", "tip4p_seed1_n6_l3_odd", "point_cage11_n10_l2_odd",
+                                  "point_tip4p_seed1_n6_l3_odd", "coulomb_n9_l2_all"])
 def test_boundstates_file_matches_reference(bsl, name, tmp_path):
     """boundstates.txt written from the tail on the reference's alpha/beta has the
     reference's layout, states and eigenvalues (the stored alpha/beta are the

@@ -175,3 +175,20 @@ def test_hf_gradient_tip4p(bsl):
     eq[9, 2] -= h
     f = (lev(cm, ep, q4)[0] - lev(cm, eq, q4)[0]) / (2 * h)
     assert np.allclose(dea[:, 9, 2], f, rtol=2e-4, atol=2e-5), (dea[:, 9, 2], f)
+
+
+def test_hf_gradient_needs_continuous_grid(bsl):
+    """The point-grid potentials are piecewise constant in the cage coordinates:
+    the derivative entry point refuses them instead of returning zeros."""
+    d, man, extra = case_info("point_cage11_n10_l2_odd")
+    cwd = os.getcwd()
+    os.chdir(d)
+    try:
+        h = bsl.Hamiltonian("hv_input.txt", man["calculator"], extra_input=extra)
+    finally:
+        os.chdir(cwd)
+    psi = np.random.default_rng(0).standard_normal((1, h.basis_size))
+    with pytest.raises(bsl.BslError) as e:
+        h.hf_gradient(psi, 60)
+    assert e.value.code == bsl.ERR_UNSUPPORTED
+    h.close()

@@ -89,8 +89,12 @@ def test_hv_mixed_engines_match_fp64(bsl, name):
     h.close()
 
 
-@pytest.mark.parametrize("name", ["cage11_n10_l3_all", "seed1_n6_l3_odd"])
+@pytest.mark.parametrize("name", ["cage11_n10_l3_all", "seed1_n6_l3_odd", "point_cage11_n10_l2_odd",
+                                  "coulomb_n9_l2_all"])
 def test_potential_grid_and_blocks_match_oracle(bsl, name):
+    """V(x, y, z, theta, phi) and the V blocks against the oracle; for the point
+    grid every value is a table lookup, so a nearest-point index that differed
+    from the reference's would show as an O(1) error here."""
     h, d, man, extra = make(bsl, name)
     cwd = os.getcwd()
     os.chdir(d)

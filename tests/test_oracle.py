@@ -80,6 +80,48 @@ def test_oracle_tail_reproduces_stored_2013_run():
     assert np.max(np.abs(bs[:, 0] - ev)) <= 1e-13
 
 
+def test_oracle_point_grid_reproduces_stored_2013_run():
+    """Point-grid Alavi SPC/E (linRotCartSph_NoQuad_Alavi_SPCE): the reference's
+    alpha/beta (final tree) through the oracle tail reproduce the reference's
+    own stored 2013-08-30 15:06 run (same inputs) on its converged levels, and
+    the final tree's boundstates.txt agrees with the stored one there."""
+    stored = json.load(open(os.path.join(GOLDEN, "stored_2013_runs.json")))["SmallBasisTest2_2013-08-30_15_06_49"]
+    d = os.path.join(GOLDEN, "point_cage11_n10_l2_odd")
+    ref = np.load(os.path.join(d, "ref_alpha_beta.npz"))
+    assert len(ref["alpha"]) == stored["niter"]
+    b = np.concatenate([[0.0], ref["beta"]])
+    ev, er = oracle_lancbis(ref["alpha"], b, b * b)
+    levels = np.array(stored["levels"])
+    conv = levels[levels[:, 1] < 1e-8]
+    assert len(conv) >= 10
+    for e, _ in conv:
+        assert np.min(np.abs(ev - e)) <= 5e-12, e
+    bs = read_boundstates(os.path.join(d, "ref_boundstates.txt"))
+    assert len(bs) == len(ev) == len(levels)
+    assert np.max(np.abs(bs[:, 0] - ev)) <= 1e-13
+
+
+def test_oracle_coulomb_is_orientation_independent():
+    """The Coulomb calculator's V does not depend on the H2 orientation, so its
+    V blocks are diagonal in (l, m) (orthonormal tesseral harmonics on the
+    exact quadrature) and the origin point, where 1/|r| is infinite, carries
+    the clipped value."""
+    d, man, extra = case_info("coulomb_n9_l2_all")
+    cwd = os.getcwd()
+    os.chdir(d)
+    try:
+        m = OracleModel(man["calculator"], "hv_input.txt", extra)
+        v1, v2 = m.vgrid()
+        blocks = m.vblocks()
+    finally:
+        os.chdir(cwd)
+    nn = m.nn
+    b = blocks.reshape(-1, nn, nn)
+    off = b - np.einsum("pi,ij->pij", np.einsum("pii->pi", b), np.eye(nn))
+    assert np.max(np.abs(off)) <= 1e-12 * np.max(np.abs(b))
+    assert np.min(v1) == -20.0 and np.array_equal(v1, v2)
+
+
 def test_oracle_isoharmosc_analytic():
     """IsoHarmOsc levels = hbar w (n + 3/2) + B l(l+1) up to the DVR error."""
     d, man, extra = case_info("iso_n20_l2_all")
