@@ -5,38 +5,44 @@
 // Reference: Tv_5D_oneCompositeIndex / Mv_5D_oneCompositeIndex,
 // Hv-calculators/linRotor/cartSphBasis/HvCalc/linRotCartSphHvRoutines.cpp:1807-1969.
 //
-// Products (M = 128 rows, N = 64 output columns, K = 64):
-//   x and y, one (y, x) plane of fixed (s, z) per batch: rows 0-63 are the rows of
-//   the plane (D[y][x] = sum_q v(y, q) Tx[x][q]) and rows 64-127 its columns
-//   (D[64 + x][y] = sum_q v(q, x) Ty[y][q]), so both directions of one plane
-//   come out of one set of accumulators (the y part is transposed through
-//   shared memory before the coalesced store);
-//   z, two (z, x) planes of fixed (s, y) per batch: rows (p, x) are the columns
-//   of the planes (D[(p, x)][z] = sum_q v(p, q, x) Tz[z][q]).
+// Work unit: a pair of planes.  The accumulator D has M = 128 rows (p, x) --
+// plane p of the pair, grid column x -- and N = 64 columns (the other in-plane
+// index), K = 64 per contraction:
+//   x and y (k_kin_xy_tc), planes (y, x) of fixed (s, z); both directions
+//     accumulate into the same D[(p, x)][y]:
+//       y:  sum_q v_p(q, x) Ty[y][q]      A = v tile read MN-major, B = T
+//       x:  sum_q Tx[x][q] v_p(y, q)      A = diag(Tx, Tx) over K = (p', q), B = v tile
+//     (the block-diagonal A is two 128-row tiles [T; 0] and [0; T] made from the
+//     T tile and zero tiles laid out around it);
+//   z (k_kin_z_tc), planes (z, x) of fixed (s, y):
+//       sum_q v_p(q, x) Tz[z][q]           A = v tile read MN-major, B = T
+//     and the result is added to the x/y result.
+// Every v tile is stored once, row by row as it lies in memory (64 FP16 per
+// 128-byte swizzled row), and read by both terms; the output rows of D are
+// grid columns, so the epilogue's stores are coalesced along x.
 //
 // Exactness (error-free slicing after Ozaki, Ogita, Oishi and Rump,
-// Numer. Algorithms 59, 2012, here with 9-bit fixed-point slices): the values of
-// the double-float Lanczos vector are scaled by a power of two to below 1 in
-// magnitude -- one scale per (y, x) plane for x and y, one per operand row for
-// z -- and cut into four 9-bit signed integer slices,
+// Numer. Algorithms 59, 2012, here with 9-bit fixed-point slices): each plane
+// of the double-float Lanczos vector is scaled by a power of two to below 1 in
+// magnitude and cut into four 9-bit signed integer slices,
 // v = 2^(e - 8) (a1 + 2^-9 a2 + 2^-18 a3 + 2^-27 a4) (36 bits relative to the
-// scale's maximum: far below the FP32 noise of the potential apply); T is
-// scaled from its largest element and cut into four slices the same way,
-// rounded to nearest so that the symmetric T stays exactly symmetric (a
-// Lanczos recurrence on a non-symmetric H scatters the converged copies of a
-// level).  The slices are
-// integers in [-256, 256], exact in FP16, their products are exact, and every
-// partial sum of one product class (at most 4 products of 64 terms) is an
-// integer of magnitude at most 2^24: the FP32 accumulation in tensor memory is
-// exact whatever its internal rounding, so the result carries no accumulation
-// bias.  The products of each scale class k + l <= 3 share one accumulator and
-// the four classes are combined on the CUDA cores into a double-float pair.
-// The rounding of T is the same along each Toeplitz diagonal and adds up
-// coherently for smooth states: with 36 bits it shifts levels by ~1e-7 kJ/mol
-// per axis.
+// plane's maximum); T is scaled from its largest element and cut the same way,
+// rounded to nearest so that the symmetric T stays exactly symmetric.  The
+// slices are integers in [-256, 256], exact in FP16, their products are exact,
+// and the products of each scale class k + l <= 3 (10 products) share one
+// accumulator.  A class sum is bounded by 2 * sum_{k+l=c} 256 max_x sum_q |b_l[x][q]|,
+// below 2^23.6 for the sinc-DVR T (its first slice decays as 1/(x - q)^2), so
+// the FP32 accumulation in tensor memory is exact whatever its internal
+// rounding.  The four classes are combined on the CUDA cores into a
+// double-float pair.
 //
-// Pipeline: persistent CTAs, two per SM with 256 tensor-memory columns each, so
-// that one CTA slices or finishes its epilogue while the other's products run.
+// Pipeline: one persistent CTA per SM with three roles.  Eight producer warps
+// load a plane pair, find each plane's scale and write the slices into one of
+// two 64 KiB shared-memory stages; one thread issues the pair's 120 (x/y) or
+// 40 (z) MMAs into one of two 256-column accumulator stages; eight epilogue
+// warps read the finished accumulators and store (x/y) or add (z) the
+// double-float results.  mbarriers hand the stages over; every wait is bounded
+// and a timeout sets status[3].
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -49,14 +55,19 @@
 namespace bsl {
 namespace {
 
-constexpr int kVS = 4;                       // slices of v
-constexpr int kTS = 4;                       // slices of T
-constexpr uint32_t kTileA = 128 * 128;       // 16 KiB: 128 rows x 64 FP16 (one 128-byte swizzle atom per row)
-constexpr uint32_t kTileB = 64 * 128;        // 8 KiB
-constexpr uint32_t kBatchA = kVS * kTileA;   // operand slices of one batch
-constexpr uint32_t kCols = 4 * 64;           // accumulator columns of one batch (classes 0..3)
-constexpr int kTcThreads = 256;       // threads per CTA
-constexpr int kPairs = 10;                   // slice products (k, l) with k + l <= 3, by class
+constexpr int kVS = 4;                        // slices of v
+constexpr int kTS = 4;                        // slices of T
+constexpr uint32_t kTile = 64 * 128;          // 8 KiB: 64 rows x 64 FP16, one 128-byte swizzled row each
+constexpr uint32_t kStage = kVS * 2 * kTile;  // v slices of a plane pair: [slice][plane] tiles
+constexpr int kStages = 2;                    // shared-memory stages and accumulator stages
+constexpr uint32_t kAccCols = 4 * 64;         // accumulator columns of one pair (classes 0..3)
+constexpr int kEpiWarps = 8;                  // warps 0-7
+constexpr int kProdWarps = 8;                 // warps 8-15
+constexpr int kMmaWarp = kEpiWarps + kProdWarps;  // warp 16: MMA issue and tensor-memory owner
+constexpr int kWsThreads = (kMmaWarp + 1) * 32;
+constexpr int kProdThreads = kProdWarps * 32;
+constexpr int kEpiThreads = kEpiWarps * 32;
+constexpr int kPairs = 10;  // slice products (k, l) with k + l <= 3, by class
 __constant__ int8_t c_pk[kPairs] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
 __constant__ int8_t c_pl[kPairs] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
 __constant__ int8_t c_first[kPairs] = {1, 1, 0, 1, 0, 0, 1, 0, 0, 0};
@@ -74,7 +85,7 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~(uintptr_t)1023);
 }
 
-// byte offset of element k (a multiple of 4) of row r in an SW128 K-major tile with K = 64 FP16
+// byte offset of element k (a multiple of 4) of row r in an SW128 tile of 64 FP16 per row
 __device__ __forceinline__ uint32_t quad_offset(int r, int k) {
   return (uint32_t)(r * 128 + (((k >> 3) ^ (r & 7)) << 4) + ((k & 7) << 1));
 }
@@ -106,21 +117,6 @@ __device__ __forceinline__ void slice4(float yh, float yl, float (&a)[kVS]) {
   a[3] = rintf(r);
 }
 
-// D_c += A_k B_l^T for the slice products, class c in accumulator columns [64 c, 64 c + 64)
-__device__ __forceinline__ void issue_products(uint32_t d, uint32_t a, uint32_t b) {
-  const uint32_t idesc = tc::idesc_f16(128, 64);
-#pragma unroll 1
-  for (int pr = 0; pr < kPairs; ++pr) {
-    const int k = c_pk[pr], l = c_pl[pr];
-    const uint32_t dc = d + (uint32_t)(k + l) * 64u;
-    const bool first = c_first[pr] != 0;
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-      tc::mma_f16(dc, tc::sw128_desc(a + (uint32_t)k * kTileA + (uint32_t)s * 32u),
-                  tc::sw128_desc(b + (uint32_t)l * kTileB + (uint32_t)s * 32u), idesc, (first && s == 0) ? 0u : 1u);
-  }
-}
-
 // the four class accumulators of 8 consecutive columns combined into
 // double-float pairs and multiplied by `scale` (a power of two).  The classes
 // are exact integers below 2^24: the head is c0 + 2^-9 c1 with its rounding
@@ -143,347 +139,257 @@ __device__ __forceinline__ void load_pairs8(uint32_t taddr, float scale, float2 
   }
 }
 
-__device__ __forceinline__ void load_b(uint8_t* B, const uint16_t* src) {
-  for (int e = threadIdx.x; e < kTS * 64 * 16; e += kTcThreads) {  // kTS tiles of 64 rows x 16 quads
-    const int l = e >> 10, r = (e >> 4) & 63, q = (e & 15) * 4;
-    *reinterpret_cast<uint2*>(B + l * kTileB + quad_offset(r, q)) =
-        *reinterpret_cast<const uint2*>(src + ((size_t)l * 64 + r) * 64 + q);
-  }
-}
-
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-
-
-// Column maxima of the same blocks through shared memory (part: [16][64]
-// partials, then [64] maxima).  Contains two __syncthreads.
-__device__ __forceinline__ void block_col_max(const float2 (&x)[4][4], float* part, int bj, int bi, float (&cm)[4]) {
-#pragma unroll
-  for (int c = 0; c < 4; ++c)
-    part[bj * 64 + 4 * bi + c] =
-        fmaxf(fmaxf(fabsf(x[0][c].x), fabsf(x[1][c].x)), fmaxf(fabsf(x[2][c].x), fabsf(x[3][c].x)));
-  __syncthreads();
-  if (threadIdx.x < 64) {
-    float m = 0.f;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) m = fmaxf(m, part[q * 64 + threadIdx.x]);
-    part[16 * 64 + threadIdx.x] = m;
+// Plane geometry: x/y planes are the contiguous (y, x) planes of fixed (s, z);
+// z planes are the (z, x) planes of fixed (s, y), rows nx * ny apart.
+template <bool kXY>
+struct Planes {
+  int nx, ny, nz, nplanes;
+  __device__ __forceinline__ long long base(int plane) const {
+    if (kXY) return (long long)plane * nx * ny;
+    return (long long)(plane / ny) * nz * nx * ny + (long long)(plane % ny) * nx;
   }
-  __syncthreads();
-  const float4 m4 = *reinterpret_cast<const float4*>(part + 16 * 64 + 4 * bi);
-  cm[0] = m4.x;
-  cm[1] = m4.y;
-  cm[2] = m4.z;
-  cm[3] = m4.w;
-}
+  __device__ __forceinline__ long long row_stride() const { return kXY ? (long long)nx : (long long)nx * ny; }
+  __device__ __forceinline__ int rows() const { return kXY ? ny : nz; }
+};
 
-// Slices of a 4 x 4 block, each row r scaled by sc[r] and written as row row0 + r
-// with K = k0.. (by_rows), or each column c scaled by sc[c] and written as row
-// row0 + c with K = k0.. (columns).
-template <bool by_rows>
-__device__ __forceinline__ void write_block(uint8_t* A, const float2 (&x)[4][4], const float (&sc)[4], int row0,
-                                            int k0) {
-#pragma unroll
-  for (int o = 0; o < 4; ++o) {  // output row
-    float s[4][kVS];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const float2 v = by_rows ? x[o][u] : x[u][o];
-      slice4(__fmul_rn(v.x, sc[o]), __fmul_rn(v.y, sc[o]), s[u]);
-    }
-#pragma unroll
-    for (int k = 0; k < kVS; ++k)
-      *reinterpret_cast<uint2*>(A + k * kTileA + quad_offset(row0 + o, k0)) =
-          make_uint2(pack_h2(s[0][k], s[1][k]), pack_h2(s[2][k], s[3][k]));
-  }
-}
-
-// Slices of a 4 x 4 block with one scale, written both as rows row_a + r (K =
-// c0..) and as rows row_b + c (K = r0..).
-__device__ __forceinline__ void write_block_both(uint8_t* A, const float2 (&x)[4][4], float sc, int row_a, int row_b,
-                                                 int r0, int c0) {
-  float s[4][4][kVS];
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) slice4(__fmul_rn(x[r][c].x, sc), __fmul_rn(x[r][c].y, sc), s[r][c]);
-#pragma unroll
-  for (int k = 0; k < kVS; ++k) {
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-      *reinterpret_cast<uint2*>(A + k * kTileA + quad_offset(row_a + r, c0)) =
-          make_uint2(pack_h2(s[r][0][k], s[r][1][k]), pack_h2(s[r][2][k], s[r][3][k]));
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-      *reinterpret_cast<uint2*>(A + k * kTileA + quad_offset(row_b + c, r0)) =
-          make_uint2(pack_h2(s[0][c][k], s[1][c][k]), pack_h2(s[2][c][k], s[3][c][k]));
-  }
-}
-
-// maximum over the CTA (red: one float per warp); contains a __syncthreads
-__device__ __forceinline__ float cta_max(float m, float* red) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  m = red[0];
-#pragma unroll
-  for (int w = 1; w < kTcThreads / 32; ++w) m = fmaxf(m, red[w]);
-  return m;
-}
-
-// x and y contractions; out(y, x) = (Tx v + Ty v) as double-float pairs.  One
-// plane per batch: operand rows 0-63 are the plane's rows, rows 64-127 its
-// columns, all with one scale per plane (each value is sliced once).  Two CTAs
-// per SM, 256 tensor-memory columns each.
-__global__ void __launch_bounds__(kTcThreads, 2) k_kin_xy_tc(KinTC a) {
+template <bool kXY>
+__device__ __forceinline__ void kin_ws_body(const KinTC& a) {
   extern __shared__ uint8_t smraw[];
   uint8_t* sm = align1024(smraw);
-  uint8_t* A = sm;                                        // kVS tiles
-  uint8_t* B = sm + kBatchA;                              // kTS tiles
-  float* part = reinterpret_cast<float*>(B + kTS * kTileB);  // [16][64] column-maximum partials
-  float2* Xs = reinterpret_cast<float2*>(sm);             // [64][64] x part, column swizzled, over A
-  float2* Ys = Xs + 64 * 64;                              // [64][64] y part, over A
-  __shared__ uint64_t bar;
+  // T tiles: x/y as Z T0 Z T1 Z T2 Z T3 Z (Z = zero tile) so that [T; 0] and
+  // [0; T] are 128-row tiles; z as T0 T1 T2 T3.  Then the v stages.
+  constexpr int kTTiles = kXY ? 2 * kTS + 1 : kTS;
+  uint8_t* V = sm + kTTiles * kTile;
+  __shared__ uint64_t v_full[kStages], v_empty[kStages], acc_full[kStages], acc_empty[kStages], e_full[kStages];
   __shared__ uint32_t tmem_slot;
-  __shared__ int failed;
-  __shared__ int e_plane;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int nx = a.nx, ny = a.ny;
-  const long long psz = (long long)ny * nx;
-  int plane_parity = 0;  // alternates the reduction slots of consecutive planes
-  load_b(B, a.tslices);
-  if (tid == 0) {
-    failed = 0;
-    tc::mbar_init(&bar, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, kCols);
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tmem = tmem_slot;
-  const int lrow = (warp & 3) * 32 + (tid & 31);  // tensor-memory lane of this thread in the epilogue
-  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-  const int half = warp >> 2;
-  const int bj = tid >> 4, bi = tid & 15;  // 4 x 4 block of the plane sliced by this thread
-  // this thread's 4 x 4 block of a plane, loaded one plane ahead (software pipeline)
-  auto load_block = [&](int plane, float2 (&x)[4][4]) {
-    const float2* src = a.v + (long long)plane * psz;
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const int j = 4 * bj + r, i = 4 * bi + c;
-        x[r][c] = (j < ny && i < nx) ? __ldg(src + (long long)j * nx + i) : make_float2(0.f, 0.f);
-      }
-  };
-  float2 xn[4][4];
-  if ((int)blockIdx.x < a.nplanes) load_block(blockIdx.x, xn);
-  uint32_t phase = 0;
-  for (int plane = blockIdx.x; plane < a.nplanes; plane += gridDim.x) {
-    float2 x[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) x[r][c] = xn[r][c];
-    const int nxt = plane + (int)gridDim.x;
-    {  // the plane after next into L2
-      const int far = nxt + (int)gridDim.x;
-      if (far < a.nplanes)
-        for (long long o = (long long)tid * 4; o < psz; o += kTcThreads * 4) prefetch_l2(a.v + (long long)far * psz + o);
-    }
-    // one scale per plane: every operand row keeps 36 bits relative to the plane maximum
-    float m = 0.f;
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) m = fmaxf(m, fabsf(x[r][c].x));
-    const int e = plane_exponent(cta_max(m, part + 16 * 64 + (plane_parity ? 8 : 0)));
-    plane_parity ^= 1;
-    if (tid == 0) e_plane = e;
-    write_block_both(A, x, pow2f(8 - e), 4 * bj, 64 + 4 * bi, 4 * bj, 4 * bi);
-    tc::fence_smem_to_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0 && !failed) {
-      issue_products(tmem, tc::smem_u32(A), tc::smem_u32(B));
-      tc::mma_commit(&bar);
-    }
-    if (nxt < a.nplanes) load_block(nxt, xn);  // in flight during the products and the epilogue
-    if (!failed && !tc::mbar_wait(&bar, phase)) failed = 1;
-    phase ^= 1u;
-    tc::fence_after_sync();
-    __syncthreads();
-    if (failed) break;
-    // epilogue: rows 0-63 (x part) and 64-127 (y part) to shared memory over A
-    const float scale = pow2f(e_plane + a.e_t - 16);
-#pragma unroll 1
-    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 8) {
-      float2 v[8];
-      load_pairs8(tmem + lane_base + (uint32_t)c0, scale, v);
-      if (lrow < 64) {  // x part: row y = lrow, columns x
-#pragma unroll
-        for (int u = 0; u < 8; ++u) Xs[lrow * 64 + ((c0 + u) ^ (lrow & 31))] = v[u];
-      } else {          // y part: x = lrow - 64, columns y
-#pragma unroll
-        for (int u = 0; u < 8; ++u) Ys[(c0 + u) * 64 + (lrow - 64)] = v[u];
-      }
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    const int i = tid & 63;
-    float2* dst = a.out + (long long)plane * psz;
-    if (i < nx)
-#pragma unroll 2
-      for (int j = tid >> 6; j < ny; j += kTcThreads / 64)
-        dst[(long long)j * nx + i] = df_add_fast(Xs[j * 64 + (i ^ (j & 31))], Ys[j * 64 + i]);
-    __syncthreads();  // A (under Xs, Ys) is sliced again next
-  }
-  if (failed && tid == 0) a.status[3] = 1;
-  tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, kCols);
-}
-
-// z contraction added into the pairs: out(z, x) += Tz v, two (z, x) planes of
-// fixed (s, y) per batch, operand rows (p, x) each scaled by its own maximum.
-// Two CTAs per SM, 256 tensor-memory columns each.
-__global__ void __launch_bounds__(kTcThreads, 2) k_kin_z_tc(KinTC a) {
-  extern __shared__ uint8_t smraw[];
-  uint8_t* sm = align1024(smraw);
-  uint8_t* A = sm;                                           // kVS tiles
-  uint8_t* B = sm + kBatchA;                                 // kTS tiles
-  float* part = reinterpret_cast<float*>(B + kTS * kTileB);  // [16][64] column-maximum partials
-  __shared__ uint64_t bar;
-  __shared__ uint32_t tmem_slot;
-  __shared__ int failed;
-  __shared__ int e_row[128];
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int nx = a.nx, ny = a.ny, nz = a.nz;
-  const long long pstride = (long long)ny * nx;
-  load_b(B, a.tslices);
-  if (tid == 0) {
-    failed = 0;
-    tc::mbar_init(&bar, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, kCols);
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tmem = tmem_slot;
-  const int lrow = (warp & 3) * 32 + (tid & 31);
-  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-  const int half = warp >> 2;
-  const int bk = tid >> 4, bi = tid & 15;  // 4 x 4 block of each of the two planes
+  __shared__ int e_stage[kStages][2], e_acc[kStages][2];
+  __shared__ float red[2][kProdWarps];
+  __shared__ int prod_go, failed;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const Planes<kXY> pg{a.nx, a.ny, a.nz, a.nplanes};
   const int npairs = (a.nplanes + 1) / 2;
-  auto plane_base = [&](int plane) {  // plane = s * ny + y
-    return (long long)(plane / ny) * nz * pstride + (long long)(plane % ny) * nx;
-  };
-  // this thread's 4 x 4 block of one plane (zeros beyond the planes)
-  auto load_block = [&](int plane, float2 (&x)[4][4]) {
-    const bool pv = plane < a.nplanes;
-    const float2* src = a.v + (pv ? plane_base(plane) : 0);
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const int k = 4 * bk + r, i = 4 * bi + c;
-        x[r][c] = (pv && k < nz && i < nx) ? __ldg(src + k * pstride + i) : make_float2(0.f, 0.f);
-      }
-  };
-  auto slice_plane = [&](int pl, const float2 (&x)[4][4]) {
-    float cm[4], scl[4];
-    block_col_max(x, part, bk, bi, cm);
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int ec = plane_exponent(cm[u]);
-      scl[u] = pow2f(8 - ec);
-      if (bk == 0) e_row[pl * 64 + 4 * bi + u] = ec;
+
+  // T slices into shared memory, zero tiles around them for x/y
+  for (int e = tid; e < kTTiles * (int)kTile / 16; e += kWsThreads)
+    reinterpret_cast<uint4*>(sm)[e] = make_uint4(0u, 0u, 0u, 0u);
+  __syncthreads();
+  for (int e = tid; e < kTS * 64 * 16; e += kWsThreads) {  // kTS tiles of 64 rows x 16 quads
+    const int l = e >> 10, r = (e >> 4) & 63, q = (e & 15) * 4;
+    uint8_t* tl = sm + (kXY ? 2 * l + 1 : l) * kTile;
+    *reinterpret_cast<uint2*>(tl + quad_offset(r, q)) =
+        *reinterpret_cast<const uint2*>(a.tslices + ((size_t)l * 64 + r) * 64 + q);
+  }
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      tc::mbar_init(&v_full[s], kProdThreads);
+      tc::mbar_init(&v_empty[s], 1);
+      tc::mbar_init(&acc_full[s], 1);
+      tc::mbar_init(&acc_empty[s], kEpiThreads);
+      tc::mbar_init(&e_full[s], 1);
     }
-    write_block<false>(A, x, scl, pl * 64 + 4 * bi, 4 * bk);
-    __syncthreads();  // part[] is reused by the next plane
-  };
-  float2 xn[4][4];  // first plane of the next pair, loaded during the products (software pipeline)
-  if ((int)blockIdx.x < npairs) load_block(2 * blockIdx.x, xn);
-  uint32_t phase = 0;
-  for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x) {
-    {
-      float2 x0[4][4], x1[4][4];
+    failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == kMmaWarp) tc::tmem_alloc(&tmem_slot, kStages * kAccCols);
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp < kEpiWarps) {
+    // ---- epilogue: TMEM lane quadrant warp % 4 = (plane p, 32-column block of
+    // x), columns [32 half, 32 half + 32) ----
+    const int quad = warp & 3, half = warp >> 2;
+    const int p = quad >> 1, x = ((quad & 1) << 5) + lane;
+    const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
+    const int ncols = pg.rows();
+    const long long cstride = pg.row_stride();
+    for (int it = 0, pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
+      const int st = it & 1;
+      const uint32_t par = (uint32_t)(it >> 1) & 1u;
+      // lane 0 waits (bounded) and the warp leaves together on a timeout; once the
+      // phases are complete every lane's own wait returns at once and orders its
+      // reads after the producers' and the MMA thread's writes
+      int ok = 1;
+      if (lane == 0) ok = tc::mbar_wait(&acc_full[st], par) && tc::mbar_wait(&e_full[st], par);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) {
+        failed = 1;
+        break;
+      }
+      tc::mbar_wait(&acc_full[st], par);
+      tc::mbar_wait(&e_full[st], par);
+      tc::fence_after_sync();
+      const int plane = 2 * pair + p;
+      const bool valid = plane < a.nplanes && x < a.nx;
+      const float scale = pow2f(e_acc[st][p] + a.e_t - 16);
+      const long long ob = valid ? pg.base(plane) + x : 0;
+      const uint32_t tbase = tmem + (uint32_t)st * kAccCols + lane_base;
+#pragma unroll 1
+      for (int c0 = half * 32; c0 < half * 32 + 32 && c0 < ncols; c0 += 8) {
+        float2 v[8];
+        if (kXY) {
+          load_pairs8(tbase + (uint32_t)c0, scale, v);
+          if (valid)
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+              if (c0 + u < ncols) a.out[ob + (c0 + u) * cstride] = v[u];
+        } else {
+          float2 u0[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            u0[u] = (valid && c0 + u < ncols) ? a.out[ob + (c0 + u) * cstride] : make_float2(0.f, 0.f);
+          load_pairs8(tbase + (uint32_t)c0, scale, v);
+          if (valid)
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+              if (c0 + u < ncols) a.out[ob + (c0 + u) * cstride] = df_add_fast(u0[u], v[u]);
+        }
+      }
+      tc::fence_before_sync();
+      tc::mbar_arrive(&acc_empty[st]);
+    }
+  } else if (warp < kMmaWarp) {
+    // ---- producers: thread (bj, bi) owns rows 4 bj.., columns 4 bi.. of a plane ----
+    const int ptid = tid - kEpiThreads, pw = ptid >> 5;
+    const int bj = ptid >> 4, bi = ptid & 15;
+    const int nrows = pg.rows();
+    const long long rstride = pg.row_stride();
+    auto load_block = [&](int plane, float2 (&x)[4][4]) {
+      const bool pv = plane < a.nplanes;
+      const float2* src = a.v + (pv ? pg.base(plane) : 0);
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) x0[r][c] = xn[r][c];
-      load_block(2 * pair + 1, x1);  // in flight while the first plane is sliced
-      slice_plane(0, x0);
-      slice_plane(1, x1);
-    }
-    const int nxt = pair + (int)gridDim.x;
-    {  // the pair after next into L2
-      const int far = nxt + (int)gridDim.x;
-      if (far < npairs) {
-        const int plane = 2 * far + (tid >> 7);
-        const int i = (tid & 127) * 4;
-        if (plane < a.nplanes && i < nx)
-          for (int k = 0; k < nz; ++k) prefetch_l2(a.v + plane_base(plane) + k * pstride + i);
+        for (int c = 0; c < 4; ++c) {
+          const int j = 4 * bj + r, i = 4 * bi + c;
+          x[r][c] = (pv && j < nrows && i < a.nx) ? __ldg(src + j * rstride + i) : make_float2(0.f, 0.f);
+        }
+    };
+    auto prefetch_plane = [&](int plane) {  // into L2, one 4-value row segment per thread
+      if (plane >= a.nplanes) return;
+      const int j = ptid >> 2, i = (ptid & 3) * 16;
+      if (j < nrows && i < a.nx) prefetch_l2(a.v + pg.base(plane) + j * rstride + i);
+    };
+    float2 x[4][4];
+    load_block(2 * (int)blockIdx.x, x);
+    int slot = 0;
+    for (int it = 0, pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
+      const int st = it & 1;
+      const uint32_t par = (uint32_t)(it >> 1) & 1u;
+      if (ptid == 0) prod_go = tc::mbar_wait(&v_empty[st], par ^ 1u) ? 1 : 0;
+      tc::named_sync(1, kProdThreads);
+      if (!prod_go) {
+        if (ptid == 0) failed = 1;
+        break;
       }
-    }
-    tc::fence_smem_to_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0 && !failed) {
-      issue_products(tmem, tc::smem_u32(A), tc::smem_u32(B));
-      tc::mma_commit(&bar);
-    }
-    if (nxt < npairs) load_block(2 * nxt, xn);
-    {  // this thread's epilogue targets into L1 while the products run
-      const int pl = lrow >> 6, i = lrow & 63;
-      const int plane = 2 * pair + pl;
-      if (plane < a.nplanes && i < nx) {
-        const long long ob = plane_base(plane) + i;
-        for (int k = half * 32; k < half * 32 + 32 && k < nz; ++k)
-          asm volatile("prefetch.global.L1 [%0];" ::"l"(a.out + ob + k * pstride));
+      {  // the pair after next into L2
+        const int far = 2 * (pair + 2 * (int)gridDim.x);
+        prefetch_plane(far);
+        prefetch_plane(far + 1);
       }
-    }
-    if (!failed && !tc::mbar_wait(&bar, phase)) failed = 1;
-    phase ^= 1u;
-    tc::fence_after_sync();
-    __syncthreads();
-    if (failed) break;
-    const int pl = lrow >> 6, i = lrow & 63;
-    const int plane = 2 * pair + pl;
-    const bool cv = plane < a.nplanes && i < nx;
-    const long long ob = cv ? plane_base(plane) + i : 0;
-    const float scale = pow2f(e_row[lrow] + a.e_t - 16);
+      uint8_t* vs = V + st * kStage;
 #pragma unroll 1
-    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 8) {
-      float2 v[8], u0[8];
+      for (int pl = 0; pl < 2; ++pl) {
+        float2 y[4][4];  // the next plane, in flight while this one is sliced
+        load_block(pl == 0 ? 2 * pair + 1 : 2 * (pair + (int)gridDim.x), y);
+        float m = 0.f;
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
-        u0[u] = (cv && c0 + u < nz) ? a.out[ob + (c0 + u) * pstride] : make_float2(0.f, 0.f);
-      load_pairs8(tmem + lane_base + (uint32_t)c0, scale, v);
+        for (int r = 0; r < 4; ++r)
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
-        if (cv && c0 + u < nz) a.out[ob + (c0 + u) * pstride] = df_add_fast(u0[u], v[u]);
+          for (int c = 0; c < 4; ++c) m = fmaxf(m, fabsf(x[r][c].x));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) red[slot][pw] = m;
+        tc::named_sync(1, kProdThreads);
+#pragma unroll
+        for (int w = 0; w < kProdWarps; ++w) m = fmaxf(m, red[slot][w]);
+        slot ^= 1;
+        const int e = plane_exponent(m);
+        if (ptid == 0) e_stage[st][pl] = e;
+        const float sc = pow2f(8 - e);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          float s[4][kVS];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) slice4(__fmul_rn(x[r][c].x, sc), __fmul_rn(x[r][c].y, sc), s[c]);
+#pragma unroll
+          for (int k = 0; k < kVS; ++k)
+            *reinterpret_cast<uint2*>(vs + (2 * k + pl) * kTile + quad_offset(4 * bj + r, 4 * bi)) =
+                make_uint2(pack_h2(s[0][k], s[1][k]), pack_h2(s[2][k], s[3][k]));
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) x[r][c] = y[r][c];
+      }
+      tc::fence_smem_to_async();
+      tc::mbar_arrive(&v_full[st]);
     }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
+  } else if (lane == 0) {
+    // ---- MMA issue ----
+    const uint32_t idesc_t = tc::idesc_f16(128, 64);              // A and B K-major
+    const uint32_t idesc_v = idesc_t | tc::kIdescAMajorMN;        // A (the v tiles) MN-major
+    const uint32_t tb = tc::smem_u32(sm);
+    for (int it = 0, pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
+      const int st = it & 1;
+      const uint32_t par = (uint32_t)(it >> 1) & 1u;
+      if (!tc::mbar_wait(&v_full[st], par) || !tc::mbar_wait(&acc_empty[st], par ^ 1u)) {
+        failed = 1;
+        break;
+      }
+      tc::fence_after_sync();
+      e_acc[st][0] = e_stage[st][0];
+      e_acc[st][1] = e_stage[st][1];
+      tc::mbar_arrive(&e_full[st]);
+      const uint32_t d0 = tmem + (uint32_t)st * kAccCols;
+      const uint32_t vb = tc::smem_u32(V + st * kStage);
+#pragma unroll 1
+      for (int pr = 0; pr < kPairs; ++pr) {
+        const int k = c_pk[pr], l = c_pl[pr];
+        const uint32_t dc = d0 + (uint32_t)(k + l) * 64u;
+        const uint32_t vk = vb + (uint32_t)k * 2u * kTile;                        // slice k: plane 0, plane 1
+        const uint32_t tl = tb + (uint32_t)(kXY ? 2 * l + 1 : l) * kTile;         // T slice l
+        // contraction over the rows of each plane: A = v tile (M = (p, x), the
+        // planes 8 KiB apart), B = T; 16 rows (2 KiB) per K step
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+          tc::mma_f16(dc, tc::sw128_mn_desc(vk + (uint32_t)s * 2048u, kTile, 1024u),
+                      tc::sw128_desc(tl + (uint32_t)s * 32u), idesc_v, (c_first[pr] && s == 0) ? 0u : 1u);
+        if (kXY) {  // contraction along x: A = diag(T, T) over K = (p', q), B = v rows of plane p'
+#pragma unroll
+          for (int s = 0; s < 8; ++s) {
+            const uint32_t pp = (uint32_t)(s >> 2), q = (uint32_t)(s & 3) * 32u;
+            tc::mma_f16(dc, tc::sw128_desc(tl - pp * kTile + q), tc::sw128_desc(vk + pp * kTile + q), idesc_t, 1u);
+          }
+        }
+      }
+      tc::mma_commit(&v_empty[st]);
+      tc::mma_commit(&acc_full[st]);
+    }
   }
-  if (failed && tid == 0) a.status[3] = 1;
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+  if (failed && tid == 0) a.status[3] = 1;
+  if (warp == kMmaWarp) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, kStages * kAccCols);
+  }
 }
 
-constexpr size_t kSmemXY = kBatchA + kTS * kTileB + 17 * 64 * sizeof(float) + 1024;
-constexpr size_t kSmemZ = kSmemXY;
-static_assert(2 * 64 * 64 * sizeof(float2) <= kBatchA, "x and y staging must fit over the operand tiles");
-static_assert(2 * (kSmemXY + 1024) <= 228 * 1024, "two CTAs per SM");
-static_assert(2 * kCols <= 512, "the accumulators of two CTAs must fit in tensor memory");
+// x and y contractions: out(y, x) = (Tx v + Ty v) as double-float pairs
+__global__ void __launch_bounds__(kWsThreads, 1) k_kin_xy_tc(KinTC a) { kin_ws_body<true>(a); }
+
+// z contraction added into the pairs: out(z, x) += Tz v
+__global__ void __launch_bounds__(kWsThreads, 1) k_kin_z_tc(KinTC a) { kin_ws_body<false>(a); }
+
+constexpr size_t kSmemXY = 1024 + (2 * kTS + 1) * kTile + kStages * kStage;
+constexpr size_t kSmemZ = 1024 + kTS * kTile + kStages * kStage;
+static_assert(kSmemXY + 1024 <= 227 * 1024, "x/y stages and T tiles must fit in one CTA's shared memory");
+static_assert(kStages * kAccCols <= 512, "the accumulator stages must fit in tensor memory");
 
 int sm_count() {
   int dev = 0, sms = 0;
@@ -530,7 +436,7 @@ int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   DeviceState& d = h->d;
   cudaFuncSetAttribute(k_kin_xy_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemXY);
   KinTC a{d.kxy_slices, d.e_txy, v, reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status};
-  k_kin_xy_tc<<<std::min(a.nplanes, 2 * sm_count()), kTcThreads, kSmemXY, s>>>(a);
+  k_kin_xy_tc<<<std::min((a.nplanes + 1) / 2, sm_count()), kWsThreads, kSmemXY, s>>>(a);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }
@@ -540,7 +446,7 @@ int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   DeviceState& d = h->d;
   cudaFuncSetAttribute(k_kin_z_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemZ);
   KinTC a{d.kz_slices, d.e_tz, v, reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status};
-  k_kin_z_tc<<<std::min((a.nplanes + 1) / 2, 2 * sm_count()), kTcThreads, kSmemZ, s>>>(a);
+  k_kin_z_tc<<<std::min((a.nplanes + 1) / 2, sm_count()), kWsThreads, kSmemZ, s>>>(a);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }

@@ -40,6 +40,20 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
+// shared-memory matrix descriptor of an MN-major operand, 128-byte swizzle: the
+// rows of the stored tile run along K (one 128-byte row = 64 FP16 values along
+// M or N, chunk c of row r at chunk c ^ (r % 8)), 8-row groups `sbo` bytes
+// apart, and 64-wide blocks along M or N `lbo` bytes apart
+__device__ __forceinline__ uint64_t sw128_mn_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)2u << 61;
+  return d;
+}
+
 // instruction descriptor, kind::tf32, FP32 accumulate, both operands K-major
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
   return (1u << 4)                       // D format F32
@@ -55,6 +69,9 @@ __host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
          | ((uint32_t)(N >> 3) << 17)    // N / 8
          | ((uint32_t)(M >> 4) << 24);   // M / 16
 }
+
+// instruction-descriptor bit of an MN-major (transposed) A operand
+constexpr uint32_t kIdescAMajorMN = 1u << 15;
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
@@ -75,6 +92,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   while (!mbar_try_wait(bar, parity))
     if (clock64() - t0 > kSpinCycles) return false;
   return true;
+}
+
+// arrive on `bar` (release at CTA scope)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// barrier `id` (1..15) among `nthreads` threads (a multiple of 32)
+__device__ __forceinline__ void named_sync(uint32_t id, uint32_t nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
 // allocate `ncols` (power of two >= 32) tensor-memory columns; warp-wide
