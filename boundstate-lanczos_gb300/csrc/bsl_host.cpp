@@ -424,9 +424,9 @@ int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
   if ((rc = upload(&d.kz_head, hi, "Tz")) || (rc = upload(&d.kz_band, lo, "Tz"))) return bail(rc);
   if (kinetic_tc_supported(t)) {
     std::vector<uint16_t> sl;
-    kinetic_f16_slices(t.tx, t.nx, &sl, &d.e_txy);
+    kinetic_smem_image(t.tx, t.nx, true, &sl, &d.e_txy);
     if ((rc = upload(&d.kxy_slices, sl, "Tx"))) return bail(rc);
-    kinetic_f16_slices(t.tz, t.nz, &sl, &d.e_tz);
+    kinetic_smem_image(t.tz, t.nz, false, &sl, &d.e_tz);
     if ((rc = upload(&d.kz_slices, sl, "Tz"))) return bail(rc);
     h->kinetic_engine = BSL_KIN_TENSOR;
   }

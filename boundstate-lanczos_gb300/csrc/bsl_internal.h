@@ -181,7 +181,8 @@ int launch_kin_z_mixed(bsl_handle* h, const float* v, cudaStream_t s);
 // tensor-core kinetic (bsl_kinetic_tc.cu): the same output as the mixed
 // kernels, from the double-float Lanczos vector, for grids of at most 64 points
 // per axis with Tx = Ty
-void kinetic_f16_slices(const std::vector<double>& T, int n, std::vector<uint16_t>* slices, int* e_t);
+void kinetic_smem_image(const std::vector<double>& T, int n, bool with_zero_tiles, std::vector<uint16_t>* image,
+                        int* e_t);
 bool kinetic_tc_supported(const Tables& t);
 int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s);
 int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s);

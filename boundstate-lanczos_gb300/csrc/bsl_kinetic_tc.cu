@@ -38,8 +38,8 @@
 //
 // Pipeline: one persistent CTA per SM with three roles.  Eight producer warps
 // load a plane pair, find each plane's scale and write the slices into one of
-// two 64 KiB shared-memory stages; one thread issues the pair's 120 (x/y) or
-// 40 (z) MMAs into one of two 256-column accumulator stages; eight epilogue
+// two 64 KiB shared-memory stages; one thread issues the pair's 72 (x/y) or
+// 16 (z) MMAs into one of two 256-column accumulator stages; eight epilogue
 // warps read the finished accumulators and store (x/y) or add (z) the
 // double-float results.  mbarriers hand the stages over; every wait is bounded
 // and a timeout sets status[3].
@@ -58,7 +58,8 @@ namespace {
 constexpr int kVS = 4;                        // slices of v
 constexpr int kTS = 4;                        // slices of T
 constexpr uint32_t kTile = 64 * 128;          // 8 KiB: 64 rows x 64 FP16, one 128-byte swizzled row each
-constexpr uint32_t kStage = kVS * 2 * kTile;  // v slices of a plane pair: [slice][plane] tiles
+constexpr uint32_t kPlaneSlices = kVS * kTile;  // the v slices of one plane, contiguous
+constexpr uint32_t kStage = 2 * kPlaneSlices;   // v slices of a plane pair: [plane][slice] tiles
 constexpr int kStages = 2;                    // shared-memory stages and accumulator stages
 constexpr uint32_t kAccCols = 4 * 64;         // accumulator columns of one pair (classes 0..3)
 constexpr int kEpiWarps = 8;                  // warps 0-7
@@ -67,13 +68,11 @@ constexpr int kMmaWarp = kEpiWarps + kProdWarps;  // warp 16: MMA issue and tens
 constexpr int kWsThreads = (kMmaWarp + 1) * 32;
 constexpr int kProdThreads = kProdWarps * 32;
 constexpr int kEpiThreads = kEpiWarps * 32;
-constexpr int kPairs = 10;  // slice products (k, l) with k + l <= 3, by class
-__constant__ int8_t c_pk[kPairs] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
-__constant__ int8_t c_pl[kPairs] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
-__constant__ int8_t c_first[kPairs] = {1, 1, 0, 1, 0, 0, 1, 0, 0, 0};
+constexpr int kMaxItems = 64 * 16 / kProdThreads;  // (row, 4-column group) items per producer thread
 
 struct KinTC {
-  const uint16_t* tslices;  // [kTS][64][64] FP16 bits, row = output index, column = q, zero padded
+  const uint4* timage;      // the T tiles as laid out in shared memory (kinetic_smem_image)
+  int timage16;             // its size in 16-byte units
   int e_t;                  // T = 2^(e_t - 8) (b1 + 2^-9 b2 + 2^-18 b3 + 2^-27 b4)
   const float2* v;          // the Lanczos v as double-float pairs
   float2* out;
@@ -141,6 +140,7 @@ __device__ __forceinline__ void load_pairs8(uint32_t taddr, float scale, float2 
 
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
+
 // Plane geometry: x/y planes are the contiguous (y, x) planes of fixed (s, z);
 // z planes are the (z, x) planes of fixed (s, y), rows nx * ny apart.
 template <bool kXY>
@@ -158,11 +158,12 @@ template <bool kXY>
 __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
   extern __shared__ uint8_t smraw[];
   uint8_t* sm = align1024(smraw);
-  // T tiles: x/y as Z T0 Z T1 Z T2 Z T3 Z (Z = zero tile) so that [T; 0] and
-  // [0; T] are 128-row tiles; z as T0 T1 T2 T3.  Then the v stages.
-  constexpr int kTTiles = kXY ? 2 * kTS + 1 : kTS;
+  // T tiles: x/y as Z T0 T1 T2 T3 Z (Z = zero tile), z as T0 T1 T2 T3; then
+  // the v stages
+  constexpr int kTTiles = kXY ? kTS + 2 : kTS;
   uint8_t* V = sm + kTTiles * kTile;
   __shared__ uint64_t v_full[kStages], v_empty[kStages], acc_full[kStages], acc_empty[kStages], e_full[kStages];
+  __shared__ uint64_t setup_done;  // T tiles written and v stages zeroed (by the epilogue warps)
   __shared__ uint32_t tmem_slot;
   __shared__ int e_stage[kStages][2], e_acc[kStages][2];
   __shared__ float red[2][kProdWarps];
@@ -171,16 +172,6 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
   const Planes<kXY> pg{a.nx, a.ny, a.nz, a.nplanes};
   const int npairs = (a.nplanes + 1) / 2;
 
-  // T slices into shared memory, zero tiles around them for x/y
-  for (int e = tid; e < kTTiles * (int)kTile / 16; e += kWsThreads)
-    reinterpret_cast<uint4*>(sm)[e] = make_uint4(0u, 0u, 0u, 0u);
-  __syncthreads();
-  for (int e = tid; e < kTS * 64 * 16; e += kWsThreads) {  // kTS tiles of 64 rows x 16 quads
-    const int l = e >> 10, r = (e >> 4) & 63, q = (e & 15) * 4;
-    uint8_t* tl = sm + (kXY ? 2 * l + 1 : l) * kTile;
-    *reinterpret_cast<uint2*>(tl + quad_offset(r, q)) =
-        *reinterpret_cast<const uint2*>(a.tslices + ((size_t)l * 64 + r) * 64 + q);
-  }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
       tc::mbar_init(&v_full[s], kProdThreads);
@@ -189,11 +180,11 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
       tc::mbar_init(&acc_empty[s], kEpiThreads);
       tc::mbar_init(&e_full[s], 1);
     }
+    tc::mbar_init(&setup_done, kEpiThreads);
     failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == kMmaWarp) tc::tmem_alloc(&tmem_slot, kStages * kAccCols);
-  tc::fence_smem_to_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -207,9 +198,44 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
     const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
     const int ncols = pg.rows();
     const long long cstride = pg.row_stride();
+    const int c_begin = half * 32, c_end = min(half * 32 + 32, ncols);
+    {  // setup while the producers' first planes are in flight: the T tiles (a
+       // prebuilt image of that region) and zeroed v stages (the producers write
+       // only the rows and 4-column groups that hold data, so the padding of
+       // every stage stays zero)
+      constexpr int kBatch = 6;
+      for (int e0 = tid; e0 < a.timage16; e0 += kBatch * kEpiThreads) {
+        uint4 img[kBatch];
+#pragma unroll
+        for (int r = 0; r < kBatch; ++r) {
+          const int e = e0 + r * kEpiThreads;
+          img[r] = e < a.timage16 ? a.timage[e] : make_uint4(0u, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for (int r = 0; r < kBatch; ++r) {
+          const int e = e0 + r * kEpiThreads;
+          if (e < a.timage16) reinterpret_cast<uint4*>(sm)[e] = img[r];
+        }
+      }
+      for (int e = tid; e < (int)(kStages * kStage / 16); e += kEpiThreads)
+        reinterpret_cast<uint4*>(V)[e] = make_uint4(0u, 0u, 0u, 0u);
+      tc::fence_smem_to_async();
+      tc::mbar_arrive(&setup_done);
+    }
+    // z: the values the epilogue adds to, 8 columns of this thread's x
+    auto load8 = [&](long long ob, bool valid, int c0, float2 (&u0)[8]) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        u0[u] = (valid && c0 + u < c_end) ? a.out[ob + (c0 + u) * cstride] : make_float2(0.f, 0.f);
+    };
     for (int it = 0, pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
       const int st = it & 1;
       const uint32_t par = (uint32_t)(it >> 1) & 1u;
+      const int plane = 2 * pair + p;
+      const bool valid = plane < a.nplanes && x < a.nx;
+      const long long ob = valid ? pg.base(plane) + x : 0;
+      float2 nxt[8];  // z: first chunk loaded while the products run
+      if (!kXY) load8(ob, valid, c_begin, nxt);
       // lane 0 waits (bounded) and the warp leaves together on a timeout; once the
       // phases are complete every lane's own wait returns at once and orders its
       // reads after the producers' and the MMA thread's writes
@@ -223,64 +249,64 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
       tc::mbar_wait(&acc_full[st], par);
       tc::mbar_wait(&e_full[st], par);
       tc::fence_after_sync();
-      const int plane = 2 * pair + p;
-      const bool valid = plane < a.nplanes && x < a.nx;
       const float scale = pow2f(e_acc[st][p] + a.e_t - 16);
-      const long long ob = valid ? pg.base(plane) + x : 0;
       const uint32_t tbase = tmem + (uint32_t)st * kAccCols + lane_base;
 #pragma unroll 1
-      for (int c0 = half * 32; c0 < half * 32 + 32 && c0 < ncols; c0 += 8) {
+      for (int c0 = c_begin; c0 < c_end; c0 += 8) {
         float2 v[8];
         if (kXY) {
           load_pairs8(tbase + (uint32_t)c0, scale, v);
           if (valid)
 #pragma unroll
             for (int u = 0; u < 8; ++u)
-              if (c0 + u < ncols) a.out[ob + (c0 + u) * cstride] = v[u];
+              if (c0 + u < c_end) a.out[ob + (c0 + u) * cstride] = v[u];
         } else {
-          float2 u0[8];
+          float2 cur[8];
 #pragma unroll
-          for (int u = 0; u < 8; ++u)
-            u0[u] = (valid && c0 + u < ncols) ? a.out[ob + (c0 + u) * cstride] : make_float2(0.f, 0.f);
+          for (int u = 0; u < 8; ++u) cur[u] = nxt[u];
+          if (c0 + 8 < c_end) load8(ob, valid, c0 + 8, nxt);  // the next chunk, in flight meanwhile
           load_pairs8(tbase + (uint32_t)c0, scale, v);
           if (valid)
 #pragma unroll
             for (int u = 0; u < 8; ++u)
-              if (c0 + u < ncols) a.out[ob + (c0 + u) * cstride] = df_add_fast(u0[u], v[u]);
+              if (c0 + u < c_end) a.out[ob + (c0 + u) * cstride] = df_add_fast(cur[u], v[u]);
         }
       }
       tc::fence_before_sync();
       tc::mbar_arrive(&acc_empty[st]);
     }
   } else if (warp < kMmaWarp) {
-    // ---- producers: thread (bj, bi) owns rows 4 bj.., columns 4 bi.. of a plane ----
+    // ---- producers: item i = (row i / ncg, 4-column group i % ncg) of a plane,
+    // items ptid, ptid + 256, ...; the next plane's items are loaded into
+    // registers while this one is sliced ----
     const int ptid = tid - kEpiThreads, pw = ptid >> 5;
-    const int bj = ptid >> 4, bi = ptid & 15;
-    const int nrows = pg.rows();
+    const int nrows = pg.rows(), nx = a.nx, ncg = (nx + 3) >> 2, nitems = nrows * ncg;
     const long long rstride = pg.row_stride();
-    auto load_block = [&](int plane, float2 (&x)[4][4]) {
+    auto load_items = [&](int plane, float2 (&x)[kMaxItems][4]) {
       const bool pv = plane < a.nplanes;
       const float2* src = a.v + (pv ? pg.base(plane) : 0);
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
+      for (int t = 0; t < kMaxItems; ++t) {
+        const int i = ptid + t * kProdThreads;
+        const int j = i / ncg, c = (i - j * ncg) * 4;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const int j = 4 * bj + r, i = 4 * bi + c;
-          x[r][c] = (pv && j < nrows && i < a.nx) ? __ldg(src + j * rstride + i) : make_float2(0.f, 0.f);
-        }
+        for (int u = 0; u < 4; ++u)
+          x[t][u] = (pv && i < nitems && c + u < nx) ? __ldg(src + j * rstride + c + u) : make_float2(0.f, 0.f);
+      }
     };
-    auto prefetch_plane = [&](int plane) {  // into L2, one 4-value row segment per thread
+    auto prefetch_plane = [&](int plane) {  // into L2, one 16-value row segment per thread
       if (plane >= a.nplanes) return;
       const int j = ptid >> 2, i = (ptid & 3) * 16;
-      if (j < nrows && i < a.nx) prefetch_l2(a.v + pg.base(plane) + j * rstride + i);
+      if (j < nrows && i < nx) prefetch_l2(a.v + pg.base(plane) + j * rstride + i);
     };
-    float2 x[4][4];
-    load_block(2 * (int)blockIdx.x, x);
+    float2 x[kMaxItems][4];
+    load_items(2 * (int)blockIdx.x, x);  // in flight during the setup
     int slot = 0;
     for (int it = 0, pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
       const int st = it & 1;
       const uint32_t par = (uint32_t)(it >> 1) & 1u;
-      if (ptid == 0) prod_go = tc::mbar_wait(&v_empty[st], par ^ 1u) ? 1 : 0;
+      if (ptid == 0)
+        prod_go = ((it > 0 || tc::mbar_wait(&setup_done, 0u)) && tc::mbar_wait(&v_empty[st], par ^ 1u)) ? 1 : 0;
       tc::named_sync(1, kProdThreads);
       if (!prod_go) {
         if (ptid == 0) failed = 1;
@@ -294,47 +320,52 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
       uint8_t* vs = V + st * kStage;
 #pragma unroll 1
       for (int pl = 0; pl < 2; ++pl) {
-        float2 y[4][4];  // the next plane, in flight while this one is sliced
-        load_block(pl == 0 ? 2 * pair + 1 : 2 * (pair + (int)gridDim.x), y);
-        float m = 0.f;
+        float2 y[kMaxItems][4];  // the next plane, in flight while this one is sliced
+        load_items(pl == 0 ? 2 * pair + 1 : 2 * (pair + (int)gridDim.x), y);
+        float mx = 0.f;
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
+        for (int t = 0; t < kMaxItems; ++t)
 #pragma unroll
-          for (int c = 0; c < 4; ++c) m = fmaxf(m, fabsf(x[r][c].x));
+          for (int u = 0; u < 4; ++u) mx = fmaxf(mx, fabsf(x[t][u].x));
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) red[slot][pw] = m;
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) red[slot][pw] = mx;
         tc::named_sync(1, kProdThreads);
 #pragma unroll
-        for (int w = 0; w < kProdWarps; ++w) m = fmaxf(m, red[slot][w]);
+        for (int w = 0; w < kProdWarps; ++w) mx = fmaxf(mx, red[slot][w]);
         slot ^= 1;
-        const int e = plane_exponent(m);
+        const int e = plane_exponent(mx);
         if (ptid == 0) e_stage[st][pl] = e;
         const float sc = pow2f(8 - e);
+        uint8_t* vp = vs + pl * kPlaneSlices;
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          float s[4][kVS];
+        for (int t = 0; t < kMaxItems; ++t) {
+          const int i = ptid + t * kProdThreads;
+          if (i < nitems) {
+            const int j = i / ncg, c = (i - j * ncg) * 4;
+            float sl[4][kVS];
 #pragma unroll
-          for (int c = 0; c < 4; ++c) slice4(__fmul_rn(x[r][c].x, sc), __fmul_rn(x[r][c].y, sc), s[c]);
+            for (int u = 0; u < 4; ++u) slice4(__fmul_rn(x[t][u].x, sc), __fmul_rn(x[t][u].y, sc), sl[u]);
+            const uint32_t off = quad_offset(j, c);
 #pragma unroll
-          for (int k = 0; k < kVS; ++k)
-            *reinterpret_cast<uint2*>(vs + (2 * k + pl) * kTile + quad_offset(4 * bj + r, 4 * bi)) =
-                make_uint2(pack_h2(s[0][k], s[1][k]), pack_h2(s[2][k], s[3][k]));
+            for (int k = 0; k < kVS; ++k)
+              *reinterpret_cast<uint2*>(vp + k * kTile + off) =
+                  make_uint2(pack_h2(sl[0][k], sl[1][k]), pack_h2(sl[2][k], sl[3][k]));
+          }
         }
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
+        for (int t = 0; t < kMaxItems; ++t)
 #pragma unroll
-          for (int c = 0; c < 4; ++c) x[r][c] = y[r][c];
+          for (int u = 0; u < 4; ++u) x[t][u] = y[t][u];
       }
       tc::fence_smem_to_async();
       tc::mbar_arrive(&v_full[st]);
     }
   } else if (lane == 0) {
     // ---- MMA issue ----
-    const uint32_t idesc_t = tc::idesc_f16(128, 64);              // A and B K-major
-    const uint32_t idesc_v = idesc_t | tc::kIdescAMajorMN;        // A (the v tiles) MN-major
     const uint32_t tb = tc::smem_u32(sm);
-    for (int it = 0, pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
+    if (!tc::mbar_wait(&setup_done, 0u)) failed = 1;
+    for (int it = 0, pair = blockIdx.x; pair < npairs && !failed; pair += gridDim.x, ++it) {
       const int st = it & 1;
       const uint32_t par = (uint32_t)(it >> 1) & 1u;
       if (!tc::mbar_wait(&v_full[st], par) || !tc::mbar_wait(&acc_empty[st], par ^ 1u)) {
@@ -347,23 +378,40 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
       tc::mbar_arrive(&e_full[st]);
       const uint32_t d0 = tmem + (uint32_t)st * kAccCols;
       const uint32_t vb = tc::smem_u32(V + st * kStage);
+      // Class c accumulates in columns [64 c, 64 c + 64).  An MMA whose B stacks
+      // the slices l = 0 .. 3 - k of one operand along N (rows 64 l ..) and
+      // whose D starts at column 64 k puts product (k, l) into class k + l.
+      // Contraction over the rows of each plane (y for x/y, z for z): A = v
+      // slice k (M = (p, x), MN-major, the planes kPlaneSlices apart), B = T
+      // slices 0 .. 3 - k; 16 rows (2 KiB) per K step.  The first MMA (k = 0,
+      // N = 256) sets all four classes.
+      const uint32_t t0 = tb + (kXY ? kTile : 0u);
 #pragma unroll 1
-      for (int pr = 0; pr < kPairs; ++pr) {
-        const int k = c_pk[pr], l = c_pl[pr];
-        const uint32_t dc = d0 + (uint32_t)(k + l) * 64u;
-        const uint32_t vk = vb + (uint32_t)k * 2u * kTile;                        // slice k: plane 0, plane 1
-        const uint32_t tl = tb + (uint32_t)(kXY ? 2 * l + 1 : l) * kTile;         // T slice l
-        // contraction over the rows of each plane: A = v tile (M = (p, x), the
-        // planes 8 KiB apart), B = T; 16 rows (2 KiB) per K step
+      for (int k = 0; k < kVS; ++k) {
+        const uint32_t idesc = tc::idesc_f16(128, 64 * (kTS - k)) | tc::kIdescAMajorMN;
 #pragma unroll
         for (int s = 0; s < 4; ++s)
-          tc::mma_f16(dc, tc::sw128_mn_desc(vk + (uint32_t)s * 2048u, kTile, 1024u),
-                      tc::sw128_desc(tl + (uint32_t)s * 32u), idesc_v, (c_first[pr] && s == 0) ? 0u : 1u);
-        if (kXY) {  // contraction along x: A = diag(T, T) over K = (p', q), B = v rows of plane p'
+          tc::mma_f16(d0 + (uint32_t)k * 64u,
+                      tc::sw128_mn_desc(vb + (uint32_t)k * kTile + (uint32_t)s * 2048u, kPlaneSlices, 1024u),
+                      tc::sw128_desc(t0 + (uint32_t)s * 32u), idesc, (k == 0 && s == 0) ? 0u : 1u);
+      }
+      if (kXY) {
+        // contraction along x: A = diag(T_l, T_l) over K = (p', q), read MN-major
+        // (T is symmetric) with its two 64-row blocks chosen by the start address
+        // and the block stride: [T_l; 0] = (T_l, the zero tile above) and
+        // [0; T_l] = (the zero tile below, T_l); B = v slices 0 .. 3 - l of plane p'
+        // stacked along N
+        const uint32_t zlo = tb, zhi = tb + (uint32_t)(kTS + 1) * kTile;
+#pragma unroll 1
+        for (int l = 0; l < kTS; ++l) {
+          const uint32_t tl = t0 + (uint32_t)l * kTile;
+          const uint32_t idesc = tc::idesc_f16(128, 64 * (kVS - l)) | tc::kIdescAMajorMN;
 #pragma unroll
           for (int s = 0; s < 8; ++s) {
-            const uint32_t pp = (uint32_t)(s >> 2), q = (uint32_t)(s & 3) * 32u;
-            tc::mma_f16(dc, tc::sw128_desc(tl - pp * kTile + q), tc::sw128_desc(vk + pp * kTile + q), idesc_t, 1u);
+            const uint32_t pp = (uint32_t)(s >> 2), q = (uint32_t)(s & 3);
+            const uint64_t adesc = pp ? tc::sw128_mn_desc(zlo + q * 2048u, tl - zlo, 1024u)
+                                      : tc::sw128_mn_desc(tl + q * 2048u, zhi - tl, 1024u);
+            tc::mma_f16(d0 + (uint32_t)l * 64u, adesc, tc::sw128_desc(vb + pp * kPlaneSlices + q * 32u), idesc, 1u);
           }
         }
       }
@@ -386,9 +434,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_kin_xy_tc(KinTC a) { kin_ws_b
 // z contraction added into the pairs: out(z, x) += Tz v
 __global__ void __launch_bounds__(kWsThreads, 1) k_kin_z_tc(KinTC a) { kin_ws_body<false>(a); }
 
-constexpr size_t kSmemXY = 1024 + (2 * kTS + 1) * kTile + kStages * kStage;
+constexpr size_t kSmemXY = 1024 + (kTS + 2) * kTile + kStages * kStage;
 constexpr size_t kSmemZ = 1024 + kTS * kTile + kStages * kStage;
-static_assert(kSmemXY + 1024 <= 227 * 1024, "x/y stages and T tiles must fit in one CTA's shared memory");
+static_assert(kSmemXY + 512 <= 227 * 1024, "x/y T tiles and stages must fit in one CTA's shared memory");
 static_assert(kStages * kAccCols <= 512, "the accumulator stages must fit in tensor memory");
 
 int sm_count() {
@@ -407,23 +455,30 @@ uint16_t half_bits(float x) {  // FP16 bits of a small integer (|x| <= 2048: exa
 
 }  // namespace
 
-// Fixed-point FP16 slices of an n x n kinetic matrix: T = 2^(e_t - 8) (b1 + 2^-9 b2
-// + 2^-18 b3 + 2^-27 b4) + O(2^(e_t - 36)), each b an integer in [-256, 256]
-// rounded to nearest (a symmetric T stays symmetric), as zero-padded
-// [kTS][64][64] tiles (row = output index, column = contraction index).
-void kinetic_f16_slices(const std::vector<double>& T, int n, std::vector<uint16_t>* slices, int* e_t) {
+// Fixed-point FP16 slices of an n x n kinetic matrix, T = 2^(e_t - 8) (b1 +
+// 2^-9 b2 + 2^-18 b3 + 2^-27 b4) + O(2^(e_t - 36)), each b an integer in
+// [-256, 256] rounded to nearest (a symmetric T stays symmetric), as the bytes
+// of the kernels' shared-memory T region: tiles of 64 rows (output index) x 64
+// FP16 (contraction index), zero padded, 128-byte rows with 16-byte chunk c of
+// row r at chunk c ^ (r % 8); with_zero_tiles adds a zero tile before and after
+// the four slice tiles (the x/y layout).
+void kinetic_smem_image(const std::vector<double>& T, int n, bool with_zero_tiles, std::vector<uint16_t>* image,
+                        int* e_t) {
   double m = 0.0;
   for (double x : T) m = std::max(m, std::fabs(x));
   int e = 0;
   if (m > 0.0) std::frexp(m, &e);  // m = f 2^e, f in [0.5, 1)
   *e_t = e;
-  slices->assign((size_t)kTS * 64 * 64, half_bits(0.f));
+  const int first = with_zero_tiles ? 1 : 0, ntiles = kTS + 2 * first;
+  image->assign((size_t)ntiles * kTile / 2, half_bits(0.f));
   for (int i = 0; i < n; ++i)
     for (int q = 0; q < n; ++q) {
       double r = std::ldexp(T[(size_t)i * n + q], 8 - e);
       for (int l = 0; l < kTS; ++l) {
         const double b = std::nearbyint(r);
-        (*slices)[((size_t)l * 64 + i) * 64 + q] = half_bits((float)b);
+        const size_t byte = (size_t)(first + l) * kTile + (size_t)i * 128 + (size_t)(((q >> 3) ^ (i & 7)) << 4) +
+                            (size_t)(q & 7) * 2;
+        (*image)[byte / 2] = half_bits((float)b);
         r = (r - b) * 512.0;
       }
     }
@@ -435,7 +490,8 @@ int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   const Tables& t = h->t;
   DeviceState& d = h->d;
   cudaFuncSetAttribute(k_kin_xy_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemXY);
-  KinTC a{d.kxy_slices, d.e_txy, v, reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status};
+  KinTC a{reinterpret_cast<const uint4*>(d.kxy_slices), (int)((kTS + 2) * kTile / 16), d.e_txy, v,
+          reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status};
   k_kin_xy_tc<<<std::min((a.nplanes + 1) / 2, sm_count()), kWsThreads, kSmemXY, s>>>(a);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
@@ -445,7 +501,8 @@ int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   const Tables& t = h->t;
   DeviceState& d = h->d;
   cudaFuncSetAttribute(k_kin_z_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemZ);
-  KinTC a{d.kz_slices, d.e_tz, v, reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status};
+  KinTC a{reinterpret_cast<const uint4*>(d.kz_slices), (int)(kTS * kTile / 16), d.e_tz, v,
+          reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status};
   k_kin_z_tc<<<std::min((a.nplanes + 1) / 2, sm_count()), kWsThreads, kSmemZ, s>>>(a);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
