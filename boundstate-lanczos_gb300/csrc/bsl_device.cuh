@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "bsl_internal.h"
 
 namespace bsl {
@@ -214,6 +216,33 @@ __device__ __forceinline__ bool reduce_grid(double part, double* partials, unsig
     *counter = 0u;
   }
   return true;
+}
+
+// ---------------------------------------------------------------------------
+// Programmatic dependent launch: the kernels of the Lanczos iteration are
+// launched with programmatic stream serialization, so a kernel's CTAs may start
+// (and run their prologue) while the previous kernel's last CTAs finish.
+// pdl_wait() blocks until the previous kernel has completed and its memory is
+// visible; every thread calls it before touching data another kernel writes or
+// reads.  Without the launch attribute both are no-ops.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// launch with programmatic stream serialization
+template <typename... K, typename... A>
+cudaError_t launch_pdl(void (*kernel)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
 }
 
 }  // namespace bsl

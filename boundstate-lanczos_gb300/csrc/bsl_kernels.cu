@@ -480,6 +480,8 @@ __global__ void __launch_bounds__(256, 3) k_update_pair(const float2* __restrict
                                                         long long L, float* __restrict__ v32_next, long long D,
                                                         double* partials, unsigned int* counter, double* scalars,
                                                         double* hist, int hist_stride, int j, int* status) {
+  pdl_launch_dependents();
+  pdl_wait();  // alpha and R come from the potential stream
   // per-thread constants prepared by the previous kernels' last blocks (no FP64 work per thread)
   const float2 na = reinterpret_cast<const float2*>(scalars)[9];  // -alpha c
   const int e = reinterpret_cast<const int*>(scalars)[20];         // g = 2^e, e = ilogb(sr) - ilogb(beta_{j-1})
@@ -928,10 +930,9 @@ int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s) {
 int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaStream_t s) {
   DeviceState& d = h->d;
   if (h->state_pairs == 1)
-    k_update_pair<<<d.pair_blocks, kThreads, 0, s>>>(
-        reinterpret_cast<const float2*>(V), reinterpret_cast<float2*>(R), L,
-        h->kinetic_engine == BSL_KIN_TENSOR ? nullptr : d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
-        d.hist_cap, j, d.status);
+    BSL_CUDA(launch_pdl(k_update_pair, dim3(d.pair_blocks), dim3(kThreads), 0, s, reinterpret_cast<const float2*>(V),
+                        reinterpret_cast<float2*>(R), L, h->kinetic_engine == BSL_KIN_TENSOR ? nullptr : d.v32, L - 1,
+                        d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j, d.status));
   else
     k_update_fold<<<d.red_blocks, kThreads, 0, s>>>(V, R, L, d.v32, L - 1, d.partials, d.counter, d.scalars, d.hist,
                                                     d.hist_cap, j, d.status);

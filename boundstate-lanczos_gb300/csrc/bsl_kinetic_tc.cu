@@ -49,6 +49,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "bsl_device.cuh"
 #include "bsl_internal.h"
 #include "bsl_tc.cuh"
 
@@ -163,7 +164,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
   constexpr int kTTiles = kXY ? kTS + 2 : kTS;
   uint8_t* V = sm + kTTiles * kTile;
   __shared__ uint64_t v_full[kStages], v_empty[kStages], acc_full[kStages], acc_empty[kStages], e_full[kStages];
-  __shared__ uint64_t setup_done;  // T tiles written and v stages zeroed (by the epilogue warps)
+  __shared__ uint64_t stages_zeroed, t_ready;  // setup by the epilogue warps
   __shared__ uint32_t tmem_slot;
   __shared__ int e_stage[kStages][2], e_acc[kStages][2];
   __shared__ float red[2][kProdWarps];
@@ -180,7 +181,8 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
       tc::mbar_init(&acc_empty[s], kEpiThreads);
       tc::mbar_init(&e_full[s], 1);
     }
-    tc::mbar_init(&setup_done, kEpiThreads);
+    tc::mbar_init(&stages_zeroed, kEpiThreads);
+    tc::mbar_init(&t_ready, kEpiThreads);
     failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -189,6 +191,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
+  pdl_launch_dependents();
 
   if (warp < kEpiWarps) {
     // ---- epilogue: TMEM lane quadrant warp % 4 = (plane p, 32-column block of
@@ -199,10 +202,14 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
     const int ncols = pg.rows();
     const long long cstride = pg.row_stride();
     const int c_begin = half * 32, c_end = min(half * 32 + 32, ncols);
-    {  // setup while the producers' first planes are in flight: the T tiles (a
-       // prebuilt image of that region) and zeroed v stages (the producers write
-       // only the rows and 4-column groups that hold data, so the padding of
-       // every stage stays zero)
+    {  // setup while the producers' first planes are in flight: zeroed v stages
+       // (the producers write only the rows and 4-column groups that hold data,
+       // so the padding of every stage stays zero), then the T tiles (a
+       // prebuilt image of that region) for the MMA thread
+      for (int e = tid; e < (int)(kStages * kStage / 16); e += kEpiThreads)
+        reinterpret_cast<uint4*>(V)[e] = make_uint4(0u, 0u, 0u, 0u);
+      tc::fence_smem_to_async();
+      tc::mbar_arrive(&stages_zeroed);
       constexpr int kBatch = 6;
       for (int e0 = tid; e0 < a.timage16; e0 += kBatch * kEpiThreads) {
         uint4 img[kBatch];
@@ -217,11 +224,10 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
           if (e < a.timage16) reinterpret_cast<uint4*>(sm)[e] = img[r];
         }
       }
-      for (int e = tid; e < (int)(kStages * kStage / 16); e += kEpiThreads)
-        reinterpret_cast<uint4*>(V)[e] = make_uint4(0u, 0u, 0u, 0u);
       tc::fence_smem_to_async();
-      tc::mbar_arrive(&setup_done);
+      tc::mbar_arrive(&t_ready);
     }
+    pdl_wait();  // the output (and, for z, the values added to) belong to earlier kernels
     // z: the values the epilogue adds to, 8 columns of this thread's x
     auto load8 = [&](long long ob, bool valid, int c0, float2 (&u0)[8]) {
 #pragma unroll
@@ -282,17 +288,26 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
     const int ptid = tid - kEpiThreads, pw = ptid >> 5;
     const int nrows = pg.rows(), nx = a.nx, ncg = (nx + 3) >> 2, nitems = nrows * ncg;
     const long long rstride = pg.row_stride();
+    // per item: offset in a plane, offset in a shared-memory tile, values present
+    int goff[kMaxItems], cnt[kMaxItems];
+    uint32_t soff[kMaxItems];
+#pragma unroll
+    for (int t = 0; t < kMaxItems; ++t) {
+      const int i = ptid + t * kProdThreads;
+      const int j = i / ncg, c = (i - j * ncg) * 4;
+      const bool iv = i < nitems;
+      goff[t] = iv ? (int)(j * rstride) + c : 0;
+      soff[t] = iv ? quad_offset(j, c) : 0u;
+      cnt[t] = iv ? min(4, nx - c) : 0;
+    }
     auto load_items = [&](int plane, float2 (&x)[kMaxItems][4]) {
       const bool pv = plane < a.nplanes;
       const float2* src = a.v + (pv ? pg.base(plane) : 0);
 #pragma unroll
-      for (int t = 0; t < kMaxItems; ++t) {
-        const int i = ptid + t * kProdThreads;
-        const int j = i / ncg, c = (i - j * ncg) * 4;
+      for (int t = 0; t < kMaxItems; ++t)
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          x[t][u] = (pv && i < nitems && c + u < nx) ? __ldg(src + j * rstride + c + u) : make_float2(0.f, 0.f);
-      }
+          x[t][u] = (pv && u < cnt[t]) ? __ldg(src + goff[t] + u) : make_float2(0.f, 0.f);
     };
     auto prefetch_plane = [&](int plane) {  // into L2, one 16-value row segment per thread
       if (plane >= a.nplanes) return;
@@ -300,13 +315,14 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
       if (j < nrows && i < nx) prefetch_l2(a.v + pg.base(plane) + j * rstride + i);
     };
     float2 x[kMaxItems][4];
+    pdl_wait();  // v is written by the previous iteration's update
     load_items(2 * (int)blockIdx.x, x);  // in flight during the setup
     int slot = 0;
     for (int it = 0, pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
       const int st = it & 1;
       const uint32_t par = (uint32_t)(it >> 1) & 1u;
       if (ptid == 0)
-        prod_go = ((it > 0 || tc::mbar_wait(&setup_done, 0u)) && tc::mbar_wait(&v_empty[st], par ^ 1u)) ? 1 : 0;
+        prod_go = ((it > 0 || tc::mbar_wait(&stages_zeroed, 0u)) && tc::mbar_wait(&v_empty[st], par ^ 1u)) ? 1 : 0;
       tc::named_sync(1, kProdThreads);
       if (!prod_go) {
         if (ptid == 0) failed = 1;
@@ -340,16 +356,13 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
         uint8_t* vp = vs + pl * kPlaneSlices;
 #pragma unroll
         for (int t = 0; t < kMaxItems; ++t) {
-          const int i = ptid + t * kProdThreads;
-          if (i < nitems) {
-            const int j = i / ncg, c = (i - j * ncg) * 4;
+          if (cnt[t] > 0) {
             float sl[4][kVS];
 #pragma unroll
             for (int u = 0; u < 4; ++u) slice4(__fmul_rn(x[t][u].x, sc), __fmul_rn(x[t][u].y, sc), sl[u]);
-            const uint32_t off = quad_offset(j, c);
 #pragma unroll
             for (int k = 0; k < kVS; ++k)
-              *reinterpret_cast<uint2*>(vp + k * kTile + off) =
+              *reinterpret_cast<uint2*>(vp + k * kTile + soff[t]) =
                   make_uint2(pack_h2(sl[0][k], sl[1][k]), pack_h2(sl[2][k], sl[3][k]));
           }
         }
@@ -364,7 +377,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
   } else if (lane == 0) {
     // ---- MMA issue ----
     const uint32_t tb = tc::smem_u32(sm);
-    if (!tc::mbar_wait(&setup_done, 0u)) failed = 1;
+    if (!tc::mbar_wait(&t_ready, 0u)) failed = 1;
     for (int it = 0, pair = blockIdx.x; pair < npairs && !failed; pair += gridDim.x, ++it) {
       const int st = it & 1;
       const uint32_t par = (uint32_t)(it >> 1) & 1u;
@@ -492,7 +505,7 @@ int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   cudaFuncSetAttribute(k_kin_xy_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemXY);
   KinTC a{reinterpret_cast<const uint4*>(d.kxy_slices), (int)((kTS + 2) * kTile / 16), d.e_txy, v,
           reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status};
-  k_kin_xy_tc<<<std::min((a.nplanes + 1) / 2, sm_count()), kWsThreads, kSmemXY, s>>>(a);
+  BSL_CUDA(launch_pdl(k_kin_xy_tc, dim3(std::min((a.nplanes + 1) / 2, sm_count())), dim3(kWsThreads), kSmemXY, s, a));
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }
@@ -503,7 +516,7 @@ int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   cudaFuncSetAttribute(k_kin_z_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemZ);
   KinTC a{reinterpret_cast<const uint4*>(d.kz_slices), (int)(kTS * kTile / 16), d.e_tz, v,
           reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status};
-  k_kin_z_tc<<<std::min((a.nplanes + 1) / 2, sm_count()), kWsThreads, kSmemZ, s>>>(a);
+  BSL_CUDA(launch_pdl(k_kin_z_tc, dim3(std::min((a.nplanes + 1) / 2, sm_count())), dim3(kWsThreads), kSmemZ, s, a));
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }

@@ -115,6 +115,10 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
   };
   if (tid == 0 && !abort_flag)
     for (long long g = 0; g < nchunks && g < kStages; ++g) issue(g);
+  // the potential blocks are constant: their first chunks stream in while the
+  // kinetic kernel finishes; everything below reads that kernel's output
+  pdl_launch_dependents();
+  pdl_wait();
 
   const float2* Vp = reinterpret_cast<const float2*>(A.vec);
   float2* Rp = reinterpret_cast<float2*>(A.out);
@@ -259,8 +263,8 @@ int launch_nn(StreamArgs a, cudaStream_t s) {
   const long long slots = (long long)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   a.tiles_per_cta = (tiles + slots - 1) / slots;
   const long long grid = (tiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
-  k_vstream<NN><<<(unsigned)grid, kTilePts, smem, s>>>(a);
-  return BSL_OK;
+  const cudaError_t e = launch_pdl(k_vstream<NN>, dim3((unsigned)grid), dim3(kTilePts), smem, s, a);
+  return e == cudaSuccess ? BSL_OK : cuda_fail(e, "potential stream launch");
 }
 
 }  // namespace
