@@ -219,6 +219,37 @@ __device__ __forceinline__ bool reduce_grid(double part, double* partials, unsig
 }
 
 // ---------------------------------------------------------------------------
+// End of the double-float Lanczos update (the last block, thread 0), given
+// total = ||R_new||^2 with R_new = g (R - alpha c V), g = 2^e: beta, its
+// history, the next folded scales and the next g.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void finish_update_pair(double total, int e, double* scalars, double* hist, int hist_stride,
+                                                   int j, int* status) {
+  const double alpha = scalars[0], sv = scalars[4], sr = scalars[5];
+  const double sr_g = ldexp(sr, -e);  // r = (sr / g) R_new
+  const double b2 = sr_g * sr_g * total;
+  const double b = sqrt(b2);
+  scalars[1] = b;
+  scalars[2] = b2;
+  scalars[3] = 1. / b;
+  hist[hist_stride + j] = b;
+  hist[2 * hist_stride + j] = b2;
+  const double sv_n = sr_g / b, sr_n = -b * sv;
+  scalars[4] = sv_n;
+  scalars[5] = sr_n;
+  scalars[6] = sv_n / sr_n;
+  scalars[7] = sv_n * sr_n;
+  reinterpret_cast<float2*>(scalars)[8] = df_of(sv_n / sr_n);
+  // next update: ||R_next|| = beta_{j+1} / |sr_n| ~ b / |sr_n|, so g = 2^(ilogb(sr_n) - ilogb(b))
+  int en = (b > 0.0 && isfinite(b) && sr_n != 0.0) ? ilogb(sr_n) - ilogb(b) : 0;
+  reinterpret_cast<int*>(scalars)[20] = max(-60, min(60, en));
+  if (!(b > 0.0) || !isfinite(b) || !isfinite(alpha)) {
+    if (status[0] == 0) status[1] = j;
+    status[0] = 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Programmatic dependent launch: the kernels of the Lanczos iteration are
 // launched with programmatic stream serialization, so a kernel's CTAs may start
 // (and run their prologue) while the previous kernel's last CTAs finish.

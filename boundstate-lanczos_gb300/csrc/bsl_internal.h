@@ -206,6 +206,10 @@ struct StreamArgs {
 };
 int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s);
 long long vstream_tile_points();
+// double-float update R = g (R - alpha c V), beta and the next scales, streamed
+// with bulk copies (V, R 16-byte aligned; partials sized for 2 CTAs per SM)
+int launch_update_stream(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
+                         double* scalars, double* hist, int hist_stride, int j, int* status, cudaStream_t s);
 int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
                       const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
                       double* scalars, double* hist, int j, long long dpk);

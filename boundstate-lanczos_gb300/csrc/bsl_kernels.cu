@@ -530,30 +530,8 @@ __global__ void __launch_bounds__(256, 3) k_update_pair(const float2* __restrict
     if (v32_next && i < D) v32_next[i] = r.x;
   }
   double total;
-  if (reduce_grid_df(acc, partials, counter, &total) && threadIdx.x == 0) {
-    const double alpha = scalars[0], sv = scalars[4], sr = scalars[5];
-    const double sr_g = ldexp(sr, -e);  // r = (sr / g) R_new
-    const double b2 = sr_g * sr_g * total;
-    const double b = sqrt(b2);
-    scalars[1] = b;
-    scalars[2] = b2;
-    scalars[3] = 1. / b;
-    hist[hist_stride + j] = b;
-    hist[2 * hist_stride + j] = b2;
-    const double sv_n = sr_g / b, sr_n = -b * sv;
-    scalars[4] = sv_n;
-    scalars[5] = sr_n;
-    scalars[6] = sv_n / sr_n;
-    scalars[7] = sv_n * sr_n;
-    reinterpret_cast<float2*>(scalars)[8] = df_of(sv_n / sr_n);
-    // next update: ||R_next|| = beta_{j+1} / |sr_n| ~ b / |sr_n|, so g = 2^(ilogb(sr_n) - ilogb(b))
-    int en = (b > 0.0 && isfinite(b) && sr_n != 0.0) ? ilogb(sr_n) - ilogb(b) : 0;
-    reinterpret_cast<int*>(scalars)[20] = max(-60, min(60, en));
-    if (!(b > 0.0) || !isfinite(b) || !isfinite(alpha)) {
-      if (status[0] == 0) status[1] = j;
-      status[0] = 1;
-    }
-  }
+  if (reduce_grid_df(acc, partials, counter, &total) && threadIdx.x == 0)
+    finish_update_pair(total, e, scalars, hist, hist_stride, j, status);
 }
 
 // double-float pairs of an FP64 vector
@@ -929,6 +907,9 @@ int dev_hv(bsl_handle* h, const double* v, double* u, cudaStream_t s) {
 // r -= alpha v, beta and the next scales, on FP64 or double-float buffers
 int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaStream_t s) {
   DeviceState& d = h->d;
+  if (h->state_pairs == 1 && h->kinetic_engine == BSL_KIN_TENSOR)  // nothing reads an FP32 copy of v
+    return launch_update_stream(reinterpret_cast<const float2*>(V), reinterpret_cast<float2*>(R), L, d.partials,
+                                d.counter, d.scalars, d.hist, d.hist_cap, j, d.status, s);
   if (h->state_pairs == 1)
     BSL_CUDA(launch_pdl(k_update_pair, dim3(d.pair_blocks), dim3(kThreads), 0, s, reinterpret_cast<const float2*>(V),
                         reinterpret_cast<float2*>(R), L, h->kinetic_engine == BSL_KIN_TENSOR ? nullptr : d.v32, L - 1,
@@ -994,7 +975,7 @@ const char* dev_stage_name(bsl_handle* h, int i) {
   const bool mixed = h->precision == BSL_PREC_MIXED;
   static const char* n64[4] = {"k_kin_xy_f64", "k_kin_z_f64", "k_vapply<NN,double>", "k_update_fold"};
   static const char* nmx[4] = {"k_kin_xy_split", "k_kin_z_split", "k_vstream<NN>", "k_update_pair"};
-  static const char* ntc[4] = {"k_kin_xy_tc", "k_kin_z_tc", "k_vstream<NN>", "k_update_pair"};
+  static const char* ntc[4] = {"k_kin_xy_tc", "k_kin_z_tc", "k_vstream<NN>", "k_update_stream"};
   if (!mixed) return n64[i];
   return h->kinetic_engine == BSL_KIN_TENSOR ? ntc[i] : nmx[i];
 }

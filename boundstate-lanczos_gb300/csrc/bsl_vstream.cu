@@ -267,7 +267,132 @@ int launch_nn(StreamArgs a, cudaStream_t s) {
   return e == cudaSuccess ? BSL_OK : cuda_fail(e, "potential stream launch");
 }
 
+// ---------------------------------------------------------------------------
+// Double-float Lanczos update R = g (R - alpha c V) and ||R||^2 (the same
+// arithmetic as k_update_pair), streamed: CTA b owns a contiguous range of
+// 16-byte units (two pairs) of V and R, brings them in chunks of kUpdUnits
+// units per array through a kUpdStages-stage ring of bulk copies, updates R in
+// shared memory and writes it back with bulk stores.
+// ---------------------------------------------------------------------------
+constexpr int kUpdThreads = 256;
+constexpr int kUpdUnits = 1024;  // 16 KiB of V and 16 KiB of R per chunk
+constexpr int kUpdStages = 3;
+
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+               "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const float4* __restrict__ V4, float4* __restrict__ R4,
+                                                                  long long L, long long units_per_cta,
+                                                                  double* partials, unsigned int* counter,
+                                                                  double* scalars, double* hist, int hist_stride,
+                                                                  int j, int* status) {
+  extern __shared__ float4 upd[];  // [stage][V, R][kUpdUnits]
+  __shared__ uint64_t full[kUpdStages];
+  __shared__ int failed;
+  const int tid = threadIdx.x;
+  const long long L2 = L / 2;
+  const long long u0 = (long long)blockIdx.x * units_per_cta;
+  const long long u1 = u0 + units_per_cta < L2 ? u0 + units_per_cta : L2;
+  const long long nchunks = u1 > u0 ? (u1 - u0 + kUpdUnits - 1) / kUpdUnits : 0;
+  if (tid == 0) {
+    for (int s = 0; s < kUpdStages; ++s) mbar_init(&full[s], 1);
+    failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  pdl_launch_dependents();
+  pdl_wait();  // R and alpha come from the potential stream
+  const float2 na = reinterpret_cast<const float2*>(scalars)[9];  // -alpha c
+  const int e = reinterpret_cast<const int*>(scalars)[20];
+  const float g = ldexpf(1.f, e);
+  auto chunk_units = [&](long long k) { return (int)(u1 - (u0 + k * kUpdUnits) < kUpdUnits ? u1 - (u0 + k * kUpdUnits) : kUpdUnits); };
+  long long issued = 0;
+  auto issue = [&](long long k) {  // thread 0
+    const int st = (int)(k % kUpdStages);
+    const long long c0 = u0 + k * kUpdUnits;
+    const uint32_t bytes = (uint32_t)chunk_units(k) * 16u;
+    mbar_expect_tx(&full[st], 2 * bytes);
+    bulk_copy(upd + (size_t)(2 * st) * kUpdUnits, V4 + c0, bytes, &full[st]);
+    bulk_copy(upd + (size_t)(2 * st + 1) * kUpdUnits, R4 + c0, bytes, &full[st]);
+    issued = k + 1;
+  };
+  if (tid == 0)
+    for (long long k = 0; k < nchunks && k < kUpdStages; ++k) issue(k);
+  float2 acc = make_float2(0.f, 0.f);
+  for (long long k = 0; k < nchunks; ++k) {
+    const int st = (int)(k % kUpdStages);
+    if (!mbar_wait(&full[st], (uint32_t)((k / kUpdStages) & 1))) failed = 1;
+    __syncthreads();
+    if (failed) break;
+    const int n = chunk_units(k);
+    const float4* vs = upd + (size_t)(2 * st) * kUpdUnits;
+    float4* rs = upd + (size_t)(2 * st + 1) * kUpdUnits;
+    for (int q = tid; q < n; q += kUpdThreads) {
+      const float4 v = vs[q], r = rs[q];
+      const float2 r0 = df_scale2(df_fma_fast(na, make_float2(v.x, v.y), make_float2(r.x, r.y)), g);
+      const float2 r1 = df_scale2(df_fma_fast(na, make_float2(v.z, v.w), make_float2(r.z, r.w)), g);
+      rs[q] = make_float4(r0.x, r0.y, r1.x, r1.y);
+      acc = df_add_fast(df_sqr(r0), acc);
+      acc = df_add_fast(df_sqr(r1), acc);
+    }
+    __syncthreads();  // the chunk's new R is complete in shared memory
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bulk_store(R4 + u0 + k * kUpdUnits, rs, (uint32_t)n * 16u);
+      if (k + kUpdStages < nchunks) {
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the store has read this stage
+        issue(k + kUpdStages);
+      }
+    }
+  }
+  if (tid == 0) {
+    if (failed) {  // let the copies in flight land (bounded) before the shared memory is released
+      status[2] = 1;
+      for (long long k = issued - kUpdStages; k < issued; ++k)
+        if (k >= 0) mbar_wait(&full[k % kUpdStages], (uint32_t)((k / kUpdStages) & 1));
+    }
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  }
+  if ((L & 1) && blockIdx.x == 0 && tid == 0) {  // the coordinate outside the symmetry block
+    const long long i = L - 1;
+    const float2* V = reinterpret_cast<const float2*>(V4);
+    float2* R = reinterpret_cast<float2*>(R4);
+    const float2 r = df_scale2(df_fma_fast(na, V[i], R[i]), g);
+    R[i] = r;
+    acc = df_add_fast(df_sqr(r), acc);
+  }
+  double total;
+  if (reduce_grid_df(acc, partials, counter, &total) && tid == 0)
+    finish_update_pair(total, e, scalars, hist, hist_stride, j, status);
+}
+
 }  // namespace
+
+int launch_update_stream(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
+                         double* scalars, double* hist, int hist_stride, int j, int* status, cudaStream_t s) {
+  const size_t smem = (size_t)kUpdStages * 2 * kUpdUnits * sizeof(float4);
+  cudaFuncSetAttribute(k_update_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long grid = 2LL * (sms > 0 ? sms : 1);
+  const long long L2 = L / 2;
+  const long long per = (L2 + grid - 1) / grid;
+  BSL_CUDA(launch_pdl(k_update_stream, dim3((unsigned)grid), dim3(kUpdThreads), smem, s,
+                      reinterpret_cast<const float4*>(V), reinterpret_cast<float4*>(R), L, per, partials, counter,
+                      scalars, hist, hist_stride, j, status));
+  return BSL_OK;
+}
 
 long long vstream_tile_points() { return kTilePts; }
 
