@@ -169,7 +169,8 @@ def measured_peak_hbm():
 NCU_TRAFFIC = {"k_kin_xy_tc": (26.64e6, "profiles/k_kin_xy_tc_54cubed_odd_l5.md"),
                "k_kin_z_tc": (53.18e6, "profiles/k_kin_z_tc_54cubed_odd_l5.md"),
                "k_vstream<NN>": (229.43e6, "profiles/k_vstream_54cubed_odd_l5.md"),
-               "k_update_pair": (52.96e6, "profiles/k_update_pair_54cubed_odd_l5.md")}
+               "k_update_pair": (52.96e6, "profiles/k_update_pair_54cubed_odd_l5.md"),
+               "k_update_stream": (52.96e6, "profiles/k_update_pair_54cubed_odd_l5.md")}
 
 
 def stage_bytes(cfg, D, N, nn, mixed):
