@@ -329,6 +329,7 @@ void free_device(DeviceState& d) {
   if (d.vpair) cudaFree(d.vpair);
   if (d.kxy_slices) cudaFree(d.kxy_slices);
   if (d.kz_slices) cudaFree(d.kz_slices);
+  if (d.jdev) cudaFree(d.jdev);
   if (d.copy_done) cudaEventDestroy(d.copy_done);
   if (d.vec_in) cudaEventDestroy(d.vec_in);
   if (d.copy_stream) cudaStreamDestroy(d.copy_stream);
@@ -464,7 +465,7 @@ int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
   const size_t nparts = std::max((size_t)d.red_blocks, (N + 63) / 64) + 64;
   if ((rc = dalloc(&d.partials, nparts, "reduction scratch")) ||
       (rc = dalloc(&d.counter, 4, "reduction counter")) || (rc = dalloc(&d.scalars, 16, "scalars")) ||
-      (rc = dalloc(&d.status, 4, "status")))
+      (rc = dalloc(&d.status, 4, "status")) || (rc = dalloc(&d.jdev, 1, "iteration counter")))
     return bail(rc);
   if ((e = cudaMemset(d.counter, 0, 4 * sizeof(unsigned int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));
   if ((e = cudaMemset(d.status, 0, 4 * sizeof(int))) != cudaSuccess) return bail(cuda_fail(e, "memset"));

@@ -131,6 +131,7 @@ struct DeviceState {
   double* ritz = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int red_blocks = 0;
+  int* jdev = nullptr;  // iteration counter of graph-replayed Lanczos loops
   int pair_blocks = 0;  // grid of the double-float update: a few resident blocks per SM
 };
 
@@ -154,6 +155,8 @@ namespace bsl {
 // ---- kernel launchers (bsl_kernels.cu) -----------------------------------
 int dev_potential_alavi(bsl_handle* h);
 int dev_potential_iso(bsl_handle* h);
+int dev_set_iteration(bsl_handle* h, int j, cudaStream_t s);
+bool device_counted_iterations(const bsl_handle* h);
 int dev_potential_point_alavi(bsl_handle* h);
 int dev_potential_coulomb(bsl_handle* h);
 int dev_vblocks(bsl_handle* h);
@@ -199,7 +202,8 @@ struct StreamArgs {
   double* out;          // mode 0: u = H v; mode 1: the Lanczos r buffer (r += c H v)
   long long npts, dpk;
   long long tiles_per_cta;  // set by the launcher
-  int mode, j;
+  int mode, j;          // j > 0: the iteration; j == 0: read it from *jdev
+  const int* jdev;
   double *partials, *scalars, *hist;
   unsigned int* counter;
   int* status;
@@ -208,8 +212,10 @@ int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s);
 long long vstream_tile_points();
 // double-float update R = g (R - alpha c V), beta and the next scales, streamed
 // with bulk copies (V, R 16-byte aligned; partials sized for 2 CTAs per SM)
+// j == 0: the iteration is read from *jdev, which the last block then advances
 int launch_update_stream(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
-                         double* scalars, double* hist, int hist_stride, int j, int* status, cudaStream_t s);
+                         double* scalars, double* hist, int hist_stride, int j, int* jdev, int* status,
+                         cudaStream_t s);
 int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
                       const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
                       double* scalars, double* hist, int j, long long dpk);

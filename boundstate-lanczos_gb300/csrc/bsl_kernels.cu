@@ -609,6 +609,7 @@ int launch_vapply(bsl_handle* h, const double* v, double* out, int mode, int j, 
     a.dpk = dpk;
     a.mode = mode;
     a.j = j;
+    a.jdev = d.jdev;
     a.partials = d.partials;
     a.scalars = d.scalars;
     a.hist = d.hist;
@@ -909,7 +910,7 @@ int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaS
   DeviceState& d = h->d;
   if (h->state_pairs == 1 && h->kinetic_engine == BSL_KIN_TENSOR)  // nothing reads an FP32 copy of v
     return launch_update_stream(reinterpret_cast<const float2*>(V), reinterpret_cast<float2*>(R), L, d.partials,
-                                d.counter, d.scalars, d.hist, d.hist_cap, j, d.status, s);
+                                d.counter, d.scalars, d.hist, d.hist_cap, j, d.jdev, d.status, s);
   if (h->state_pairs == 1)
     BSL_CUDA(launch_pdl(k_update_pair, dim3(d.pair_blocks), dim3(kThreads), 0, s, reinterpret_cast<const float2*>(V),
                         reinterpret_cast<float2*>(R), L, h->kinetic_engine == BSL_KIN_TENSOR ? nullptr : d.v32, L - 1,
@@ -919,6 +920,24 @@ int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaS
                                                     d.hist_cap, j, d.status);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
+}
+
+namespace {
+__global__ void k_set_int(int* p, int v) { *p = v; }
+}  // namespace
+
+// the iteration counter read by the kernels of an iteration launched with j = 0
+int dev_set_iteration(bsl_handle* h, int j, cudaStream_t s) {
+  k_set_int<<<1, 1, 0, s>>>(h->d.jdev, j);
+  BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+// Iterations whose kernels take j from the device counter (and so can be
+// captured once and replayed): the double-float path with the tensor-core
+// kinetic and the streamed update.
+bool device_counted_iterations(const bsl_handle* h) {
+  return h->precision == BSL_PREC_MIXED && h->state_pairs == 1 && h->kinetic_engine == BSL_KIN_TENSOR;
 }
 
 int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s) {

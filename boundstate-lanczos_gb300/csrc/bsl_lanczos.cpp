@@ -122,6 +122,68 @@ int check_status(bsl_handle* h) {
   return BSL_OK;
 }
 
+// niter Lanczos iterations of one problem on stream s.  Where the iteration's
+// kernels can take j from the device counter, kGraphIters iterations are
+// captured once into a CUDA graph (programmatic launches become programmatic
+// edges) and replayed; an even count leaves the buffer roles as they were.
+// The remainder, and every other configuration, is launched directly.
+constexpr int kGraphIters = 8;
+
+struct IterationGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~IterationGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
+// capture kGraphIters device-counted iterations of h on s (nothing runs)
+int capture_iterations(bsl_handle* h, cudaStream_t s, IterationGraph* g) {
+  BSL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+  int rc = BSL_OK;
+  for (int i = 0; i < kGraphIters && rc == BSL_OK; ++i) rc = dev_lanczos_iteration(h, 0, s);
+  const cudaError_t e = cudaStreamEndCapture(s, &g->graph);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  BSL_CUDA(cudaGraphInstantiate(&g->exec, g->graph, 0));
+  return BSL_OK;
+}
+
+// the iterations of several problems, iteration blocks interleaved across
+// their streams; graphs[b] must outlive the launches (synchronise first)
+int run_iterations(bsl_handle** hs, int n, int niter, std::vector<IterationGraph>* graphs) {
+  graphs->resize(n);
+  std::vector<char> counted(n, 0);
+  int rc;
+  for (int b = 0; b < n; ++b) {
+    bsl_handle* h = hs[b];
+    cudaSetDevice(h->p.device);
+    counted[b] = device_counted_iterations(h) ? 1 : 0;
+    if (!counted[b]) continue;
+    if ((rc = dev_set_iteration(h, 1, h->d.stream))) return rc;
+    if (niter >= kGraphIters && (rc = capture_iterations(h, h->d.stream, &(*graphs)[b]))) return rc;
+  }
+  const int nblocks = niter / kGraphIters;
+  for (int k = 0; k < nblocks; ++k)
+    for (int b = 0; b < n; ++b) {
+      bsl_handle* h = hs[b];
+      cudaSetDevice(h->p.device);
+      if (counted[b]) {
+        BSL_CUDA(cudaGraphLaunch((*graphs)[b].exec, h->d.stream));
+      } else {
+        for (int i = 0; i < kGraphIters; ++i)
+          if ((rc = dev_lanczos_iteration(h, k * kGraphIters + i + 1, h->d.stream))) return rc;
+      }
+    }
+  for (int j = nblocks * kGraphIters + 1; j <= niter; ++j)
+    for (int b = 0; b < n; ++b) {
+      cudaSetDevice(hs[b]->p.device);
+      if ((rc = dev_lanczos_iteration(hs[b], counted[b] ? 0 : j, hs[b]->d.stream))) return rc;
+    }
+  return BSL_OK;
+}
+
 }  // namespace
 }  // namespace bsl
 
@@ -137,9 +199,12 @@ int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed
   int rc;
   if ((rc = ensure_hist(h, niter)) || (rc = init_state(h, start, seed))) return rc;
   cudaStream_t s = d.stream;
+  std::vector<IterationGraph> graphs;
   BSL_CUDA(cudaEventRecord(d.ev0, s));
-  for (int j = 1; j <= niter; ++j)
-    if ((rc = dev_lanczos_iteration(h, j, s))) return rc;
+  if ((rc = run_iterations(&h, 1, niter, &graphs))) {
+    cudaStreamSynchronize(s);  // nothing of a replayed graph may still run when it is destroyed
+    return rc;
+  }
   BSL_CUDA(cudaEventRecord(d.ev1, s));
   BSL_CUDA(cudaStreamSynchronize(s));
   float ms = 0.f;
@@ -170,13 +235,13 @@ int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned
     cudaSetDevice(hs[b]->p.device);
     if ((rc = ensure_hist(hs[b], niter)) || (rc = init_state(hs[b], start, seed))) return rc;
   }
-  // iteration j of every problem before iteration j + 1 of any: each problem
-  // runs on its own stream, so the kernels of different problems overlap
-  for (int j = 1; j <= niter; ++j)
-    for (int b = 0; b < n; ++b) {
-      cudaSetDevice(hs[b]->p.device);
-      if ((rc = dev_lanczos_iteration(hs[b], j, hs[b]->d.stream))) return rc;
-    }
+  // blocks of iterations interleaved across the problems' streams, so the
+  // kernels of different problems overlap
+  std::vector<IterationGraph> graphs;
+  if ((rc = run_iterations(hs, n, niter, &graphs))) {
+    for (int b = 0; b < n; ++b) cudaStreamSynchronize(hs[b]->d.stream);
+    return rc;
+  }
   for (int b = 0; b < n; ++b) {
     bsl_handle* h = hs[b];
     cudaSetDevice(h->p.device);

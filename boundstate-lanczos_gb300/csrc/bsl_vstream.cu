@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kTilePts) k_vstream(const StreamArgs A) {
     if (last && threadIdx.x == 0) {
       const double alpha = A.scalars[7] * total;
       A.scalars[0] = alpha;
-      A.hist[A.j - 1] = alpha;
+      A.hist[(A.j > 0 ? A.j : *A.jdev) - 1] = alpha;
       reinterpret_cast<float2*>(A.scalars)[9] = df_of(-alpha * A.scalars[6]);  // for the pair update
     }
   }
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const float4* 
                                                                   long long L, long long units_per_cta,
                                                                   double* partials, unsigned int* counter,
                                                                   double* scalars, double* hist, int hist_stride,
-                                                                  int j, int* status) {
+                                                                  int j_arg, int* jdev, int* status) {
   extern __shared__ float4 upd[];  // [stage][V, R][kUpdUnits]
   __shared__ uint64_t full[kUpdStages];
   __shared__ int failed;
@@ -312,6 +312,7 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const float4* 
   __syncthreads();
   pdl_launch_dependents();
   pdl_wait();  // R and alpha come from the potential stream
+  const int j = j_arg > 0 ? j_arg : *jdev;
   const float2 na = reinterpret_cast<const float2*>(scalars)[9];  // -alpha c
   const int e = reinterpret_cast<const int*>(scalars)[20];
   const float g = ldexpf(1.f, e);
@@ -372,14 +373,17 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const float4* 
     acc = df_add_fast(df_sqr(r), acc);
   }
   double total;
-  if (reduce_grid_df(acc, partials, counter, &total) && tid == 0)
+  if (reduce_grid_df(acc, partials, counter, &total) && tid == 0) {
     finish_update_pair(total, e, scalars, hist, hist_stride, j, status);
+    if (j_arg <= 0) *jdev = j + 1;  // every block has read j before the last one gets here
+  }
 }
 
 }  // namespace
 
 int launch_update_stream(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
-                         double* scalars, double* hist, int hist_stride, int j, int* status, cudaStream_t s) {
+                         double* scalars, double* hist, int hist_stride, int j, int* jdev, int* status,
+                         cudaStream_t s) {
   const size_t smem = (size_t)kUpdStages * 2 * kUpdUnits * sizeof(float4);
   cudaFuncSetAttribute(k_update_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int dev = 0, sms = 0;
@@ -390,7 +394,7 @@ int launch_update_stream(const float2* V, float2* R, long long L, double* partia
   const long long per = (L2 + grid - 1) / grid;
   BSL_CUDA(launch_pdl(k_update_stream, dim3((unsigned)grid), dim3(kUpdThreads), smem, s,
                       reinterpret_cast<const float4*>(V), reinterpret_cast<float4*>(R), L, per, partials, counter,
-                      scalars, hist, hist_stride, j, status));
+                      scalars, hist, hist_stride, j, jdev, status));
   return BSL_OK;
 }
 
