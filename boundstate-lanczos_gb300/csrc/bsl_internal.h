@@ -169,7 +169,8 @@ const char* dev_stage_name(bsl_handle* h, int i);
 int dev_fill_start(bsl_handle* h, int start, unsigned long long seed, cudaStream_t s);
 int dev_gather_packed(bsl_handle* h, const double* full, double* packed, cudaStream_t s);
 int dev_hv_full(bsl_handle* h, const double* full, double* out, cudaStream_t s);
-int dev_full_step_fused(bsl_handle* h, double* v, double* r, long long L, const double* hv, int j, cudaStream_t s);
+int dev_full_step_fused(bsl_handle* h, double* v, double* r, long long L, const double* hv, int j, cudaStream_t s,
+                        double* v_out = nullptr, double* r_out = nullptr);
 int dev_scatter_full(bsl_handle* h, const double* packed, double* full_accum, cudaStream_t s);
 int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, int ngood, double* ritz,
                         cudaStream_t s);

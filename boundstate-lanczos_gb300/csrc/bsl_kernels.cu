@@ -399,6 +399,20 @@ __global__ void k_normalize_fused(double* __restrict__ v, double* __restrict__ r
   }
 }
 
+// the same, written to other buffers (the caller's host vec and rvec, mapped
+// into the device address space, so the results cross the host link once)
+__global__ void k_normalize_to(const double* __restrict__ v, const double* __restrict__ r, long long L,
+                               const double* __restrict__ scalars, double* __restrict__ v_out,
+                               double* __restrict__ r_out) {
+  const double alpha = scalars[0], b = scalars[1], inv = scalars[3];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x) {
+    const double vi = v[i];
+    const double x = r[i] - alpha * vi;
+    v_out[i] = inv * x;
+    r_out[i] = (-b) * vi;
+  }
+}
+
 // packed FP32 copy and double-float pairs of a full-layout FP64 vector
 __global__ void k_gather_mixed(const double* __restrict__ full, float* __restrict__ v32, float2* __restrict__ vpair,
                                const int* __restrict__ full_of, long long npts, int nn) {
@@ -1051,13 +1065,17 @@ int dev_hv_full(bsl_handle* h, const double* full, double* out, cudaStream_t s) 
 }
 
 // The full-layout host step after H v: r += S H v, alpha, beta, normalise and swap.
-int dev_full_step_fused(bsl_handle* h, double* v, double* r, long long L, const double* hv, int j, cudaStream_t s) {
+int dev_full_step_fused(bsl_handle* h, double* v, double* r, long long L, const double* hv, int j, cudaStream_t s,
+                        double* v_out, double* r_out) {
   DeviceState& d = h->d;
   const int g = d.red_blocks;
   k_scatter_dot<<<g, kThreads, 0, s>>>(v, r, L, hv, d.packed_of, h->t.npts, h->t.nn_full, d.partials, d.counter,
                                        d.scalars, d.hist, j);
   k_beta_only<<<g, kThreads, 0, s>>>(v, r, L, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, j, d.status);
-  k_normalize_fused<<<g, kThreads, 0, s>>>(v, r, L, d.scalars);
+  if (v_out)
+    k_normalize_to<<<g, kThreads, 0, s>>>(v, r, L, d.scalars, v_out, r_out);
+  else
+    k_normalize_fused<<<g, kThreads, 0, s>>>(v, r, L, d.scalars);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }

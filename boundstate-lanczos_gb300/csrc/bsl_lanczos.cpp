@@ -39,6 +39,16 @@ int ensure_hist(bsl_handle* h, int niter) {
   return BSL_OK;
 }
 
+// device address of a page-locked (pinned or registered) host buffer, or null
+double* mapped_host(double* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? static_cast<double*>(a.devicePointer) : nullptr;
+}
+
 int ensure_staging(bsl_handle* h) {
   DeviceState& d = h->d;
   if (!d.copy_stream) {
@@ -286,9 +296,16 @@ int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alph
   h->state_pairs = -1;
   if ((rc = dev_hv_full(h, d.ref_vec, d.rvec, s))) return rc;
   BSL_CUDA(cudaStreamWaitEvent(s, d.copy_done, 0));
-  if ((rc = dev_full_step_fused(h, d.ref_vec, d.ref_out, (long long)Df, d.rvec, 1, s))) return rc;
-  BSL_CUDA(cudaMemcpyAsync(vec, d.ref_vec, Df * sizeof(double), cudaMemcpyDeviceToHost, s));
-  BSL_CUDA(cudaMemcpyAsync(rvec, d.ref_out, Df * sizeof(double), cudaMemcpyDeviceToHost, s));
+  // page-locked caller buffers are written by the last pass itself; others by copies
+  double* vec_d = mapped_host(vec);
+  double* rvec_d = vec_d ? mapped_host(rvec) : nullptr;
+  if (vec_d && rvec_d) {
+    if ((rc = dev_full_step_fused(h, d.ref_vec, d.ref_out, (long long)Df, d.rvec, 1, s, vec_d, rvec_d))) return rc;
+  } else {
+    if ((rc = dev_full_step_fused(h, d.ref_vec, d.ref_out, (long long)Df, d.rvec, 1, s))) return rc;
+    BSL_CUDA(cudaMemcpyAsync(vec, d.ref_vec, Df * sizeof(double), cudaMemcpyDeviceToHost, s));
+    BSL_CUDA(cudaMemcpyAsync(rvec, d.ref_out, Df * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
   double sc[3];
   BSL_CUDA(cudaMemcpyAsync(sc, d.scalars, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   BSL_CUDA(cudaStreamSynchronize(s));

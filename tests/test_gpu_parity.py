@@ -195,6 +195,28 @@ def test_step_host_matches_oracle_loop(bsl):
     h.close()
 
 
+def test_step_host_pinned_buffers_match_pageable(bsl):
+    """Page-locked vec/rvec are written by the step's last pass directly; the
+    results are bit-identical to the copy path of ordinary host memory."""
+    torch = pytest.importorskip("torch")
+    h, d, man, extra = make(bsl, "seed1_n6_l3_odd")
+    D = h.basis_size
+    out = []
+    for pinned in (False, True):
+        if pinned:
+            vec = torch.empty(D, dtype=torch.float64, pin_memory=True).numpy()
+            rvec = torch.empty(D, dtype=torch.float64, pin_memory=True).numpy()
+        else:
+            vec, rvec = np.empty(D), np.empty(D)
+        vec[:] = 1.0 / np.sqrt(D)
+        rvec[:] = 0.0
+        ab = [h.step_host(vec, rvec) for _ in range(4)]
+        out.append((np.array(ab), vec.copy(), rvec.copy()))
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(x, y)
+    h.close()
+
+
 def test_ritz_vectors_match_oracle(bsl):
     import ctypes as C
     from conftest import load_oracle, ptr
