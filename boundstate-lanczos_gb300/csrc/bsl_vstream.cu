@@ -401,9 +401,9 @@ int launch_update_stream(const float2* V, float2* R, long long L, double* partia
 long long vstream_tile_points() { return kTilePts; }
 
 int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s) {
-#define BSL_CASE(K)      \
-  case K:                \
-    launch_nn<K>(a, s);  \
+#define BSL_CASE(K)                          \
+  case K:                                    \
+    if (int rc = launch_nn<K>(a, s)) return rc; \
     break;
   switch (nn) {
     BSL_CASE(1)
