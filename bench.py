@@ -166,11 +166,10 @@ def measured_peak_hbm():
 # DRAM bytes (read + write) per launch from one ncu capture of each mixed-path
 # kernel at the metric workload (profiles/k_*_54cubed_odd_l5.md).  Writes that
 # stay in L2 until after the kernel are not counted there.
-NCU_TRAFFIC = {"k_kin_xy_tc": (26.64e6, "profiles/k_kin_xy_tc_54cubed_odd_l5.md"),
-               "k_kin_z_tc": (53.18e6, "profiles/k_kin_z_tc_54cubed_odd_l5.md"),
-               "k_vstream<NN>": (229.43e6, "profiles/k_vstream_54cubed_odd_l5.md"),
-               "k_update_pair": (52.96e6, "profiles/k_update_pair_54cubed_odd_l5.md"),
-               "k_update_stream": (52.96e6, "profiles/k_update_pair_54cubed_odd_l5.md")}
+NCU_TRAFFIC = {"k_kin_xy_tc": (26.65e6, "profiles/k_kin_xy_tc_54cubed_odd_l5.md"),
+               "k_kin_z_tc": (53.25e6, "profiles/k_kin_z_tc_54cubed_odd_l5.md"),
+               "k_vstream<NN>": (229.62e6, "profiles/k_vstream_54cubed_odd_l5.md"),
+               "k_update_stream": (52.95e6, "profiles/k_update_stream_54cubed_odd_l5.md")}
 
 
 def stage_bytes(cfg, D, N, nn, mixed):
