@@ -172,6 +172,33 @@ NCU_TRAFFIC = {"k_kin_xy_tc": (26.65e6, "profiles/k_kin_xy_tc_54cubed_odd_l5.md"
                "k_update_stream": (52.95e6, "profiles/k_update_stream_54cubed_odd_l5.md")}
 
 
+def sync_ranks(dist):
+    """Finish this rank's GPU work, then wait for every rank (replicas only:
+    the ranks share nothing but this barrier and the timing maximum)."""
+    import torch
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(x, dist):
+    """The largest value of x over the ranks: the slowest replica's time."""
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank, seconds, world):
+    """Whole-job rate of world independent replicas (weak scaling): all the
+    ranks' units over the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
 def stage_bytes(cfg, D, N, nn, mixed):
     """Algorithmic bytes per launch of each stage of one Lanczos iteration."""
     ntri = nn * (nn + 1) // 2
@@ -256,9 +283,7 @@ def main():
         return
 
     def barrier():
-        torch.cuda.synchronize()
-        if dist is not None:
-            dist.barrier()
+        sync_ranks(dist)
 
     # ---- device-resident mixed path (value) ----
     h.lanczos(max(3, args.warmup))
@@ -269,12 +294,8 @@ def main():
         barrier()
         wall = time.perf_counter() - t0
     ms_event = h.last_ms_per_iter()
-    ms_step = ms_event
-    if dist is not None:
-        t = torch.tensor([ms_step], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * 1000.0 / ms_step
+    ms_step = max_over_ranks(ms_event, dist)
+    value = replica_rate(1000.0, ms_step, world)
 
     # ---- per-kernel times (CUDA events around each launch on the library stream) ----
     stage_ms = np.zeros(5)
@@ -301,12 +322,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         h.step_host(vec, rvec)
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * args.e2e_steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e_value = replica_rate(args.e2e_steps, e2e_s, world)
     # the transfer floor of that path: the same bytes between pinned host memory
     # and the device through torch, each direction on its own
     dv = torch.empty(Df, dtype=torch.float64, device="cuda")
