@@ -163,13 +163,14 @@ def measured_peak_hbm():
         return 6800.0, "fallback 6.8 TB/s"
 
 
-# DRAM bytes (read + write) per launch from one ncu capture of each mixed-path
-# kernel at the metric workload (profiles/k_*_54cubed_odd_l5.md).  Writes that
-# stay in L2 until after the kernel are not counted there.
-NCU_TRAFFIC = {"k_kin_xy_tc": (26.65e6, "profiles/k_kin_xy_tc_54cubed_odd_l5.md"),
-               "k_kin_z_tc": (53.25e6, "profiles/k_kin_z_tc_54cubed_odd_l5.md"),
-               "k_vstream<NN>": (229.62e6, "profiles/k_vstream_54cubed_odd_l5.md"),
-               "k_update_stream": (52.95e6, "profiles/k_update_stream_54cubed_odd_l5.md")}
+# DRAM bytes (read + write) per launch of each mixed-path kernel in the running
+# iteration: one-pass ncu capture with the L2 left as the previous kernel left it
+# (profiles/pipeline_traffic_warm_54cubed_odd_l5.md).
+_TRAFFIC_SRC = "profiles/pipeline_traffic_warm_54cubed_odd_l5.md"
+NCU_TRAFFIC = {"k_kin_xy_tc": (12.35e6, _TRAFFIC_SRC),
+               "k_kin_z_tc": (2.90e6, _TRAFFIC_SRC),
+               "k_vstream<NN>": (201.72e6, _TRAFFIC_SRC),
+               "k_update_stream": (10.19e6, _TRAFFIC_SRC)}
 
 
 def sync_ranks(dist):
