@@ -75,7 +75,9 @@ def config_record(cfg, D=None, Df=None, precision="mixed"):
 # (serial kinetic, OpenMP potential blocks), on the same basis sizes with
 # synthetic block values (the cost does not depend on the values).
 # --------------------------------------------------------------------------
-def cpu_baseline(cfg, budget_s=15.0):
+def cpu_baseline(cfg, budget_s=15.0, max_iters=30, warmup=1):
+    """`warmup` untimed iterations (at least one, which also sizes the sample),
+    then min(max_iters, budget_s / one iteration) timed iterations (at least 1)."""
     if not os.path.exists(ORACLE_LIB):
         subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "port"], check=True, capture_output=True)
     L = C.CDLL(ORACLE_LIB)
@@ -98,7 +100,9 @@ def cpu_baseline(cfg, budget_s=15.0):
         return L.orc_lanczos(h, n, None, a.ctypes.data_as(P), b.ctypes.data_as(P), b2.ctypes.data_as(P), cores)
 
     t1 = run(1)
-    n = int(max(2, min(30, budget_s / max(t1, 1e-3))))
+    for _ in range(max(0, warmup - 1)):
+        run(1)
+    n = int(max(1, min(max_iters, budget_s / max(t1, 1e-3))))
     t = run(n)
     L.orc_destroy(h)
     return {"value": n / t, "unit": UNIT, "cores": cores, "kind": "port",
@@ -249,13 +253,18 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_baseline(cfg, budget_s=max(5.0, args.cpu_budget))
+        # a step is one Lanczos iteration of the reference algorithm; K steps
+        # after W warm-up ones, bounded to about a minute of host time
+        warm = max(1, min(args.warmup, 3))
+        cb = cpu_baseline(cfg, budget_s=60.0, max_iters=max(1, args.steps), warmup=warm)
         line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": cb["iterations"],
-                "warmup": 1, "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True, "scaling": "weak",
+                "warmup": warm, "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (generated cage; block values synthetic)",
                 "config": config_record(cfg, precision="fp64"), "impl": "reference",
                 "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if cb["iterations"] != args.steps:
+            line["requested_steps"] = args.steps  # bounded to about a minute of host time
         print(json.dumps(line))
         return
 
