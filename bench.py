@@ -116,7 +116,9 @@ def cpu_baseline(cfg, budget_s=15.0, max_iters=30, warmup=1):
 # clocks during the timed region
 # --------------------------------------------------------------------------
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi samples every 200 ms while the context is open; `summary`
+    keeps the samples whose timestamps fall inside [start(), stop()]."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -124,6 +126,13 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.path = tempfile.mktemp(suffix=".csv")
+        self.t_start = self.t_stop = None
+
+    def start(self):
+        self.t_start = time.time()
+
+    def stop(self):
+        self.t_stop = time.time()
 
     def __enter__(self):
         try:
@@ -142,20 +151,36 @@ class ClockSampler:
             self.proc.wait()
             self.f.close()
 
+    @staticmethod
+    def _when(stamp):
+        import datetime
+        try:
+            return datetime.datetime.strptime(stamp.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
+
     def summary(self):
         try:
-            rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+            rows = [[c.strip() for c in l.split(",")] for l in open(self.path).read().strip().splitlines()
+                    if l.strip()]
         except Exception:
             rows = []
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        inside = [r for r in rows if self.t_start is not None and self._when(r[0]) is not None
+                  and self.t_start <= self._when(r[0]) <= self.t_stop]
+        scope = "timed region" if inside else "whole sampler run (no sample fell inside the timed region)"
+        rows = inside or rows
+        num = lambda x: x.replace(".", "", 1).isdigit()
+        sm = [float(r[2]) for r in rows if len(r) > 2 and num(r[2])]
+        mx = [float(r[3]) for r in rows if len(r) > 3 and num(r[3])]
+        pw = [float(r[4]) for r in rows if len(r) > 4 and num(r[4])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]
-                          and "Not" not in r[5 + i]})
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 6 + i and "Active" in r[6 + i]
+                          and "Not" not in r[6 + i]})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "power_w_median": float(np.median(pw)) if pw else None, "reasons": reasons,
+                "samples": len(rows), "scope": scope}
 
 
 def measured_peak_hbm():
@@ -229,7 +254,7 @@ def stable_levels(bsl, a, b, b2, drop=200, tol=1e-9, unit=None):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--accuracy-iters", type=int, default=10000)
@@ -299,10 +324,13 @@ def main():
     h.lanczos(max(3, args.warmup))
     barrier()
     with ClockSampler(local) as clk:
+        clk.start()
         t0 = time.perf_counter()
         h.lanczos(args.steps)
         barrier()
         wall = time.perf_counter() - t0
+        clk.stop()
+        time.sleep(0.25)  # the sample that covers the end of the region
     ms_event = h.last_ms_per_iter()
     ms_step = max_over_ranks(ms_event, dist)
     value = replica_rate(1000.0, ms_step, world)
