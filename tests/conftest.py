@@ -132,6 +132,10 @@ CASES = ["cage11_n10_l3_all", "seed1_n6_l3_odd", "seed0_n5_l4_even", "iso_n20_l2
 # cases whose fixtures come from the compiled reference but that the CPU oracle
 # restatement does not cover (other water models of the same path)
 REF_ONLY_CASES = ["tip4p_seed1_n6_l3_odd", "point_tip4p_seed1_n6_l3_odd"]
+# the largest potential blocks (36 and 28 functions): the oracle is pinned to
+# the reference on them here, the GPU path to the oracle on the same inputs in
+# test_gpu_block_sizes.py
+BLOCK_CASES = ["seed1_n8_l5_all", "seed1_n8_l6_even"]
 
 
 def case_info(name):

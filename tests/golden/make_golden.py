@@ -68,6 +68,10 @@ CASES = {
                                     ("point", 13, 0.1)),
     # charge at the origin (an odd grid has a point there: 1/0 is clipped)
     "coulomb_n9_l2_all": (COULOMB, 9, 0.3, 2, 4, 4, "All", "NULL", 300, True, ("coulomb", 0.1, -0.1, -20.0)),
+    # the largest blocks of the potential stream: 36 functions (all l <= 5) and
+    # 28 (even l <= 6), the inputs of the GPU block-size tests
+    "seed1_n8_l5_all": (CONTGRID, 8, 0.08, 5, 8, 8, "All", "cage_seed1.xyz", 200, True, None),
+    "seed1_n8_l6_even": (CONTGRID, 8, 0.08, 6, 8, 8, "Even", "cage_seed1.xyz", 200, True, None),
 }
 
 

@@ -10,10 +10,10 @@ import os
 import numpy as np
 import pytest
 
-from conftest import CASES, GOLDEN, OracleModel, case_info, oracle_lancbis, read_boundstates
+from conftest import BLOCK_CASES, CASES, GOLDEN, OracleModel, case_info, oracle_lancbis, read_boundstates
 
 
-@pytest.mark.parametrize("name", CASES + ["cpu_workload"])
+@pytest.mark.parametrize("name", CASES + BLOCK_CASES + ["cpu_workload"])
 def test_oracle_hv_matches_reference(name, in_case_dir):
     d, man, extra = in_case_dir(name)
     m = OracleModel(man["calculator"], "hv_input.txt", extra)
@@ -32,7 +32,7 @@ def test_oracle_hv_matches_reference(name, in_case_dir):
     m.close()
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", CASES + BLOCK_CASES)
 def test_oracle_lanczos_matches_reference(name, in_case_dir):
     d, man, extra = in_case_dir(name)
     m = OracleModel(man["calculator"], "hv_input.txt", extra)
