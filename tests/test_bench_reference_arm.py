@@ -1,7 +1,8 @@
 """The reference arm of bench.py (`--impl reference`): the reference
 algorithm on the host cores for the bench workload, K timed iterations after
 W warm-up ones, one JSON line from rank 0 with the CPU baseline and a
-host-only e2e record; other ranks print nothing."""
+host-only e2e record; other ranks print nothing.  Also the algorithmic bytes
+per launch that the GPU arm's roofline divides by."""
 import json
 import os
 import subprocess
@@ -37,3 +38,21 @@ def test_reference_arm_other_ranks_are_silent():
     p = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}, "--steps", "1", "--warmup", "1")
     assert p.returncode == 0, p.stderr[-2000:]
     assert p.stdout.strip() == ""
+
+
+def test_algorithmic_bytes_of_the_iteration_kernels():
+    """Per-launch algorithmic bytes the roofline divides by, at 54^3 odd
+    l <= 5 (N = 157,464 points, 21 functions, D = 3,306,744): x/y kinetic 16 B,
+    z kinetic 24 B and update 24 B per coefficient; potential stream 231 FP32
+    block entries per point plus 32 B per coefficient; 463 MB per iteration."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_for_bytes", os.path.join(REPO, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    N, nn = 54 ** 3, 21
+    D = N * nn
+    assert D == 3306744
+    sb = bench.stage_bytes(bench._load("bsl_inputs_b", os.path.join(bench.PKG, "inputs.py")).CONFIG_METRIC, D, N,
+                           nn, True)
+    assert [round(x / 1e5) / 10 for x in sb] == [52.9, 79.4, 251.3, 79.4]
+    assert abs(sum(sb) - 462944184) <= 8
