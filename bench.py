@@ -77,7 +77,8 @@ def config_record(cfg, D=None, Df=None, precision="mixed"):
 # --------------------------------------------------------------------------
 def cpu_baseline(cfg, budget_s=15.0, max_iters=30, warmup=1):
     """`warmup` untimed iterations (at least one, which also sizes the sample),
-    then min(max_iters, budget_s / one iteration) timed iterations (at least 1)."""
+    then min(max_iters, budget_s / one iteration) timed iterations (at least 1)
+    on every host thread, and one iteration on a single thread."""
     if not os.path.exists(ORACLE_LIB):
         subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "port"], check=True, capture_output=True)
     L = C.CDLL(ORACLE_LIB)
@@ -95,17 +96,18 @@ def cpu_baseline(cfg, budget_s=15.0, max_iters=30, warmup=1):
                                           0.709648713, cfg["sym"].encode()))
     D = L.orc_basis_size(h)
 
-    def run(n):
+    def run(n, threads=cores):
         a, b, b2 = np.zeros(n), np.zeros(n + 1), np.zeros(n + 1)
-        return L.orc_lanczos(h, n, None, a.ctypes.data_as(P), b.ctypes.data_as(P), b2.ctypes.data_as(P), cores)
+        return L.orc_lanczos(h, n, None, a.ctypes.data_as(P), b.ctypes.data_as(P), b2.ctypes.data_as(P), threads)
 
     t1 = run(1)
     for _ in range(max(0, warmup - 1)):
         run(1)
     n = int(max(1, min(max_iters, budget_s / max(t1, 1e-3))))
     t = run(n)
+    t_one = run(1, threads=1)
     L.orc_destroy(h)
-    return {"value": n / t, "unit": UNIT, "cores": cores, "kind": "port",
+    return {"value": n / t, "unit": UNIT, "cores": cores, "kind": "port", "one_thread_value": 1.0 / t_one,
             "sample": "%d Lanczos iterations of the reference algorithm (oracle restatement: serial sinc-DVR "
                       "kinetic, OpenMP potential blocks, serial recurrence) on the %d-function reference basis "
                       "(%d^3 x (l_max+1)^2 with parity mask), %.1f s" % (n, D, cfg["n"], t),
@@ -286,7 +288,7 @@ def main():
                 "warmup": warm, "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (generated cage; block values synthetic)",
                 "config": config_record(cfg, precision="fp64"), "impl": "reference",
-                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "one_thread_value")},
                 "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         if cb["iterations"] != args.steps:
             line["requested_steps"] = args.steps  # bounded to about a minute of host time
@@ -460,7 +462,7 @@ def main():
         "fp64": {"value": 1000.0 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
                  "stages_ms": [float(x) for x in fp64_stage[:nst]], "speedup_mixed_vs_fp64": fp64_ms / (ms_step)},
         "accuracy": acc,
-        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "one_thread_value")},
         "clocks": clocks, "gpu_launches": nst * args.steps, "prep_seconds": prep_s,
         "wall_ms_per_step": 1000.0 * wall / args.steps,
     }

@@ -30,6 +30,7 @@ def test_reference_arm_times_k_iterations_and_prints_one_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert "reference basis" in cb["sample"]
+    assert 0 < cb["one_thread_value"]
     assert d["e2e"] == {"value": d["value"], "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["grid"] == 54 and d["config"]["l_max"] == 5
 
