@@ -201,7 +201,8 @@ using namespace bsl;
 
 extern "C" int bsl_hf_gradient(bsl_handle* h, int nlev, const double* psi, double* dq_site, double* dr_site,
                                double* dq_alavi) {
-  if (!h || nlev < 1 || !psi || !dq_site || !dr_site || !dq_alavi) return fail(BSL_ERR_INPUT, "bad arguments");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (nlev < 1 || !psi || !dq_site || !dr_site || !dq_alavi) return fail(BSL_ERR_INPUT, "bad arguments");
   if (h->p.potential != BSL_POT_ALAVI_SPCE && h->p.potential != BSL_POT_ALAVI_TIP4P)
     return fail(BSL_ERR_UNSUPPORTED,
                 "derivatives need a continuous-grid Alavi potential (the point-grid lookups are piecewise constant)");

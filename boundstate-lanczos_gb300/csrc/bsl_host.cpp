@@ -689,13 +689,15 @@ int bsl_set_kinetic_engine(bsl_handle* h, int engine) {
 int bsl_kinetic_engine(const bsl_handle* h) { return h ? h->kinetic_engine : -1; }
 
 int bsl_hv_apply_device(bsl_handle* h, const double* d_v, double* d_u, void* stream) {
-  if (!h || !d_v || !d_u) return fail(BSL_ERR_STATE, "null argument");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (!d_v || !d_u) return fail(BSL_ERR_INPUT, "null argument");
   cudaSetDevice(h->p.device);
   return dev_hv(h, d_v, d_u, (cudaStream_t)stream);
 }
 
 int bsl_hv_apply(bsl_handle* h, const double* vec, double* uec) {
-  if (!h || !vec || !uec) return fail(BSL_ERR_STATE, "null argument");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (!vec || !uec) return fail(BSL_ERR_INPUT, "null argument");
   cudaSetDevice(h->p.device);
   DeviceState& d = h->d;
   const size_t Df = (size_t)bsl_basis_size(h);
@@ -724,7 +726,8 @@ long long bsl_vgrid_size(const bsl_handle* h) { return h ? h->t.npts * h->t.na *
 
 // potential grid in the reference order ((i*ny+j)*nz+k)*na*nb + a*nb + b
 int bsl_copy_vgrid(const bsl_handle* h, double* v1, double* v2) {
-  if (!h || !v1 || !v2) return fail(BSL_ERR_STATE, "null argument");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (!v1 || !v2) return fail(BSL_ERR_INPUT, "null argument");
   if (!h->d.v1) return fail(BSL_ERR_STATE, "the potential grid of a large problem is released after HvPrep");
   cudaSetDevice(h->p.device);
   const Tables& t = h->t;
@@ -747,7 +750,8 @@ long long bsl_vblock_size(const bsl_handle* h) { return h ? h->t.npts * h->t.nn 
 // potential blocks as full squares over the packed basis, reference point order
 // [(i*ny+j)*nz+k][s][s']
 int bsl_copy_vblocks(const bsl_handle* h, double* out) {
-  if (!h || !out) return fail(BSL_ERR_STATE, "null argument");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (!out) return fail(BSL_ERR_INPUT, "null argument");
   cudaSetDevice(h->p.device);
   const Tables& t = h->t;
   const size_t N = (size_t)t.npts, nn = t.nn, ntri = nn * (nn + 1) / 2;
@@ -789,7 +793,8 @@ int bsl_tm_eigenvectors(int niter, const double* alpha, const double* beta, cons
 }
 
 int bsl_last_run_ms_per_iter(const bsl_handle* h, double* ms) {
-  if (!h || !ms) return fail(BSL_ERR_STATE, "null argument");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (!ms) return fail(BSL_ERR_INPUT, "null argument");
   *ms = h->last_ms_per_iter;
   return BSL_OK;
 }

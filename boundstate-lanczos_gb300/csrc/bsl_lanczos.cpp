@@ -203,7 +203,8 @@ extern "C" {
 
 int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed, double* alpha, double* beta,
                     double* beta2) {
-  if (!h || niter < 1 || !alpha || !beta || !beta2) return fail(BSL_ERR_INPUT, "bad arguments");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (niter < 1 || !alpha || !beta || !beta2) return fail(BSL_ERR_INPUT, "bad arguments");
   cudaSetDevice(h->p.device);
   DeviceState& d = h->d;
   int rc;
@@ -236,7 +237,8 @@ int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned
                           double** beta, double** beta2) {
   if (!hs || n < 1 || niter < 1 || !alpha || !beta || !beta2) return fail(BSL_ERR_INPUT, "bad arguments");
   for (int b = 0; b < n; ++b) {
-    if (!hs[b] || !alpha[b] || !beta[b] || !beta2[b]) return fail(BSL_ERR_INPUT, "null handle or output in the batch");
+    if (!hs[b]) return fail(BSL_ERR_STATE, "null handle in the batch");
+    if (!alpha[b] || !beta[b] || !beta2[b]) return fail(BSL_ERR_INPUT, "null output in the batch");
     for (int c = 0; c < b; ++c)
       if (hs[c] == hs[b]) return fail(BSL_ERR_INPUT, "a handle appears twice in the batch");
   }
@@ -273,7 +275,8 @@ int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned
 
 int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alpha_j, double* beta_j,
                           double* beta2_j) {
-  if (!h || !vec || !rvec) return fail(BSL_ERR_INPUT, "null argument");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (!vec || !rvec) return fail(BSL_ERR_INPUT, "null argument");
   cudaSetDevice(h->p.device);
   DeviceState& d = h->d;
   int rc;
@@ -321,7 +324,8 @@ int bsl_ritz_vectors(bsl_handle* h, int niter, const double* evtr, int ngood, do
 
 int bsl_ritz_vectors_start(bsl_handle* h, int niter, int start, unsigned long long seed, const double* evtr, int ngood,
                            double* ritz) {
-  if (!h || niter < 1 || ngood < 1 || !evtr || !ritz) return fail(BSL_ERR_INPUT, "bad arguments");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (niter < 1 || ngood < 1 || !evtr || !ritz) return fail(BSL_ERR_INPUT, "bad arguments");
   cudaSetDevice(h->p.device);
   DeviceState& d = h->d;
   const long long D = bsl_packed_size(h), Df = bsl_basis_size(h), L = D + 1;
@@ -389,7 +393,8 @@ int bsl_ritz_vectors_start(bsl_handle* h, int niter, int start, unsigned long lo
 extern "C" {
 
 int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names) {
-  if (!h || iters < 1 || !ms) return fail(BSL_ERR_INPUT, "bad arguments");
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (iters < 1 || !ms) return fail(BSL_ERR_INPUT, "bad arguments");
   cudaSetDevice(h->p.device);
   DeviceState& d = h->d;
   int rc;

@@ -263,3 +263,51 @@ def test_cage_sites_charges(bsl):
         assert np.linalg.norm(xyz[3 * m + 1] - xyz[3 * m]) == pytest.approx(0.1, rel=1e-8)
     qs = np.arange(60, dtype=float)
     assert np.array_equal(bsl.cage_sites(cm, ea, qs)[1], qs)
+
+
+def test_null_handles_and_bad_arguments_return_status(bsl):
+    """Every entry point given a null handle returns BSL_ERR_STATE ("null
+    handle"); null buffers and bad sizes give BSL_ERR_INPUT; size queries give
+    -1.  None of them touches the GPU or exits the process."""
+    L = bsl.lib()
+    state = {
+        "bsl_hv_apply": lambda: L.bsl_hv_apply(None, None, None),
+        "bsl_hv_apply_device": lambda: L.bsl_hv_apply_device(None, None, None, None),
+        "bsl_lanczos_run": lambda: L.bsl_lanczos_run(None, 10, 0, 0, None, None, None),
+        "bsl_lanczos_step_host": lambda: L.bsl_lanczos_step_host(None, None, None, None, None, None),
+        "bsl_ritz_vectors": lambda: L.bsl_ritz_vectors(None, 10, None, 1, None),
+        "bsl_ritz_vectors_start": lambda: L.bsl_ritz_vectors_start(None, 10, 0, 0, None, 1, None),
+        "bsl_set_precision": lambda: L.bsl_set_precision(None, 0),
+        "bsl_set_kinetic_engine": lambda: L.bsl_set_kinetic_engine(None, 0),
+        "bsl_hf_gradient": lambda: L.bsl_hf_gradient(None, 1, None, None, None, None),
+        "bsl_last_run_ms_per_iter": lambda: L.bsl_last_run_ms_per_iter(None, None),
+        "bsl_copy_vgrid": lambda: L.bsl_copy_vgrid(None, None, None),
+        "bsl_copy_vblocks": lambda: L.bsl_copy_vblocks(None, None),
+    }
+    for name, call in state.items():
+        assert call() == bsl.ERR_STATE, name
+        assert b"null handle" in L.bsl_last_error(), name
+    inputs = {
+        "bsl_hv_prep": lambda: L.bsl_hv_prep(None, None),
+        "bsl_lanczos_run_batch": lambda: L.bsl_lanczos_run_batch(None, 0, 10, 0, 0, None, None, None),
+        "bsl_good_eigenvalues": lambda: L.bsl_good_eigenvalues(0, None, None, None, -1.0, 1.0, None, None, None),
+        "bsl_tm_eigenvectors": lambda: L.bsl_tm_eigenvectors(0, None, None, None, None, 0, None),
+    }
+    for name, call in inputs.items():
+        assert call() == bsl.ERR_INPUT, name
+    for name in ("bsl_basis_size", "bsl_packed_size", "bsl_packed_nn", "bsl_vgrid_size", "bsl_vblock_size",
+                 "bsl_kinetic_engine", "bsl_launches_per_iteration"):
+        assert getattr(L, name)(None) == -1, name
+    assert L.bsl_stream(None) is None
+
+
+def test_prep_without_a_gpu_fails_loudly(bsl, in_case_dir):
+    """No CPU fallback: where no GPU is usable, preparing H returns
+    BSL_ERR_CUDA with the CUDA runtime's text."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    in_case_dir("seed1_n6_l3_odd")
+    with pytest.raises(bsl.BslError) as e:
+        bsl.Hamiltonian("hv_input.txt")
+    assert e.value.code == bsl.ERR_CUDA and "CUDA" in str(e.value)
