@@ -13,8 +13,13 @@ library's stream (value), the same metric end to end through the C ABI with
 host buffers (e2e), the FP64 GPU path, the level accuracy of the mixed path
 against the FP64 path at the same iteration count, per-kernel times and the
 roofline of the dominant kernel, and the CPU baseline (oracle restatement of
-the reference's Hv and loop on the host cores, bounded sample).
---impl reference: only the CPU implementation, on the same workload.
+the reference's Hv and loop on the host cores, bounded sample).  Defaults:
+10,000 timed iterations after 20, so that the timed region (about 1 s) spans
+several 200 ms nvidia-smi clock samples; the working set (145 MB of potential
+blocks) is larger than L2, so no flush is needed between iterations.
+--impl reference: only the CPU implementation, on the same workload: K
+iterations after W warm-up ones (at most 3), on every host thread, bounded to
+about a minute; rank 0 only.
 """
 import argparse
 import ctypes as C
