@@ -311,3 +311,29 @@ def test_prep_without_a_gpu_fails_loudly(bsl, in_case_dir):
     with pytest.raises(bsl.BslError) as e:
         bsl.Hamiltonian("hv_input.txt")
     assert e.value.code == bsl.ERR_CUDA and "CUDA" in str(e.value)
+
+
+def test_input_writers_round_trip_through_the_parser(bsl, tmp_path):
+    """inputs.py writes HvInputFiles the C ABI parser reads back field by field
+    (the benchmark's 54^3 workload and a point-grid universe)."""
+    from conftest import load_inputs
+    inp = load_inputs()
+    cage = str(tmp_path / "cage.xyz")
+    inp.write_cage_xyz(cage, inp.dodecahedral_cage(1))
+    cfg = inp.CONFIG_METRIC
+    path = str(tmp_path / "hv_input.txt")
+    inp.write_hv_input(path, inp.hv_fields(cfg["n"], cfg["x_max"], cfg["l_max"], cfg["theta_points"],
+                                           cfg["phi_points"], cage, "metric", cfg["sym"]))
+    p = bsl.parse_hv_input(path)
+    assert (p.nx, p.ny, p.nz, p.l_max) == (54, 54, 54, 5)
+    assert (p.theta_points, p.phi_points) == (cfg["theta_points"], cfg["phi_points"])
+    assert p.x_max == p.y_max == p.z_max == cfg["x_max"]
+    assert (p.pnx, p.px_max) == (54, cfg["x_max"])
+    assert p.symmetry == bsl.SYM[cfg["sym"]] and p.geometry_filename == cage.encode()
+    assert p.total_mass == 2.01588 and p.rotational_constant == 0.709648713 and p.ceiling_potential == 18.0
+    inp.write_hv_input(path, inp.hv_fields(6, 0.08, 3, 8, 7, cage, "point", "Odd", point_grid=(13, 0.1)))
+    p = bsl.parse_hv_input(path)
+    assert (p.nx, p.pnx, p.pny, p.pnz) == (6, 13, 13, 13) and p.px_max == p.pz_max == 0.1
+    # the generated cage: one water at each vertex of the dodecahedron
+    waters = inp.dodecahedral_cage(1)
+    assert len(waters) == 20
