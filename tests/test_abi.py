@@ -337,3 +337,22 @@ def test_input_writers_round_trip_through_the_parser(bsl, tmp_path):
     # the generated cage: one water at each vertex of the dodecahedron
     waters = inp.dodecahedral_cage(1)
     assert len(waters) == 20
+
+
+def test_every_exported_c_symbol_is_declared(bsl):
+    """The library's extern "C" exports are exactly the entry points that
+    include/bsl.h declares (no undeclared C API); the three reference-signature
+    functions of include/bsl_reference_shim.h are exported with C++ linkage."""
+    import shutil
+    import subprocess
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    lib_path = os.path.join(REPO, "boundstate-lanczos_gb300", "libbsl_gb300.so")
+    out = subprocess.run([nm, "-D", "--defined-only", lib_path], capture_output=True, text=True, check=True).stdout
+    text = [ln.split()[-1] for ln in out.splitlines() if len(ln.split()) == 3 and ln.split()[1] == "T"]
+    c_exports = {s for s in text if s.startswith("bsl_")}
+    assert c_exports == set(header_functions())
+    cpp = " ".join(s for s in text if s.startswith("_Z"))
+    for name in ("bsl_reference_storage", "Hv_Prep_linRotCartSph_NoQuad_GB300", "Hv_linRotCartSph_NoQuad_GB300"):
+        assert name in cpp, name
