@@ -132,7 +132,8 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = tempfile.mktemp(suffix=".csv")
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
         self.t_start = self.t_stop = None
 
     def start(self):
