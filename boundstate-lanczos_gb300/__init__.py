@@ -114,6 +114,7 @@ def lib():
     L.bsl_parse_isoharmosc_input.argtypes = [C.c_char_p, C.POINTER(HvParams)]
     L.bsl_parse_coulomb_input.argtypes = [C.c_char_p, C.POINTER(HvParams)]
     L.bsl_calculator_potential.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
+    L.bsl_debug_inject_timeout.argtypes = [C.c_void_p, C.c_int]
     _lib = L
     return L
 
@@ -319,6 +320,12 @@ class Hamiltonian:
 
     def stream(self):
         return lib().bsl_stream(self._h)
+
+    def inject_timeout(self, kernel_mask):
+        """Test hook (bsl_debug_inject_timeout): later runs start with the
+        time-out of the potential stream (bit 0) or of the tensor-core kinetic
+        (bit 1) already recorded; 0 clears it."""
+        _check(lib().bsl_debug_inject_timeout(self._h, kernel_mask))
 
     def lanczos(self, niter, start="uniform", seed=0):
         a = np.zeros(niter)

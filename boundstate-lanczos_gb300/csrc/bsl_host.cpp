@@ -320,6 +320,7 @@ int read_cage(const std::string& path, int model, Cage* c) {
 namespace {
 
 void free_device(DeviceState& d) {
+  release_iteration_graph(d);
   void* ptrs[] = {d.tx, d.ty, d.tz, d.kx_head, d.ky_head, d.kz_head, d.kx_band, d.ky_band, d.kz_band, d.rot,
                   d.v1, d.v2, d.vb64, d.vb32, d.vec, d.rvec, d.ukin, d.v32, d.rot_hi, d.rot_lo, d.partials,
                   d.counter,

@@ -133,6 +133,14 @@ struct DeviceState {
   int red_blocks = 0;
   int* jdev = nullptr;  // iteration counter of graph-replayed Lanczos loops
   int pair_blocks = 0;  // grid of the double-float update: a few resident blocks per SM
+  // captured block of device-counted Lanczos iterations, kept across runs until
+  // something its launches depend on changes (graph_key)
+  cudaGraph_t iter_graph = nullptr;
+  cudaGraphExec_t iter_exec = nullptr;
+  long long graph_key[5] = {0, 0, 0, 0, 0};  // precision, kinetic engine, buffer roles, hist, hist_cap
+  // test hook: status words set again after every reset of the status (host-side
+  // injection of a kernel time-out; bit 2: potential stream, bit 3: kinetic)
+  int inject_status = 0;
 };
 
 }  // namespace bsl
@@ -220,6 +228,9 @@ int launch_update_stream(const float2* V, float2* R, long long L, double* partia
 int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
                       const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
                       double* scalars, double* hist, int j, long long dpk);
+
+// the cached iteration graph (bsl_lanczos.cpp)
+void release_iteration_graph(DeviceState& d);
 
 // ---- Cullum-Willoughby tail (bsl_tail.cpp) --------------------------------
 // unit <= 0: the reference's 2^-52

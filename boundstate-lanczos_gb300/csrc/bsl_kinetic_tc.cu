@@ -168,10 +168,18 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
   __shared__ uint32_t tmem_slot;
   __shared__ int e_stage[kStages][2], e_acc[kStages][2];
   __shared__ float red[2][kProdWarps];
-  __shared__ int prod_go, failed;
+  __shared__ int prod_go, failed, skip;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const Planes<kXY> pg{a.nx, a.ny, a.nz, a.nplanes};
   const int npairs = (a.nplanes + 1) / 2;
+
+  // a kinetic time-out recorded before this launch (an earlier launch of the
+  // run, or the host's injection) makes the CTA leave before it allocates
+  // tensor memory, loads, issues an MMA or waits; one thread reads the flag so
+  // that the whole CTA takes the same branch
+  if (tid == 0) skip = *(volatile int*)(a.status + 3);
+  __syncthreads();
+  if (skip) return;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {

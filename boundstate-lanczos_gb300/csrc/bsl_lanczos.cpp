@@ -28,14 +28,30 @@ int dev_to_pair(double* x, long long n, cudaStream_t s);
 
 namespace {
 
+// The history buffer grows in steps of kHistStep iterations, so runs of
+// similar length reuse it (and the captured iteration graph, whose launches
+// name it).
+constexpr int kHistStep = 1024;
+
 int ensure_hist(bsl_handle* h, int niter) {
   DeviceState& d = h->d;
   if (d.hist && d.hist_cap >= niter + 1) return BSL_OK;
+  release_iteration_graph(d);
   if (d.hist) cudaFree(d.hist);
   d.hist = nullptr;
-  d.hist_cap = niter + 1;
+  d.hist_cap = (niter + 1 + kHistStep - 1) / kHistStep * kHistStep;
   BSL_CUDA(cudaMalloc(&d.hist, 3 * (size_t)d.hist_cap * sizeof(double)));
   BSL_CUDA(cudaMemset(d.hist, 0, 3 * (size_t)d.hist_cap * sizeof(double)));
+  return BSL_OK;
+}
+
+// status words cleared at the start of a run or step, then the injected
+// time-out flags of the test hook (bsl_debug_inject_timeout)
+int reset_status(bsl_handle* h, cudaStream_t s) {
+  DeviceState& d = h->d;
+  BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
+  for (int w = 2; w <= 3; ++w)
+    if (d.inject_status & (1 << w)) BSL_CUDA(cudaMemsetAsync(d.status + w, 0x01, 1, s));
   return BSL_OK;
 }
 
@@ -107,7 +123,7 @@ int init_state(bsl_handle* h, int start, unsigned long long seed) {
     return fail(BSL_ERR_INPUT, "unknown start vector kind");
   }
   if ((rc = dev_fill(d.rvec, D + 1, 0.0, s))) return rc;
-  BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
+  if ((rc = reset_status(h, s))) return rc;
   BSL_CUDA(cudaMemsetAsync(d.scalars, 0, 16 * sizeof(double), s));
   BSL_CUDA(cudaMemcpyAsync(d.scalars, h->init_scalars, 8 * sizeof(double), cudaMemcpyHostToDevice, s));
   // pair-state constants: [8] c = 1 as a double-float pair, [10] the update's exponent 0
@@ -134,45 +150,67 @@ int check_status(bsl_handle* h) {
 
 // niter Lanczos iterations of one problem on stream s.  Where the iteration's
 // kernels can take j from the device counter, kGraphIters iterations are
-// captured once into a CUDA graph (programmatic launches become programmatic
+// captured into a CUDA graph (programmatic launches become programmatic
 // edges) and replayed; an even count leaves the buffer roles as they were.
-// The remainder, and every other configuration, is launched directly.
+// The graph is kept with the handle until the precision, the kinetic engine
+// or the history buffer changes.  The remainder, and every other
+// configuration, is launched directly.
 constexpr int kGraphIters = 8;
 
-struct IterationGraph {
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  ~IterationGraph() {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-  }
-};
-
-// capture kGraphIters device-counted iterations of h on s (nothing runs)
-int capture_iterations(bsl_handle* h, cudaStream_t s, IterationGraph* g) {
+// capture kGraphIters device-counted iterations of h on its stream (nothing
+// runs) unless the cached graph already matches the current configuration
+int ensure_iteration_graph(bsl_handle* h) {
+  DeviceState& d = h->d;
+  const long long key[5] = {h->precision, h->kinetic_engine, h->lanczos_flip, (long long)(uintptr_t)d.hist,
+                            d.hist_cap};
+  if (d.iter_exec && std::memcmp(key, d.graph_key, sizeof(key)) == 0) return BSL_OK;
+  release_iteration_graph(d);
+  cudaStream_t s = d.stream;
   BSL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
   int rc = BSL_OK;
   for (int i = 0; i < kGraphIters && rc == BSL_OK; ++i) rc = dev_lanczos_iteration(h, 0, s);
-  const cudaError_t e = cudaStreamEndCapture(s, &g->graph);
-  if (rc) return rc;
-  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-  BSL_CUDA(cudaGraphInstantiate(&g->exec, g->graph, 0));
+  const cudaError_t e = cudaStreamEndCapture(s, &d.iter_graph);
+  if (rc) {
+    release_iteration_graph(d);
+    return rc;
+  }
+  if (e != cudaSuccess) {
+    release_iteration_graph(d);
+    return cuda_fail(e, "cudaStreamEndCapture");
+  }
+  const cudaError_t ei = cudaGraphInstantiate(&d.iter_exec, d.iter_graph, 0);
+  if (ei != cudaSuccess) {
+    release_iteration_graph(d);
+    return cuda_fail(ei, "cudaGraphInstantiate");
+  }
+  BSL_CUDA(cudaGraphUpload(d.iter_exec, s));
+  std::memcpy(d.graph_key, key, sizeof(key));
+  return BSL_OK;
+}
+
+// Everything a run of niter iterations needs before its first launch: the
+// iteration graphs of the problems that replay one (captured and uploaded
+// here, outside the timed region).
+int prepare_iterations(bsl_handle** hs, int n, int niter) {
+  int rc;
+  for (int b = 0; b < n; ++b) {
+    bsl_handle* h = hs[b];
+    cudaSetDevice(h->p.device);
+    if (device_counted_iterations(h) && niter >= kGraphIters && (rc = ensure_iteration_graph(h))) return rc;
+  }
   return BSL_OK;
 }
 
 // the iterations of several problems, iteration blocks interleaved across
-// their streams; graphs[b] must outlive the launches (synchronise first)
-int run_iterations(bsl_handle** hs, int n, int niter, std::vector<IterationGraph>* graphs) {
-  graphs->resize(n);
+// their streams (prepare_iterations first)
+int run_iterations(bsl_handle** hs, int n, int niter) {
   std::vector<char> counted(n, 0);
   int rc;
   for (int b = 0; b < n; ++b) {
     bsl_handle* h = hs[b];
     cudaSetDevice(h->p.device);
     counted[b] = device_counted_iterations(h) ? 1 : 0;
-    if (!counted[b]) continue;
-    if ((rc = dev_set_iteration(h, 1, h->d.stream))) return rc;
-    if (niter >= kGraphIters && (rc = capture_iterations(h, h->d.stream, &(*graphs)[b]))) return rc;
+    if (counted[b] && (rc = dev_set_iteration(h, 1, h->d.stream))) return rc;
   }
   const int nblocks = niter / kGraphIters;
   for (int k = 0; k < nblocks; ++k)
@@ -180,7 +218,7 @@ int run_iterations(bsl_handle** hs, int n, int niter, std::vector<IterationGraph
       bsl_handle* h = hs[b];
       cudaSetDevice(h->p.device);
       if (counted[b]) {
-        BSL_CUDA(cudaGraphLaunch((*graphs)[b].exec, h->d.stream));
+        BSL_CUDA(cudaGraphLaunch(h->d.iter_exec, h->d.stream));
       } else {
         for (int i = 0; i < kGraphIters; ++i)
           if ((rc = dev_lanczos_iteration(h, k * kGraphIters + i + 1, h->d.stream))) return rc;
@@ -195,6 +233,15 @@ int run_iterations(bsl_handle** hs, int n, int niter, std::vector<IterationGraph
 }
 
 }  // namespace
+
+void release_iteration_graph(DeviceState& d) {
+  if (d.iter_exec) cudaGraphExecDestroy(d.iter_exec);
+  if (d.iter_graph) cudaGraphDestroy(d.iter_graph);
+  d.iter_exec = nullptr;
+  d.iter_graph = nullptr;
+  std::memset(d.graph_key, 0, sizeof(d.graph_key));
+}
+
 }  // namespace bsl
 
 using namespace bsl;
@@ -210,10 +257,10 @@ int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed
   int rc;
   if ((rc = ensure_hist(h, niter)) || (rc = init_state(h, start, seed))) return rc;
   cudaStream_t s = d.stream;
-  std::vector<IterationGraph> graphs;
+  if ((rc = prepare_iterations(&h, 1, niter))) return rc;
   BSL_CUDA(cudaEventRecord(d.ev0, s));
-  if ((rc = run_iterations(&h, 1, niter, &graphs))) {
-    cudaStreamSynchronize(s);  // nothing of a replayed graph may still run when it is destroyed
+  if ((rc = run_iterations(&h, 1, niter))) {
+    cudaStreamSynchronize(s);
     return rc;
   }
   BSL_CUDA(cudaEventRecord(d.ev1, s));
@@ -249,8 +296,8 @@ int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned
   }
   // blocks of iterations interleaved across the problems' streams, so the
   // kernels of different problems overlap
-  std::vector<IterationGraph> graphs;
-  if ((rc = run_iterations(hs, n, niter, &graphs))) {
+  if ((rc = prepare_iterations(hs, n, niter))) return rc;
+  if ((rc = run_iterations(hs, n, niter))) {
     for (int b = 0; b < n; ++b) cudaStreamSynchronize(hs[b]->d.stream);
     return rc;
   }
@@ -293,7 +340,7 @@ int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alph
   BSL_CUDA(cudaStreamWaitEvent(d.copy_stream, d.vec_in, 0));
   BSL_CUDA(cudaMemcpyAsync(d.ref_out, rvec, Df * sizeof(double), cudaMemcpyHostToDevice, d.copy_stream));
   BSL_CUDA(cudaEventRecord(d.copy_done, d.copy_stream));
-  BSL_CUDA(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), s));
+  if ((rc = reset_status(h, s))) return rc;
   // r += S H v: H on the packed block, nothing elsewhere (the device Lanczos
   // vectors serve as packed scratch)
   h->state_pairs = -1;
@@ -430,5 +477,12 @@ int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names) {
 }
 
 int bsl_launches_per_iteration(const bsl_handle* h) { return h ? 4 : -1; }
+
+int bsl_debug_inject_timeout(bsl_handle* h, int kernel_mask) {
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (kernel_mask & ~3) return fail(BSL_ERR_INPUT, "kernel_mask has bits other than 0 and 1");
+  h->d.inject_status = ((kernel_mask & 1) ? (1 << 2) : 0) | ((kernel_mask & 2) ? (1 << 3) : 0);
+  return BSL_OK;
+}
 
 }  // extern "C"

@@ -4,7 +4,9 @@
 // cudaMalloc, so callers that cannot allocate device memory can still run the
 // recurrence on buffers they own.  See bsl_lanczos_orthonormalize_static in
 // include/bsl.h for the contract.
+#include <cstdint>
 #include <mutex>
+#include <string>
 
 #include "bsl_device.cuh"
 
@@ -54,23 +56,28 @@ __global__ void k_na_update(const double* __restrict__ v, double* __restrict__ r
     const double b = sqrt(total);
     scratch[kNaScalars + 1] = b;
     scratch[kNaScalars + 2] = total;
-    scratch[kNaScalars + 3] = 1. / b;
+    // a zero or non-finite beta (or alpha) is a breakdown: 1/beta = 0 tells the
+    // next kernel to leave both vectors as they are
+    const bool ok = b > 0.0 && isfinite(b) && isfinite(alpha);
+    scratch[kNaScalars + 3] = ok ? 1. / b : 0.0;
   }
 }
 
 // v <- r / beta, r <- -beta v (the reference's scale then swap), and the
-// scalars to the caller's buffer
+// scalars to the caller's buffer; nothing is moved after a breakdown
 __global__ void k_na_swap(double* __restrict__ v, double* __restrict__ r, long long n, const double* scratch,
                           double* abb) {
   const double b = scratch[kNaScalars + 1], inv = scratch[kNaScalars + 3];
-  const long long base = (long long)blockIdx.x * kNaTile + threadIdx.x;
+  if (inv != 0.0) {
+    const long long base = (long long)blockIdx.x * kNaTile + threadIdx.x;
 #pragma unroll
-  for (int u = 0; u < kNaPerThread; ++u) {
-    const long long i = base + (long long)u * kThreads;
-    if (i < n) {
-      const double vi = v[i];
-      v[i] = inv * r[i];
-      r[i] = (-b) * vi;
+    for (int u = 0; u < kNaPerThread; ++u) {
+      const long long i = base + (long long)u * kThreads;
+      if (i < n) {
+        const double vi = v[i];
+        v[i] = inv * r[i];
+        r[i] = (-b) * vi;
+      }
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -80,23 +87,73 @@ __global__ void k_na_swap(double* __restrict__ v, double* __restrict__ r, long l
   }
 }
 
-// Device address of the scratch array, looked up once per device with that
-// device current (host code must not pass the symbol itself to a kernel).
-std::mutex g_na_mutex;
-double* g_na_ptr[64] = {nullptr};
+// Device address of the scratch array in the calling thread's current CUDA
+// context.  A symbol's device address belongs to a context, not to a device
+// ordinal: after cudaDeviceReset, or under another context on the same
+// device, an address looked up earlier is stale.  The cache is therefore keyed
+// by the context's unique id (cuCtxGetId, reached through the runtime's driver
+// entry points so that the library does not link the driver library), and a
+// context seen for the first time pays one cudaGetSymbolAddress.  Where the
+// id cannot be read, the address is looked up on every call.  Host code must
+// not pass the symbol itself to a kernel: in host code it names a host-side
+// stand-in, not device memory.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
 
-int scratch_for_current_device(double** out) {
-  int dev = 0;
-  BSL_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(BSL_ERR_UNSUPPORTED, "device ordinal above 63");
-  std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (!g_na_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static Lanczos scratch)");
-    g_na_ptr[dev] = static_cast<double*>(p);
+struct CtxEntry {
+  unsigned long long id;
+  double* ptr;
+};
+
+std::mutex g_na_mutex;
+constexpr int kNaCacheSlots = 16;
+CtxEntry g_na_cache[kNaCacheSlots] = {};
+int g_na_next = 0;
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+bool g_ctx_resolved = false;
+
+// the current context's id, or 0 when it cannot be read
+unsigned long long current_context_id() {
+  if (!g_ctx_resolved) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+      g_ctx_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    cudaGetLastError();
+    g_ctx_resolved = true;
   }
-  *out = g_na_ptr[dev];
+  if (!g_ctx_current || !g_ctx_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_current(&ctx) != 0 || !ctx || g_ctx_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+int scratch_for_current_context(double** out) {
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  unsigned long long id = current_context_id();
+  if (id != 0)
+    for (const CtxEntry& e : g_na_cache)
+      if (e.id == id) {
+        *out = e.ptr;
+        return BSL_OK;
+      }
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static Lanczos scratch)");
+  if (id == 0) id = current_context_id();  // the lookup made the device's primary context current
+  if (id != 0) {
+    g_na_cache[g_na_next] = CtxEntry{id, static_cast<double*>(p)};
+    g_na_next = (g_na_next + 1) % kNaCacheSlots;
+  }
+  *out = static_cast<double*>(p);
   return BSL_OK;
 }
 
@@ -111,8 +168,15 @@ extern "C" int bsl_lanczos_orthonormalize_static(double* d_vec, double* d_rvec, 
   if (n < 1 || n > kNaMaxN)
     return fail(BSL_ERR_INPUT, "vector length " + std::to_string(n) +
                                    " is outside the static scratch capacity of 1.." + std::to_string(kNaMaxN));
+  // the kernels read v and write r through restrict-qualified pointers
+  const uintptr_t v0 = reinterpret_cast<uintptr_t>(d_vec), r0 = reinterpret_cast<uintptr_t>(d_rvec);
+  const uintptr_t bytes = (uintptr_t)n * sizeof(double);
+  if (v0 < r0 + bytes && r0 < v0 + bytes) return fail(BSL_ERR_INPUT, "d_vec and d_rvec overlap");
+  const uintptr_t a0 = reinterpret_cast<uintptr_t>(d_abb);
+  if ((a0 < v0 + bytes && v0 < a0 + 3 * sizeof(double)) || (a0 < r0 + bytes && r0 < a0 + 3 * sizeof(double)))
+    return fail(BSL_ERR_INPUT, "d_abb overlaps d_vec or d_rvec");
   double* scratch = nullptr;
-  int rc = scratch_for_current_device(&scratch);
+  int rc = scratch_for_current_context(&scratch);
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   // the counter must start at zero; a previous call that failed part-way may

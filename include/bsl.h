@@ -208,26 +208,33 @@ int bsl_lanczos_step_host(bsl_handle* h, double* vec, double* rvec, double* alph
 
 /* The rest of one Lanczos iteration after r += H v, on device buffers the
    caller owns, without allocating any device memory.  No counterpart in the
-   reference: it exists for callers that cannot call cudaMalloc at the point
-   where they run the recurrence -- code that is recording a CUDA graph (stream
-   capture forbids allocation), applications that reserve all GPU memory up
-   front in their own pool, and real-time loops that cannot afford the device
-   synchronisation an allocation implies.
+   reference.  It is for callers that cannot call cudaMalloc at the point where
+   they run the recurrence: applications that reserve all GPU memory up front
+   in their own pool (an allocation would fail or break their accounting), and
+   loops that cannot afford the device-wide synchronisation an allocation or a
+   free may imply.
 
-   d_vec holds v_j, d_rvec holds r_j + H v_j (n doubles each, any layout, FP64).
-   On return, as in the reference loop body (lanczosEigenValuesVectors.cpp:202-238):
+   d_vec holds v_j, d_rvec holds r_j + H v_j (n doubles each, any layout, FP64;
+   the two ranges and d_abb must not overlap: BSL_ERR_INPUT).  On return, as in
+   the reference loop body (lanczosEigenValuesVectors.cpp:202-238):
    alpha = v.r, r -= alpha v, beta = |r|, d_vec = r / beta, d_rvec = -beta v_j,
    and d_abb[0..2] = {alpha, beta, beta^2} (device memory).  Work is queued on
-   `stream` (cudaStream_t as void*, NULL = legacy default stream) and runs on the
-   calling thread's current device.
+   `stream` (cudaStream_t as void*, NULL = legacy default stream) and runs in
+   the calling thread's current CUDA context; nothing is synchronised, so a
+   breakdown cannot be returned as a status: when beta is zero or not finite
+   (or alpha not finite) d_abb holds those values and d_vec, d_rvec are left as
+   v_j and r_j - alpha v_j, unscaled.  Check d_abb[1] > 0 and finite before the
+   next iteration.
 
    The reduction scratch is one static device array of 4112 doubles (32.9 KB)
    that every GPU loading the library holds until the process exits; it limits
-   n to 1..8,388,608 (BSL_ERR_INPUT beyond).  All calls on a device share it:
-   calls that overlap on the GPU (different streams without ordering) race and
-   give wrong results.  The first call on each device looks up the array's
-   device address (cudaGetSymbolAddress); make that first call before any
-   stream capture.  No allocation, no cudaFree, no synchronisation. */
+   n to 1..8,388,608 (BSL_ERR_INPUT beyond).  All calls in a context share it
+   and it keeps the last call's contents: calls that overlap on the GPU
+   (different streams without ordering) race and give wrong results.  The
+   array's device address is looked up once per CUDA context
+   (cudaGetSymbolAddress) by the first call made in that context, and again
+   after a cudaDeviceReset (a new context); make that first call before any
+   stream capture begins. */
 int bsl_lanczos_orthonormalize_static(double* d_vec, double* d_rvec, long long n, double* d_abb, void* stream);
 
 /* Cullum-Willoughby good eigenvalues in (emin, emax] with inverse-iteration
@@ -315,6 +322,18 @@ int bsl_selftest_tensor_core(double* max_abs_err);
    update + beta, normalise + swap} into ms[0..4]; names[i] (optional) receives
    the kernel name of stage i (static strings). */
 int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names);
+
+/* Test hook for the failure paths, with no counterpart in the reference.
+   Every bounded wait of the potential-block stream and of the tensor-core
+   kinetic records a time-out in a device status word, and the next
+   bsl_lanczos_run / bsl_lanczos_step_host returns BSL_ERR_CUDA with the
+   stage named.  kernel_mask bit 0 (potential stream) and bit 1 (tensor-core
+   kinetic) make every later run or step start with that stage's time-out
+   already recorded: the kernels then skip their copies, MMAs and waits, the
+   results are meaningless and the call returns the error.  0 clears the
+   injection; the handle is usable again at once.  Nothing on the GPU is made
+   to wait or fault. */
+int bsl_debug_inject_timeout(bsl_handle* h, int kernel_mask);
 
 /* Kernel launches per Lanczos iteration of the current configuration. */
 int bsl_launches_per_iteration(const bsl_handle* h);

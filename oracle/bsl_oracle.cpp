@@ -38,6 +38,7 @@
 // Reference paths here are relative to Hv-calculators/linRotor/cartSphBasis/
 // unless they start with headLoop/.
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -101,6 +102,8 @@ struct Cage {
   std::vector<double> pos;   // [atom][3] nm
   std::vector<double> q;     // charge
   std::vector<int> is_o;     // LJ site
+  std::vector<double> cm, ea;  // per molecule: centre of mass (Angstrom), ZY'Z'' Euler angles (rad)
+  double q_h2_h = kQ_H2_H, q_h2_cm = kQ_H2_CM;  // Alavi H2 charges (each H, centre of mass)
 };
 
 // getSPCEatoms: rotate the SPC/E body frame with the ZY'Z'' Euler angles and
@@ -118,6 +121,7 @@ bool read_cage(const std::string& path, Cage* c) {
     double cm[3], ea[3];
     f >> name >> cm[0] >> ea[0] >> cm[1] >> ea[1] >> cm[2] >> ea[2];
     if (!f) { g_err = "truncated geometry file"; return false; }
+    for (int r = 0; r < 3; ++r) { c->cm.push_back(cm[r]); c->ea.push_back(ea[r]); }
     double cp = cos(ea[0]), sp = sin(ea[0]), ct = cos(ea[1]), st = sin(ea[1]), cx = cos(ea[2]), sx = sin(ea[2]);
     double R[3][3] = {{(cp * ct * cx) - (sp * sx), (-1 * cp * ct * sx) - (sp * cx), cp * st},
                       {(sp * ct * cx) + (cp * sx), (-1 * sp * ct * sx) + (cp * cx), sp * st},
@@ -327,7 +331,7 @@ void build_potential_alavi(Model& M, int nthreads) {
   for (long p = 0; p < (long)np; ++p) {
     int i = p / ((size_t)nj * nk), j = (p / nk) % nj, k = p % nk;
     double g[3] = {M.xgrid[i], M.ygrid[j], M.zgrid[k]};
-    double c = coulomb_sum(g, kQ_H2_CM, M.cage);
+    double c = coulomb_sum(g, M.cage.q_h2_cm, M.cage);
     c += lj_sum(g, M.cage);
     cmpot[p] = c;
   }
@@ -341,8 +345,8 @@ void build_potential_alavi(Model& M, int nthreads) {
           const double* h = (half ? h2.data() : h1.data()) + ((size_t)a * nb + b) * 3;
           double p1[3] = {g[0] + h[0], g[1] + h[1], g[2] + h[2]};
           double p2[3] = {g[0] - h[0], g[1] - h[1], g[2] - h[2]};
-          double v = coulomb_sum(p1, kQ_H2_H, M.cage);
-          v += coulomb_sum(p2, kQ_H2_H, M.cage);
+          double v = coulomb_sum(p1, M.cage.q_h2_h, M.cage);
+          v += coulomb_sum(p2, M.cage.q_h2_h, M.cage);
           v += cmpot[p];
           if (v >= ceil_v) v = ceil_v;
           (half ? M.V2 : M.V1)[((size_t)p * na + a) * nb + b] = v;
@@ -544,6 +548,173 @@ void hv(const Model& M, const double* v, double* uec, int nthreads) {
           uec[o] += h;
         }
       }
+}
+
+// ---------------------------------------------------------------------------
+// Hellmann-Feynman derivatives, FP64 (no counterpart in the reference: the
+// derivative of the restated potential above).  The continuous-grid blocks are
+// the quadrature of build_vblocks,
+//   <s|V|s'>(p) = sum_{a,b} w_a w_b [Y_s Y_s' V1 + Y2_s Y2_s' V2](p, a, b),
+// so for any fixed psi (a unit-independent Rayleigh quotient, H(theta) in a
+// basis that does not depend on theta)
+//   d<psi|H|psi>/dtheta / <psi|psi> = sum_p sum_{a,b,half} w_a w_b f_half(p,a,b)^2 dV_half/dtheta / <psi|psi>,
+//   f_half(p, a, b) = sum_s psi_s(p) L_s(a) S^half_{m_s}(b),
+// over the functions of the symmetry block, and zero where the ceiling clips V
+// (V >= ceiling stored as the ceiling).  V (Alavi_ContGrid_H2_Routines.cpp:6-147,
+// SPCE_AH2_EngRoutines.cpp:110-178, energyRoutines.cpp:5-54) is
+//   K [q_cm sum_w q_w / |g - r_w| + q_h sum_w q_w (1/|g + h - r_w| + 1/|g - h - r_w|)]
+//   + sum_O (A / |g - r_O|^12 - B / |g - r_O|^6),
+// h = d u(theta_a, phi_b) (y component negated on the 2 pi - phi half).
+// Outputs per level n: dq[n][w], dr[n][w][3] (per nm), da[n][{q_h, q_cm}].
+void hf_gradient(const Model& M, int nlev, const double* psi, double* dq, double* dr, double* da, int nthreads) {
+  const HvInput& in = M.in;
+  const int ni = in.nx, nj = in.ny, nk = in.nz, na = in.theta_points, nb = in.phi_points, nn = M.nn;
+  const int lmax = in.l_max;
+  const size_t N = (size_t)ni * nj * nk, D = N * nn;
+  const Cage& c = M.cage;
+  const int nat = (int)c.q.size();
+  std::vector<int> block;
+  for (int s = 0; s < nn; ++s)
+    if (M.sym[s] != 0.0) block.push_back(s);
+  const int nbk = (int)block.size();
+  // Y[(a nb + b) 2 + half][k] for the block's functions k, with sqrt(w_a w_b)
+  std::vector<double> Y((size_t)na * nb * 2 * nbk), hoff((size_t)na * nb * 3);
+  for (int a = 0; a < na; ++a)
+    for (int b = 0; b < nb; ++b) {
+      const double w = sqrt(M.gl_w[a] * M.gc_w[b]);
+      for (int half = 0; half < 2; ++half)
+        for (int k = 0; k < nbk; ++k) {
+          const int sfun = block[k];
+          const std::vector<double>& S = half ? M.S2 : M.S1;
+          Y[(((size_t)a * nb + b) * 2 + half) * nbk + k] =
+              w * M.L[(size_t)sfun * na + a] * S[(size_t)(M.qm[sfun] + lmax) * nb + b];
+        }
+      hoff[((size_t)a * nb + b) * 3] = kH2_H1_Z * sin(M.theta[a]) * M.gc_x[b];
+      hoff[((size_t)a * nb + b) * 3 + 1] = kH2_H1_Z * sin(M.theta[a]) * sin(M.phi[b]);
+      hoff[((size_t)a * nb + b) * 3 + 2] = kH2_H1_Z * M.gl_x[a];
+    }
+  std::vector<double> norm(nlev, 0.0);
+  for (int n = 0; n < nlev; ++n)
+    for (int k = 0; k < nbk; ++k)
+      for (size_t p = 0; p < N; ++p) {
+        const double x = psi[(size_t)n * D + (size_t)block[k] * N + p];
+        norm[n] += x * x;
+      }
+  const size_t nsite = (size_t)nlev * nat * 4, nacc = nsite + (size_t)nlev * 2;
+  std::vector<double> total(nacc, 0.0);
+  const double ceil_v = in.ceiling;
+#pragma omp parallel num_threads(nthreads)
+  {
+    std::vector<double> acc(nacc, 0.0), ps(nbk * (size_t)nlev), rho(nlev), sv(nat * 4);
+#pragma omp for schedule(dynamic, 16)
+    for (long p = 0; p < (long)N; ++p) {
+      // vector index p = ((k nj) + j) ni + i; potential index (i nj + j) nk + k
+      const int i = (int)(p % ni), j = (int)((p / ni) % nj), kz = (int)(p / ((long)ni * nj));
+      const size_t pb = ((size_t)i * nj + j) * nk + kz;
+      const double g[3] = {M.xgrid[i], M.ygrid[j], M.zgrid[kz]};
+      for (int n = 0; n < nlev; ++n)
+        for (int k = 0; k < nbk; ++k) ps[(size_t)n * nbk + k] = psi[(size_t)n * D + (size_t)block[k] * N + p];
+      // centre-of-mass terms do not depend on the node: per site 1/rc, dc/rc^3 and the LJ force
+      std::vector<double> cm_inv(nat), cm_f(nat * 3);
+      for (int w = 0; w < nat; ++w) {
+        const double d0 = g[0] - c.pos[3 * w], d1 = g[1] - c.pos[3 * w + 1], d2 = g[2] - c.pos[3 * w + 2];
+        const double r2 = d0 * d0 + d1 * d1 + d2 * d2, r = sqrt(r2), inv = 1.0 / r, inv3 = inv * inv * inv;
+        cm_inv[w] = inv;
+        double f = kK * c.q[w] * c.q_h2_cm * inv3;
+        if (c.is_o[w]) f += 12.0 * kA_LJ / pow(r, 14) - 6.0 * kB_LJ / pow(r, 8);
+        cm_f[3 * w] = f * d0;
+        cm_f[3 * w + 1] = f * d1;
+        cm_f[3 * w + 2] = f * d2;
+      }
+      for (int a = 0; a < na; ++a)
+        for (int b = 0; b < nb; ++b)
+          for (int half = 0; half < 2; ++half) {
+            const double v = (half ? M.V2 : M.V1)[(pb * na + a) * nb + b];
+            if (!(v < ceil_v)) continue;
+            const double* y = &Y[(((size_t)a * nb + b) * 2 + half) * nbk];
+            double rsum = 0.0;
+            for (int n = 0; n < nlev; ++n) {
+              double f = 0.0;
+              for (int k = 0; k < nbk; ++k) f += ps[(size_t)n * nbk + k] * y[k];
+              rho[n] = f * f;
+              rsum += rho[n];
+            }
+            if (rsum == 0.0) continue;
+            const double* h = &hoff[((size_t)a * nb + b) * 3];
+            const double hx = h[0], hy = half ? -h[1] : h[1], hz = h[2];
+            double sh = 0.0, sc = 0.0;  // d V / d q_h, d V / d q_cm
+            for (int w = 0; w < nat; ++w) {
+              const double bx = g[0] - c.pos[3 * w], by = g[1] - c.pos[3 * w + 1], bz = g[2] - c.pos[3 * w + 2];
+              const double px = bx + hx, py = by + hy, pz = bz + hz, mx = bx - hx, my = by - hy, mz = bz - hz;
+              const double ip = 1.0 / sqrt(px * px + py * py + pz * pz), im = 1.0 / sqrt(mx * mx + my * my + mz * mz);
+              const double ip3 = ip * ip * ip, im3 = im * im * im;
+              const double kq = kK * c.q[w] * c.q_h2_h;
+              sv[4 * w] = kK * (c.q_h2_h * (ip + im) + c.q_h2_cm * cm_inv[w]);
+              sv[4 * w + 1] = kq * (px * ip3 + mx * im3) + cm_f[3 * w];
+              sv[4 * w + 2] = kq * (py * ip3 + my * im3) + cm_f[3 * w + 1];
+              sv[4 * w + 3] = kq * (pz * ip3 + mz * im3) + cm_f[3 * w + 2];
+              sh += kK * c.q[w] * (ip + im);
+              sc += kK * c.q[w] * cm_inv[w];
+            }
+            for (int n = 0; n < nlev; ++n) {
+              const double rn = rho[n];
+              double* o = &acc[(size_t)n * nat * 4];
+              for (int e = 0; e < nat * 4; ++e) o[e] += rn * sv[e];
+              acc[nsite + 2 * n] += rn * sh;
+              acc[nsite + 2 * n + 1] += rn * sc;
+            }
+          }
+    }
+#pragma omp critical
+    for (size_t e = 0; e < nacc; ++e) total[e] += acc[e];
+  }
+  for (int n = 0; n < nlev; ++n) {
+    for (int w = 0; w < nat; ++w) {
+      const double* t = &total[((size_t)n * nat + w) * 4];
+      dq[(size_t)n * nat + w] = t[0] / norm[n];
+      for (int k = 0; k < 3; ++k) dr[((size_t)n * nat + w) * 3 + k] = t[1 + k] / norm[n];
+    }
+    da[2 * n] = total[nsite + 2 * n] / norm[n];
+    da[2 * n + 1] = total[nsite + 2 * n + 1] / norm[n];
+  }
+}
+
+// SPC/E site s of a molecule with Euler angles e (getSPCEatoms' rotation,
+// SPCE_AH2_EngRoutines.cpp:5-108, rotmat.cpp:6-32), relative to the centre of
+// mass, for a real or complex angle type.
+template <typename T>
+void spce_site_rel(const T e[3], int s, T out[3]) {
+  using std::cos;
+  using std::sin;
+  const T cp = cos(e[0]), sp = sin(e[0]), ct = cos(e[1]), st = sin(e[1]), cx = cos(e[2]), sx = sin(e[2]);
+  const T R[3][3] = {{(cp * ct * cx) - (sp * sx), (-1.0 * cp * ct * sx) - (sp * cx), cp * st},
+                     {(sp * ct * cx) + (cp * sx), (-1.0 * sp * ct * sx) + (cp * cx), sp * st},
+                     {-1.0 * st * cx, st * sx, ct}};
+  const double* local[3] = {kO_SPCE, kH1_SPCE, kH2_SPCE};
+  for (int r = 0; r < 3; ++r) out[r] = R[r][0] * local[s][0] + R[r][1] * local[s][1] + R[r][2] * local[s][2];
+}
+
+// chain rule from site positions to (centre of mass in Angstrom, Euler angles):
+// d site / d cm_k = 0.1 e_k; d site / d e_k by complex-step differentiation of
+// the rotation (exact to rounding: Im f(x + i h) / h with h = 1e-30)
+void rigid_body_chain(const Cage& c, int nlev, const double* dr, double* dcm, double* dea) {
+  const int nmol = (int)c.cm.size() / 3, nat = (int)c.q.size();
+  for (int n = 0; n < nlev; ++n)
+    for (int m = 0; m < nmol; ++m) {
+      for (int k = 0; k < 3; ++k) {
+        double gc = 0.0;
+        for (int s = 0; s < 3; ++s) gc += kNmPerAng * dr[((size_t)n * nat + 3 * m + s) * 3 + k];
+        dcm[((size_t)n * nmol + m) * 3 + k] = gc;
+        double ge = 0.0;
+        for (int s = 0; s < 3; ++s) {
+          std::complex<double> e[3] = {c.ea[3 * m], c.ea[3 * m + 1], c.ea[3 * m + 2]}, x[3];
+          e[k] += std::complex<double>(0.0, 1e-30);
+          spce_site_rel(e, s, x);
+          for (int r = 0; r < 3; ++r) ge += dr[((size_t)n * nat + 3 * m + s) * 3 + r] * (x[r].imag() / 1e-30);
+        }
+        dea[((size_t)n * nmol + m) * 3 + k] = ge;
+      }
+    }
 }
 
 }  // namespace
@@ -757,6 +928,43 @@ void orc_ritz(void* h, int niter, const double* evtr, int ngood, double* ritz, i
     for (long i = 0; i < D; ++i) v[i] = (-b) * v[i];
     for (long i = 0; i < D; ++i) { u[i] = v[i]; v[i] = r[i]; r[i] = u[i]; }
   }
+}
+
+
+// Hellmann-Feynman derivatives of the levels of eigenvectors psi[n][D]
+// (reference layout, any normalisation) for the continuous-grid Alavi SPC/E
+// model: dq_site[n][w], dr_site[n][w][3] (per nm), dq_alavi[n][{H, centre}].
+int orc_hf_gradient(void* h, int nlev, const double* psi, double* dq_site, double* dr_site, double* dq_alavi,
+                    int nthreads) {
+  Model* M = static_cast<Model*>(h);
+  if (M->potential_kind != 0) { g_err = "derivatives need the continuous-grid Alavi SPC/E potential"; return 1; }
+  hf_gradient(*M, nlev, psi, dq_site, dr_site, dq_alavi, nthreads);
+  return 0;
+}
+
+// dr_site[n][w][3] -> d_cm[n][m][3] (per Angstrom), d_euler[n][m][3] (per rad)
+int orc_rigid_body_gradient(void* h, int nlev, const double* dr_site, double* d_cm, double* d_euler) {
+  Model* M = static_cast<Model*>(h);
+  if (M->cage.cm.empty()) { g_err = "no cage"; return 1; }
+  rigid_body_chain(M->cage, nlev, dr_site, d_cm, d_euler);
+  return 0;
+}
+
+// Replace the site charges (q_site[w], NULL: unchanged) and the Alavi H2
+// charges (q_alavi[2], NULL: unchanged), then rebuild the potential and the
+// blocks (continuous-grid Alavi SPC/E only).
+int orc_set_charges(void* h, const double* q_site, const double* q_alavi, int nthreads) {
+  Model* M = static_cast<Model*>(h);
+  if (M->potential_kind != 0) { g_err = "charges need the continuous-grid Alavi SPC/E potential"; return 1; }
+  if (q_site)
+    for (size_t w = 0; w < M->cage.q.size(); ++w) M->cage.q[w] = q_site[w];
+  if (q_alavi) {
+    M->cage.q_h2_h = q_alavi[0];
+    M->cage.q_h2_cm = q_alavi[1];
+  }
+  build_potential_alavi(*M, nthreads);
+  build_vblocks(*M, nthreads);
+  return 0;
 }
 
 }  // extern "C"

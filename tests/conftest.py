@@ -38,6 +38,14 @@ def load_inputs():
 _oracle = None
 
 
+def reference_tree():
+    """The reference tree the oracle recipe reads (BSL_REFERENCE_DIR or the
+    recipe's default); it need not exist."""
+    r = subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "print-ref"], capture_output=True,
+                       text=True)
+    return r.stdout.strip()
+
+
 def load_oracle():
     """The CPU restatement (test infrastructure), built on first use."""
     global _oracle
@@ -66,6 +74,9 @@ def load_oracle():
     L.orc_lancbis.argtypes = [C.c_int, P, P, P, C.c_double, C.c_double, P, P]
     L.orc_trivec.argtypes = [C.c_int, P, P, P, P, C.c_int, P]
     L.orc_ritz.argtypes = [C.c_void_p, C.c_int, P, C.c_int, P, C.c_int]
+    L.orc_hf_gradient.argtypes = [C.c_void_p, C.c_int, P, P, P, P, C.c_int]
+    L.orc_rigid_body_gradient.argtypes = [C.c_void_p, C.c_int, P, P, P]
+    L.orc_set_charges.argtypes = [C.c_void_p, P, P, C.c_int]
     _oracle = L
     return L
 
@@ -108,6 +119,32 @@ class OracleModel:
         out = np.zeros(self.L.orc_vblock_size(self.h))
         self.L.orc_vblocks(self.h, ptr(out))
         return out
+
+    def hf_gradient(self, psi, natoms):
+        """FP64 Hellmann-Feynman derivatives of psi[nlev, D] (continuous-grid
+        Alavi SPC/E): dq[nlev, natoms], dr[nlev, natoms, 3], da[nlev, 2]."""
+        ps = np.ascontiguousarray(psi, dtype=np.float64).reshape(-1, self.D)
+        nlev = ps.shape[0]
+        dq, dr, da = np.zeros((nlev, natoms)), np.zeros((nlev, natoms, 3)), np.zeros((nlev, 2))
+        rc = self.L.orc_hf_gradient(self.h, nlev, ptr(ps), ptr(dq), ptr(dr), ptr(da), self.threads)
+        if rc:
+            raise RuntimeError(self.L.orc_last_error().decode())
+        return dq, dr, da
+
+    def rigid_body_gradient(self, dr):
+        dr = np.ascontiguousarray(dr, dtype=np.float64)
+        nlev, nmol = dr.shape[0], dr.shape[1] // 3
+        dcm, dea = np.zeros((nlev, nmol, 3)), np.zeros((nlev, nmol, 3))
+        if self.L.orc_rigid_body_gradient(self.h, nlev, ptr(dr), ptr(dcm), ptr(dea)):
+            raise RuntimeError(self.L.orc_last_error().decode())
+        return dcm, dea
+
+    def set_charges(self, q_site=None, q_alavi=None):
+        qs = None if q_site is None else np.ascontiguousarray(q_site, dtype=np.float64)
+        qa = None if q_alavi is None else np.ascontiguousarray(q_alavi, dtype=np.float64)
+        if self.L.orc_set_charges(self.h, None if qs is None else ptr(qs), None if qa is None else ptr(qa),
+                                  self.threads):
+            raise RuntimeError(self.L.orc_last_error().decode())
 
     def close(self):
         self.L.orc_destroy(self.h)

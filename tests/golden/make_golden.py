@@ -1,6 +1,7 @@
 """Generate the committed golden fixtures from the reference itself.
 
-Run in a container that has the reference tree (default /root/reference) and
+Run in a container that has the reference tree (first argument, else the
+BSL_REFERENCE_DIR environment variable) and
 has built it with `make -C oracle ref`.  Every fixture below comes from the
 UNMODIFIED reference (oracle/_ref/libref_hv.so for single Hv applications,
 oracle/_ref/ref_lanczos for whole Lanczos runs) or is copied verbatim from the
@@ -28,7 +29,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ["BSL_REFERENCE_DIR"]
 ONLY = set(sys.argv[2:])
 REF_LIB = os.path.join(REPO, "oracle", "_ref", "libref_hv.so")
 REF_BIN = os.path.join(REPO, "oracle", "_ref", "ref_lanczos")
@@ -105,7 +106,68 @@ def run_ref_lanczos(case_dir, calc, extra):
     return alpha, beta
 
 
+# Fixture pinning the FP64 Hellmann-Feynman oracle: for a fixed vector psi the
+# Rayleigh quotient E = psi.H psi / psi.psi of the reference's own H has
+# dE/dtheta = psi.(dH/dtheta) psi / psi.psi exactly, so central differences of
+# E through the compiled reference, with the cage's centres and Euler angles
+# moved in the .xyz it reads, check the oracle's site derivatives and its
+# chain rule to the rigid-body coordinates.
+HF_FD_CASE = "hf_fd_seed1_n5_l3_odd"
+HF_FD_STEP = 1e-5
+HF_FD_PARAMS = [("cm", 0, 0), ("cm", 3, 1), ("cm", 11, 2), ("cm", 17, 0), ("euler", 2, 0), ("euler", 5, 1),
+                ("euler", 9, 2), ("euler", 14, 0), ("euler", 19, 1)]
+
+
+def make_hf_fd():
+    d = os.path.join(HERE, HF_FD_CASE)
+    os.makedirs(d, exist_ok=True)
+    waters = inputs.dodecahedral_cage(1)
+    inputs.write_cage_xyz(os.path.join(d, "cage.xyz"), waters)
+    inputs.write_hv_input(os.path.join(d, "hv_input.txt"),
+                          inputs.hv_fields(5, 0.08, 3, 6, 5, "cage.xyz", HF_FD_CASE, "Odd"))
+    lib = C.CDLL(REF_LIB)
+    lib.ref_hv_setup.restype = C.c_long
+    P = C.POINTER(C.c_double)
+    cwd = os.getcwd()
+    os.chdir(d)
+    try:
+        D = lib.ref_hv_setup(CONTGRID.encode(), b"hv_input.txt", None)
+        lmax, N = 3, 125
+        ls = [l for m in range(-lmax, lmax + 1) for l in range(abs(m), lmax + 1)]
+        psi = np.random.default_rng(7).standard_normal(D)
+        for n, l in enumerate(ls):
+            if l % 2 == 0:
+                psi[n * N:(n + 1) * N] = 0.0  # outside the odd block
+
+        def energy(ws):
+            inputs.write_cage_xyz("cage_fd.xyz", ws)
+            inputs.write_hv_input("hv_fd.txt", inputs.hv_fields(5, 0.08, 3, 6, 5, "cage_fd.xyz", HF_FD_CASE, "Odd"))
+            lib.ref_hv_setup(CONTGRID.encode(), b"hv_fd.txt", None)
+            u = np.zeros(D)
+            lib.ref_hv(psi.ctypes.data_as(P), u.ctypes.data_as(P))
+            return float(psi @ u / (psi @ psi))
+
+        rows = []
+        for kind, m, k in HF_FD_PARAMS:
+            e = []
+            for sgn in (1.0, -1.0):
+                ws = [(nm, list(cm), list(ea)) for nm, cm, ea in waters]
+                (ws[m][1] if kind == "cm" else ws[m][2])[k] += sgn * HF_FD_STEP
+                e.append(energy(ws))
+            rows.append([e[0], e[1]])
+        for f in ("cage_fd.xyz", "hv_fd.txt"):
+            os.remove(f)
+    finally:
+        os.chdir(cwd)
+    np.savez(os.path.join(d, "ref_rayleigh_fd.npz"), psi=psi, e_pm=np.array(rows), step=HF_FD_STEP,
+             params=np.array([[0 if kind == "cm" else 1, m, k] for kind, m, k in HF_FD_PARAMS]))
+    print(HF_FD_CASE, np.array(rows)[:, 0] - np.array(rows)[:, 1])
+
+
 def main():
+    if ONLY == {HF_FD_CASE}:
+        make_hf_fd()
+        return
     shutil.copy(os.path.join(REF, "Compilation", "sII_smallCage11_CM_EA_ZYZ.xyz"), os.path.join(HERE, "cage11.xyz"))
     for seed in (0, 1):
         inputs.write_cage_xyz(os.path.join(HERE, "cage_seed%d.xyz" % seed), inputs.dodecahedral_cage(seed))
@@ -171,6 +233,7 @@ def main():
         stored[run] = {"niter": niter, "levels": vals}
     with open(os.path.join(HERE, "stored_2013_runs.json"), "w") as f:
         json.dump(stored, f, indent=0)
+    make_hf_fd()
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
 

@@ -1,0 +1,71 @@
+"""The grids the benchmarks run on, checked against the oracle: edges of 27, 33
+and 41 points (the batched small problems) and 54 points (the metric
+problem), odd l <= 5 (21 functions, the benchmark's block), over +-0.4 A
+with the generated SPC/E cage (seed 1).  The angular grid is cut to 8 theta x
+16 phi so that the CPU oracle finishes in seconds at these sizes; the kernels
+under test (tensor-core kinetic with its exact slicing at the largest class
+sums, the potential-block stream at the full tile count, the FP64 path) do not
+depend on the angular grid, which only enters the potential blocks.
+
+Tolerances: FP64 H v against the oracle <= 1e-10 relative (max abs / max abs);
+the first 10 FP64 alpha/beta against the oracle's <= 1e-10 of max |alpha|, the
+first 20 <= 1e-9;
+mixed H v of both kinetic engines against FP64 <= 2e-6; the first 20 mixed
+alpha/beta against FP64 <= 1e-6 of max |alpha|.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import OracleModel, load_inputs, load_package
+
+pytestmark = pytest.mark.gpu
+CALC = "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE"
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+
+@pytest.mark.parametrize("n", [27, 33, 41, 54])
+def test_metric_and_batch_grids_match_oracle(tmp_path, n):
+    bsl = load_package()
+    inp = load_inputs()
+    cage = os.path.join(str(tmp_path), "cage.xyz")
+    inp.write_cage_xyz(cage, inp.dodecahedral_cage(1))
+    hv = os.path.join(str(tmp_path), "hv_input.txt")
+    inp.write_hv_input(hv, inp.hv_fields(n, 0.08, 5, 8, 8, cage, "grid_edge_%d" % n, "Odd"))
+    h = bsl.Hamiltonian(hv, CALC, precision="fp64")
+    m = OracleModel(CALC, hv, threads=os.cpu_count() or 8)
+    try:
+        assert h.basis_size == m.D and h.nn == 21
+        v = np.random.default_rng(n).standard_normal(h.basis_size)
+        u = np.zeros(h.basis_size)
+        h.hv(v, u)
+        err64 = rel(u, m.hv(v))
+        assert err64 <= 1e-10, err64
+        a, b, _ = h.lanczos(20)
+        ao, bo, _ = m.lanczos(20)
+        scale = np.max(np.abs(ao))
+        ea, eb = np.abs(a - ao) / scale, np.abs(b[1:] - bo[1:]) / scale
+        # the first 10 to 1e-10; later ones to 1e-9: the reference's serial FP64
+        # sums over 5.7 M terms (restated in the oracle) carry ~1e-13 relative
+        # rounding per dot product, which the recurrence amplifies (1.1e-10 at
+        # iteration 20 of the 54^3 case, measured)
+        assert ea[:10].max() <= 1e-10 and eb[:10].max() <= 1e-10, (ea, eb)
+        assert ea.max() <= 1e-9 and eb.max() <= 1e-9, (ea, eb)
+        h.set_precision("mixed")
+        assert h.kinetic_engine() == "tensor"
+        for engine in ("tensor", "simt"):
+            h.set_kinetic_engine(engine)
+            um = np.zeros(h.basis_size)
+            h.hv(v, um)
+            errm = rel(um, u)
+            assert errm <= 2e-6, (engine, errm)
+            am, bm, _ = h.lanczos(20)
+            assert np.max(np.abs(am - a)) <= 1e-6 * scale, (engine, np.max(np.abs(am - a)) / scale)
+            assert np.max(np.abs(bm - b)) <= 1e-6 * scale, (engine, np.max(np.abs(bm - b)) / scale)
+    finally:
+        m.close()
+        h.close()

@@ -11,11 +11,11 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import PKG_DIR, REPO, case_info
+from conftest import PKG_DIR, REPO, case_info, reference_tree
 
 INCLUDE = os.path.join(REPO, "include")
 DRIVER = os.path.join(REPO, "tests", "shim_driver.cpp")
-REF_TREE = "/root/reference"
+REF_TREE = reference_tree()
 
 
 def build_driver(out_dir):
