@@ -11,7 +11,9 @@ of the 54^3 x (l<=5) basis of H2 in a 20-water SPC/E dodecahedral cage (seed
 Default arm: the mixed-precision GPU path timed with CUDA events on the
 library's stream (value), the same metric end to end through the C ABI with
 host buffers (e2e), the FP64 GPU path, the level accuracy of the mixed path
-against the FP64 path at the same iteration count, per-kernel times and the
+against the FP64 path at the same iteration count, the precision variants of
+the same problem (iter/s and level errors of reduced kinetic slices, BF16
+potential blocks and the CUDA-core kinetic), per-kernel times and the
 roofline of the dominant kernel, and the CPU baseline (oracle restatement of
 the reference's Hv and loop on the host cores, bounded sample).  Defaults:
 10,000 timed iterations after 20, so that the timed region (about 1 s) spans
@@ -274,6 +276,111 @@ def stable_levels(bsl, a, b, b2, drop=200, tol=1e-9, unit=None):
     return np.array([e for e in ev if len(ev2) and np.min(np.abs(ev2 - e)) <= tol])
 
 
+# Precision variants of the metric problem: (name, potential blocks, kinetic
+# engine, tensor-core slices); the Lanczos recurrence is double-float in all.
+SWEEP = [("V fp32, kinetic tensor-core 4 slices (exact, default)", "fp32", "tensor", 4),
+         ("V fp32, kinetic tensor-core 3 slices", "fp32", "tensor", 3),
+         ("V fp32, kinetic tensor-core 2 slices (split 3-term)", "fp32", "tensor", 2),
+         ("V fp32, kinetic tensor-core 1 slice (plain 9-bit)", "fp32", "tensor", 1),
+         ("V fp32, kinetic CUDA-core fp32 head+tail", "fp32", "simt", 4),
+         ("V bf16 per-point scale, kinetic tensor-core 4 slices", "bf16", "tensor", 4),
+         ("V bf16 per-point scale, kinetic tensor-core 2 slices", "bf16", "tensor", 2),
+         ("V bf16 per-point scale, kinetic tensor-core 1 slice", "bf16", "tensor", 1)]
+
+
+def level_errors(bsl, ref_levels, a, b, b2):
+    """Per reference level, the distance (cm^-1) to the nearest level of a run,
+    through the tail with the mixed unit roundoff and with the FP64 one."""
+    evm, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF)
+    evr, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3)
+    dev = np.array([np.min(np.abs(evm - e)) for e in ref_levels]) * KJ_TO_CM if len(evm) else np.full(
+        len(ref_levels), np.inf)
+    dev_r = np.array([np.min(np.abs(evr - e)) for e in ref_levels]) * KJ_TO_CM if len(evr) else np.full(
+        len(ref_levels), np.inf)
+    return dev, dev_r
+
+
+def precision_sweep(bsl, h, ref_levels, n_it, fp64_rate, timed=2000):
+    """One record per precision variant: iter/s (CUDA events, `timed`
+    iterations after a warm-up run) and the level errors after n_it iterations
+    against the FP64 levels at the same iteration count."""
+    recs = [{"variant": "V fp64, kinetic fp64 (the FP64 path)", "iter_s": fp64_rate, "max_abs_dE_cm-1": 0.0,
+             "levels_within_1e-3_cm-1": len(ref_levels)}]
+    h.set_precision("mixed")
+    for name, vfmt, engine, slices in SWEEP:
+        h.set_potential_format(vfmt)
+        h.set_kinetic_engine(engine)
+        h.set_kinetic_slices(slices)
+        h.lanczos(64)
+        h.lanczos(timed)
+        rate = 1000.0 / h.last_ms_per_iter()
+        a, b, b2 = h.lanczos(n_it, start="normal", seed=0)
+        dev, dev_r = level_errors(bsl, ref_levels, a, b, b2)
+        recs.append({"variant": name, "iter_s": rate, "max_abs_dE_cm-1": float(dev.max()),
+                     "max_abs_dE_cm-1_lowest20": float(dev[:20].max()),
+                     "levels_within_1e-3_cm-1": int(np.sum(dev <= 1e-3)),
+                     "max_abs_dE_cm-1_fp64_tail_tolerance": float(dev_r.max()),
+                     "levels_within_1e-3_cm-1_fp64_tail_tolerance": int(np.sum(dev_r <= 1e-3))})
+    h.set_potential_format("fp32")
+    h.set_kinetic_slices(4)
+    h.set_kinetic_engine("tensor")
+    return recs
+
+
+def batched_workload(bsl, tmp, device, fp64_check=True, nlev=10):
+    """The batched workload (inputs.batch_problems: 32 uneven problems, 3000
+    iterations each): total Lanczos iterations per second of all the problems
+    through bsl_lanczos_run_batch (device time of the whole batch, the
+    iteration graphs cached by a warm-up batch), against the same problems run
+    one after another; and, per problem, the lowest `nlev` converged FP64
+    levels against the batched mixed run's levels at the same iteration
+    count."""
+    inputs = _load("bsl_inputs", os.path.join(PKG, "inputs.py"))
+    probs = inputs.batch_problems()
+    hs = []
+    t0 = time.perf_counter()
+    for k, pr in enumerate(probs):
+        cage = os.path.join(tmp, "batch_cage%d.xyz" % pr["cage_seed"])
+        if not os.path.exists(cage):
+            inputs.write_cage_xyz(cage, inputs.dodecahedral_cage(pr["cage_seed"], pr["radius"]))
+        hv = os.path.join(tmp, "batch_hv%d.txt" % k)
+        inputs.write_hv_input(hv, inputs.hv_fields(pr["n"], pr["x_max"], pr["l_max"], pr["theta_points"],
+                                                   pr["phi_points"], cage, "batch%d" % k, pr["sym"]))
+        hs.append(bsl.Hamiltonian(hv, "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE", precision="mixed",
+                                  device=device))
+    prep_s = time.perf_counter() - t0
+    niter = probs[0]["niter"]
+    total = len(probs) * niter
+    bsl.lanczos_batch(hs, 64, start="normal", seed=0)  # warm-up: graphs captured and cached
+    runs = bsl.lanczos_batch(hs, niter, start="normal", seed=0)
+    batch_ms = hs[0].last_ms_per_iter() * niter
+    sep_ms = 0.0
+    for h in hs:
+        h.lanczos(niter, start="normal", seed=0)
+        sep_ms += h.last_ms_per_iter() * niter
+    rec = {"problems": len(probs), "iterations_each": niter,
+           "coefficients_total": int(sum(h.packed_size for h in hs)),
+           "edges": [pr["n"] for pr in probs], "blocks": [h.nn for h in hs],
+           "batched_iter_s": total / (batch_ms * 1e-3), "batched_ms": batch_ms,
+           "sequential_iter_s": total / (sep_ms * 1e-3), "sequential_ms": sep_ms,
+           "path": "bsl_lanczos_run_batch (one stream per problem, 8-iteration graphs interleaved)",
+           "prep_seconds": prep_s}
+    if fp64_check:
+        worst, within, cnt = 0.0, 0, 0
+        for h, (am, bm, bm2) in zip(hs, runs):
+            h.set_precision("fp64")
+            a, b, b2 = h.lanczos(niter, start="normal", seed=0)
+            ref = np.sort(stable_levels(bsl, a, b, b2))[:nlev]
+            dev, _ = level_errors(bsl, ref, am, bm, bm2)
+            worst = max(worst, float(dev.max()))
+            within += int(np.sum(dev <= 1e-3))
+            cnt += len(ref)
+        rec.update({"levels_compared": cnt, "levels_within_1e-3_cm-1": within, "max_abs_dE_cm-1": worst})
+    for h in hs:
+        h.close()
+    return rec
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -289,6 +396,11 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--dump-lanczos", default="",
                     help="save the alpha/beta histories of the accuracy runs to this .npz file")
+    ap.add_argument("--batched", action="store_true",
+                    help="only the batched workload (32 uneven problems, 3000 iterations each)")
+    ap.add_argument("--sweep", type=int, default=1,
+                    help="1: add the precision variants of the metric problem (iter/s and level errors against "
+                         "the FP64 levels at --accuracy-iters iterations) to the line; 0: skip")
     ap.add_argument("--kinetic", default="auto", choices=["auto", "simt", "tensor"],
                     help="kinetic engine of the mixed path (auto: tensor cores where the grid allows)")
     args = ap.parse_args()
@@ -323,6 +435,11 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     bsl = _load("boundstate_lanczos_gb300", os.path.join(PKG, "__init__.py"))
+    if args.batched:
+        rec = batched_workload(bsl, tmp, local)
+        print(json.dumps(dict(record="batched workload: 16 cages x {ortho odd l<=5, para even l<=4}, edges "
+                                     "from {27, 33, 41}, 24 theta x 48 phi, 3000 iterations each", **rec)))
+        return
     t0 = time.perf_counter()
     h = bsl.Hamiltonian(hv_path, "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE", precision=args.precision, device=local)
     prep_s = time.perf_counter() - t0
@@ -414,6 +531,7 @@ def main():
 
     # ---- level accuracy: mixed vs FP64 at the same iteration count ----
     acc = {}
+    sweep = None
     if args.accuracy_iters > 0 and rank == 0:
         n_it = args.accuracy_iters
         a64, b64, b264 = h.lanczos(n_it, start="normal", seed=0)
@@ -424,10 +542,7 @@ def main():
         ref_levels = np.sort(stable_levels(bsl, a64, b64, b264))[:cfg["levels"]]
         # the mixed levels through the tail with the mixed path's unit roundoff
         # (bsl_good_eigenvalues_unit); the reference tail's FP64 tolerance is reported beside
-        evm, _ = bsl.good_eigenvalues(am, bm, bm2, -1.0e3, 1.0e3, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF)
-        evr, _ = bsl.good_eigenvalues(am, bm, bm2, -1.0e3, 1.0e3)
-        dev = np.array([np.min(np.abs(evm - e)) for e in ref_levels]) * KJ_TO_CM if len(evm) else np.array([])
-        dev_r = np.array([np.min(np.abs(evr - e)) for e in ref_levels]) * KJ_TO_CM if len(evr) else np.array([])
+        dev, dev_r = level_errors(bsl, ref_levels, am, bm, bm2)
         worst = int(np.argmax(dev)) if len(dev) else -1
         acc = {"iterations": n_it, "levels_compared": int(len(ref_levels)),
                "max_abs_dE_cm-1": float(dev.max()) if len(dev) else None,
@@ -449,6 +564,8 @@ def main():
         h.set_precision("mixed")
         h.hv(vr, um)
         acc["hv_rel_err_mixed_vs_fp64"] = float(np.max(np.abs(um - u64)) / np.max(np.abs(u64)))
+        if args.sweep:
+            sweep = precision_sweep(bsl, h, ref_levels, n_it, 1000.0 / fp64_ms)
     h.close()
 
     cb = cpu_baseline(cfg, budget_s=args.cpu_budget) if rank == 0 else None
@@ -483,6 +600,7 @@ def main():
         "fp64": {"value": 1000.0 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
                  "stages_ms": [float(x) for x in fp64_stage[:nst]], "speedup_mixed_vs_fp64": fp64_ms / (ms_step)},
         "accuracy": acc,
+        "precision_sweep": sweep,
         "cpu_baseline": dict({k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "one_thread_value")},
                              reference_vs_port_hv_ms=REFERENCE_VS_PORT_HV_MS,
                              reference_vs_port_note="compiled reference vs this port, H v ms, 8 threads, x86 "

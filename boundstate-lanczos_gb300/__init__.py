@@ -25,6 +25,7 @@ POT_POINT_ALAVI_SPCE, POT_POINT_ALAVI_TIP4P, POT_COULOMB = 3, 4, 5
 PREC = {"fp64": 0, "mixed": 1}
 START = {"uniform": 0, "normal": 1}
 KINETIC = {"simt": 0, "tensor": 1}
+VFORMAT = {"fp32": 0, "bf16": 1}
 MIXED_UNIT_ROUNDOFF = 4.0e-15  # BSL_MIXED_UNIT_ROUNDOFF
 CALCULATORS = {
     "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE": POT_ALAVI_SPCE,
@@ -115,6 +116,8 @@ def lib():
     L.bsl_parse_coulomb_input.argtypes = [C.c_char_p, C.POINTER(HvParams)]
     L.bsl_calculator_potential.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
     L.bsl_debug_inject_timeout.argtypes = [C.c_void_p, C.c_int]
+    L.bsl_set_kinetic_slices.argtypes = [C.c_void_p, C.c_int]
+    L.bsl_set_potential_format.argtypes = [C.c_void_p, C.c_int]
     _lib = L
     return L
 
@@ -303,6 +306,14 @@ class Hamiltonian:
     def set_kinetic_engine(self, engine):
         """Kinetic engine of the mixed precision: "simt" or "tensor"."""
         _check(lib().bsl_set_kinetic_engine(self._h, KINETIC[engine]))
+
+    def set_kinetic_slices(self, slices):
+        """9-bit slices kept by the tensor-core kinetic (1..4; 4 = exact)."""
+        _check(lib().bsl_set_kinetic_slices(self._h, slices))
+
+    def set_potential_format(self, fmt):
+        """Potential blocks of the mixed path: "fp32" or "bf16" (per-point scale)."""
+        _check(lib().bsl_set_potential_format(self._h, VFORMAT[fmt]))
 
     def kinetic_engine(self):
         e = lib().bsl_kinetic_engine(self._h)

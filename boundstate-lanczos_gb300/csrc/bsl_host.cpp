@@ -331,6 +331,8 @@ void free_device(DeviceState& d) {
   if (d.kxy_slices) cudaFree(d.kxy_slices);
   if (d.kz_slices) cudaFree(d.kz_slices);
   if (d.jdev) cudaFree(d.jdev);
+  if (d.vb16) cudaFree(d.vb16);
+  if (d.vscale) cudaFree(d.vscale);
   if (d.copy_done) cudaEventDestroy(d.copy_done);
   if (d.vec_in) cudaEventDestroy(d.vec_in);
   if (d.copy_stream) cudaStreamDestroy(d.copy_stream);
@@ -688,6 +690,27 @@ int bsl_set_kinetic_engine(bsl_handle* h, int engine) {
 }
 
 int bsl_kinetic_engine(const bsl_handle* h) { return h ? h->kinetic_engine : -1; }
+
+int bsl_set_kinetic_slices(bsl_handle* h, int slices) {
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (slices < 1 || slices > 4) return fail(BSL_ERR_INPUT, "kinetic slices must be 1..4");
+  h->kin_slices = slices;
+  return BSL_OK;
+}
+
+int bsl_set_potential_format(bsl_handle* h, int format) {
+  if (!h) return fail(BSL_ERR_STATE, "null handle");
+  if (format != BSL_VFMT_FP32 && format != BSL_VFMT_BF16) return fail(BSL_ERR_INPUT, "unknown block format");
+  if (format == BSL_VFMT_BF16 && h->t.nn != 15 && h->t.nn != 21)
+    return fail(BSL_ERR_UNSUPPORTED, "BF16 potential blocks are built for blocks of 15 and 21 functions");
+  cudaSetDevice(h->p.device);
+  if (format == BSL_VFMT_BF16 && !h->d.vb16) {
+    int rc = dev_vblocks_bf16(h);
+    if (rc) return rc;
+  }
+  h->vformat = format;
+  return BSL_OK;
+}
 
 int bsl_hv_apply_device(bsl_handle* h, const double* d_v, double* d_u, void* stream) {
   if (!h) return fail(BSL_ERR_STATE, "null handle");

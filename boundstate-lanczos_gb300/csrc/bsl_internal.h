@@ -137,7 +137,11 @@ struct DeviceState {
   // something its launches depend on changes (graph_key)
   cudaGraph_t iter_graph = nullptr;
   cudaGraphExec_t iter_exec = nullptr;
-  long long graph_key[5] = {0, 0, 0, 0, 0};  // precision, kinetic engine, buffer roles, hist, hist_cap
+  // precision, kinetic engine, buffer roles, hist, hist_cap, kinetic slices, block format
+  long long graph_key[7] = {0, 0, 0, 0, 0, 0, 0};
+  // BF16 potential blocks (tile-major like vb32) and their per-point FP32 scales
+  uint16_t* vb16 = nullptr;
+  float* vscale = nullptr;
   // test hook: status words set again after every reset of the status (host-side
   // injection of a kernel time-out; bit 2: potential stream, bit 3: kinetic)
   int inject_status = 0;
@@ -152,6 +156,8 @@ struct bsl_handle {
   bsl::DeviceState d;
   int precision = BSL_PREC_FP64;
   int kinetic_engine = BSL_KIN_SIMT;  // engine of the mixed-precision kinetic (BSL_KIN_*)
+  int kin_slices = 4;                 // 9-bit slices of the tensor-core kinetic (4: exact)
+  int vformat = BSL_VFMT_FP32;        // storage of the mixed path's potential blocks (BSL_VFMT_*)
   double last_ms_per_iter = 0.0;
   int lanczos_flip = 0;           // 0: vec holds v_j and rvec r_j; 1: roles swapped
   int state_pairs = -1;           // Lanczos buffers: 0 FP64, 1 double-float pairs (mixed), -1 not set up
@@ -209,6 +215,9 @@ struct StreamArgs {
   const float* rot_hi;  // rotor energies, head and tail
   const float* rot_lo;
   double* out;          // mode 0: u = H v; mode 1: the Lanczos r buffer (r += c H v)
+  const uint16_t* vb16; // BSL_VFMT_BF16: tile-major BF16 blocks, V = vscale[p] * block
+  const float* vscale;
+  int vformat;
   long long npts, dpk;
   long long tiles_per_cta;  // set by the launcher
   int mode, j;          // j > 0: the iteration; j == 0: read it from *jdev
@@ -228,6 +237,9 @@ int launch_update_stream(const float2* V, float2* R, long long L, double* partia
 int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
                       const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
                       double* scalars, double* hist, int j, long long dpk);
+
+// BF16 copy of the potential blocks with per-point scales (bsl_vstream.cu)
+int dev_vblocks_bf16(bsl_handle* h);
 
 // the cached iteration graph (bsl_lanczos.cpp)
 void release_iteration_graph(DeviceState& d);

@@ -629,6 +629,9 @@ int launch_vapply(bsl_handle* h, const double* v, double* out, int mode, int j, 
     a.hist = d.hist;
     a.counter = d.counter;
     a.status = d.status;
+    a.vb16 = d.vb16;
+    a.vscale = d.vscale;
+    a.vformat = h->vformat;
     return launch_vapply_f32(a, t.nn, s);
   }
   return launch_vapply_f64(d.vb64, g, s, t.nn, v, d.ukin, d.rot, out, N, mode, d.partials, d.counter, d.scalars,

@@ -79,6 +79,7 @@ struct KinTC {
   float2* out;
   int nx, ny, nz, nplanes;
   int* status;
+  int nslices;              // slices of v and of T kept (1-4; 4 = exact), classes k + l < nslices
 };
 
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
@@ -123,13 +124,23 @@ __device__ __forceinline__ void slice4(float yh, float yl, float (&a)[kVS]) {
 // error, the tail collects that error and the two smaller classes (its own
 // rounding is ~2^-33 of the head); the pair is left unnormalised (|lo| may
 // slightly exceed half an ulp of hi), which the double-float additions accept.
-__device__ __forceinline__ void load_pairs8(uint32_t taddr, float scale, float2 (&out)[8]) {
+// With fewer than four slices the classes at and above `nslices` were never
+// written and are taken as zero.
+__device__ __forceinline__ void load_pairs8(uint32_t taddr, float scale, int nslices, float2 (&out)[8]) {
   float c0[8], c1[8], c2[8], c3[8];
   tc::tmem_ld8_nowait(taddr, c0);
   tc::tmem_ld8_nowait(taddr + 64u, c1);
   tc::tmem_ld8_nowait(taddr + 128u, c2);
   tc::tmem_ld8_nowait(taddr + 192u, c3);
   tc::tmem_wait_ld();
+  if (nslices < 4) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      c3[u] = 0.f;
+      c2[u] = nslices > 2 ? c2[u] : 0.f;
+      c1[u] = nslices > 1 ? c1[u] : 0.f;
+    }
+  }
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
     float h, e;
@@ -269,7 +280,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
       for (int c0 = c_begin; c0 < c_end; c0 += 8) {
         float2 v[8];
         if (kXY) {
-          load_pairs8(tbase + (uint32_t)c0, scale, v);
+          load_pairs8(tbase + (uint32_t)c0, scale, a.nslices, v);
           if (valid)
 #pragma unroll
             for (int u = 0; u < 8; ++u)
@@ -279,7 +290,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
 #pragma unroll
           for (int u = 0; u < 8; ++u) cur[u] = nxt[u];
           if (c0 + 8 < c_end) load8(ob, valid, c0 + 8, nxt);  // the next chunk, in flight meanwhile
-          load_pairs8(tbase + (uint32_t)c0, scale, v);
+          load_pairs8(tbase + (uint32_t)c0, scale, a.nslices, v);
           if (valid)
 #pragma unroll
             for (int u = 0; u < 8; ++u)
@@ -370,7 +381,8 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
             for (int u = 0; u < 4; ++u) slice4(__fmul_rn(x[t][u].x, sc), __fmul_rn(x[t][u].y, sc), sl[u]);
 #pragma unroll
             for (int k = 0; k < kVS; ++k)
-              *reinterpret_cast<uint2*>(vp + k * kTile + soff[t]) =
+              if (k < a.nslices)
+                *reinterpret_cast<uint2*>(vp + k * kTile + soff[t]) =
                   make_uint2(pack_h2(sl[0][k], sl[1][k]), pack_h2(sl[2][k], sl[3][k]));
           }
         }
@@ -400,16 +412,18 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
       const uint32_t d0 = tmem + (uint32_t)st * kAccCols;
       const uint32_t vb = tc::smem_u32(V + st * kStage);
       // Class c accumulates in columns [64 c, 64 c + 64).  An MMA whose B stacks
-      // the slices l = 0 .. 3 - k of one operand along N (rows 64 l ..) and
-      // whose D starts at column 64 k puts product (k, l) into class k + l.
+      // the slices l = 0 .. ns - 1 - k of one operand along N (rows 64 l ..) and
+      // whose D starts at column 64 k puts product (k, l) into class k + l
+      // (ns = 4 slices, the exact default: classes 0..3, 10 products).
       // Contraction over the rows of each plane (y for x/y, z for z): A = v
       // slice k (M = (p, x), MN-major, the planes kPlaneSlices apart), B = T
-      // slices 0 .. 3 - k; 16 rows (2 KiB) per K step.  The first MMA (k = 0,
-      // N = 256) sets all four classes.
+      // slices 0 .. ns - 1 - k; 16 rows (2 KiB) per K step.  The first MMA
+      // (k = 0, N = 64 ns) sets every class.
       const uint32_t t0 = tb + (kXY ? kTile : 0u);
+      const int ns = a.nslices;
 #pragma unroll 1
-      for (int k = 0; k < kVS; ++k) {
-        const uint32_t idesc = tc::idesc_f16(128, 64 * (kTS - k)) | tc::kIdescAMajorMN;
+      for (int k = 0; k < ns; ++k) {
+        const uint32_t idesc = tc::idesc_f16(128, 64 * (ns - k)) | tc::kIdescAMajorMN;
 #pragma unroll
         for (int s = 0; s < 4; ++s)
           tc::mma_f16(d0 + (uint32_t)k * 64u,
@@ -424,9 +438,9 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
         // stacked along N
         const uint32_t zlo = tb, zhi = tb + (uint32_t)(kTS + 1) * kTile;
 #pragma unroll 1
-        for (int l = 0; l < kTS; ++l) {
+        for (int l = 0; l < ns; ++l) {
           const uint32_t tl = t0 + (uint32_t)l * kTile;
-          const uint32_t idesc = tc::idesc_f16(128, 64 * (kVS - l)) | tc::kIdescAMajorMN;
+          const uint32_t idesc = tc::idesc_f16(128, 64 * (ns - l)) | tc::kIdescAMajorMN;
 #pragma unroll
           for (int s = 0; s < 8; ++s) {
             const uint32_t pp = (uint32_t)(s >> 2), q = (uint32_t)(s & 3);
@@ -512,7 +526,7 @@ int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   DeviceState& d = h->d;
   cudaFuncSetAttribute(k_kin_xy_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemXY);
   KinTC a{reinterpret_cast<const uint4*>(d.kxy_slices), (int)((kTS + 2) * kTile / 16), d.e_txy, v,
-          reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status};
+          reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status, h->kin_slices};
   BSL_CUDA(launch_pdl(k_kin_xy_tc, dim3(std::min((a.nplanes + 1) / 2, sm_count())), dim3(kWsThreads), kSmemXY, s, a));
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
@@ -523,7 +537,7 @@ int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   DeviceState& d = h->d;
   cudaFuncSetAttribute(k_kin_z_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemZ);
   KinTC a{reinterpret_cast<const uint4*>(d.kz_slices), (int)(kTS * kTile / 16), d.e_tz, v,
-          reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status};
+          reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status, h->kin_slices};
   BSL_CUDA(launch_pdl(k_kin_z_tc, dim3(std::min((a.nplanes + 1) / 2, sm_count())), dim3(kWsThreads), kSmemZ, s, a));
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;

@@ -161,8 +161,8 @@ constexpr int kGraphIters = 8;
 // runs) unless the cached graph already matches the current configuration
 int ensure_iteration_graph(bsl_handle* h) {
   DeviceState& d = h->d;
-  const long long key[5] = {h->precision, h->kinetic_engine, h->lanczos_flip, (long long)(uintptr_t)d.hist,
-                            d.hist_cap};
+  const long long key[7] = {h->precision, h->kinetic_engine, h->lanczos_flip, (long long)(uintptr_t)d.hist,
+                            d.hist_cap, h->kin_slices, h->vformat};
   if (d.iter_exec && std::memcmp(key, d.graph_key, sizeof(key)) == 0) return BSL_OK;
   release_iteration_graph(d);
   cudaStream_t s = d.stream;
@@ -297,10 +297,29 @@ int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned
   // blocks of iterations interleaved across the problems' streams, so the
   // kernels of different problems overlap
   if ((rc = prepare_iterations(hs, n, niter))) return rc;
+  for (int b = 0; b < n; ++b) {
+    cudaSetDevice(hs[b]->p.device);
+    BSL_CUDA(cudaEventRecord(hs[b]->d.ev0, hs[b]->d.stream));
+  }
   if ((rc = run_iterations(hs, n, niter))) {
     for (int b = 0; b < n; ++b) cudaStreamSynchronize(hs[b]->d.stream);
     return rc;
   }
+  for (int b = 0; b < n; ++b) {
+    cudaSetDevice(hs[b]->p.device);
+    BSL_CUDA(cudaEventRecord(hs[b]->d.ev1, hs[b]->d.stream));
+  }
+  // the batch's device time: from the first problem's start to the last end
+  // (events of one device compare across streams)
+  float batch_ms = 0.f;
+  for (int b = 0; b < n; ++b) {
+    cudaSetDevice(hs[b]->p.device);
+    BSL_CUDA(cudaEventSynchronize(hs[b]->d.ev1));
+    float ms = 0.f;
+    if (hs[b]->p.device == hs[0]->p.device && cudaEventElapsedTime(&ms, hs[0]->d.ev0, hs[b]->d.ev1) == cudaSuccess)
+      batch_ms = ms > batch_ms ? ms : batch_ms;
+  }
+  for (int b = 0; b < n; ++b) hs[b]->last_ms_per_iter = batch_ms / niter;
   for (int b = 0; b < n; ++b) {
     bsl_handle* h = hs[b];
     cudaSetDevice(h->p.device);

@@ -11,10 +11,18 @@
 // so one tile's ntri x kTilePts floats are contiguous and a chunk of kChunk
 // rows is one contiguous copy of kChunk * 512 bytes.
 //
+// A precision variant streams BF16 blocks in the same layout (each point's
+// elements divided by its largest |element|, kept as one FP32 scale per point):
+// 32 rows per 8 KiB copy, the block product scaled once per point.
+//
 // One thread per grid point of a tile of 128 points:
 //   u(s) = ukin(s) + B l(l+1) v(s) + sum_s' V_ss' v(s')   (FP32 block product, FP32-pair sums)
 //   mode 0: out = u (FP64);   mode 1: R += c u (FP64), partial alpha = V . R (deterministic grid reduction);
 //   mode 2: mode 1 with V and R as double-float pairs
+#include <cuda_bf16.h>
+
+#include <type_traits>
+
 #include "bsl_device.cuh"
 
 namespace bsl {
@@ -84,12 +92,16 @@ __host__ __device__ constexpr int vstream_load_group(int nn) { return nn >= 21 &
 // Persistent: CTA b owns the contiguous tiles [b * A.tiles_per_cta, ...), and
 // its copy ring runs across tile boundaries, so the next tile's blocks are in
 // flight while the current tile finishes its epilogue.
-template <int NN>
+// kBF: BF16 blocks (A.vb16) scaled per point by A.vscale, twice the rows per
+// copy so that a copy still moves 8 KiB.
+template <int NN, bool kBF>
 __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(const StreamArgs A) {
+  using TB = typename std::conditional<kBF, uint16_t, float>::type;
   constexpr int NT = NN * (NN + 1) / 2;
-  constexpr int NCH = (NT + kChunk - 1) / kChunk;
+  constexpr int kCh = kBF ? 2 * kChunk : kChunk;  // block rows per copy
+  constexpr int NCH = (NT + kCh - 1) / kCh;
   extern __shared__ float4 ring4[];
-  float* ring = reinterpret_cast<float*>(ring4);  // [kStages][kChunk][kTilePts]
+  TB* ring = reinterpret_cast<TB*>(ring4);  // [kStages][kCh][kTilePts]
   __shared__ uint64_t full[kStages];
   __shared__ int abort_flag;
   __shared__ long long issued;
@@ -99,7 +111,8 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
   const long long t0 = (long long)blockIdx.x * A.tiles_per_cta;
   const long long t1 = t0 + A.tiles_per_cta < ntiles ? t0 + A.tiles_per_cta : ntiles;
   const long long nchunks = (t1 > t0 ? t1 - t0 : 0) * NCH;
-  const float* src0 = A.vb + t0 * (long long)NT * kTilePts;
+  const TB* src0 = reinterpret_cast<const TB*>(kBF ? (const void*)A.vb16 : (const void*)A.vb) +
+                   t0 * (long long)NT * kTilePts;
   const uint64_t pol = evict_first_policy();
   if (tid == 0) {
     // a stream that already timed out in an earlier launch disables the copies
@@ -114,12 +127,12 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
   auto issue = [&](long long g) {
     const int st = (int)(g % kStages);
     const int c = (int)(g % NCH);
-    const int rows = (c == NCH - 1) ? (NT - c * kChunk) : kChunk;
-    const uint32_t bytes = (uint32_t)rows * kTilePts * sizeof(float);
+    const int rows = (c == NCH - 1) ? (NT - c * kCh) : kCh;
+    const uint32_t bytes = (uint32_t)rows * kTilePts * sizeof(TB);
     mbar_expect_tx(&full[st], bytes);
     issued = g + 1;
-    bulk_copy_hint(ring + (size_t)st * kChunk * kTilePts,
-                   src0 + ((g / NCH) * NT + (long long)c * kChunk) * kTilePts, bytes, &full[st], pol);
+    bulk_copy_hint(ring + (size_t)st * kCh * kTilePts,
+                   src0 + ((g / NCH) * NT + (long long)c * kCh) * kTilePts, bytes, &full[st], pol);
   };
   if (tid == 0 && !abort_flag)
     for (long long g = 0; g < nchunks && g < kStages; ++g) issue(g);
@@ -166,15 +179,21 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
     for (int s = 0; s < NN; ++s) {
 #pragma unroll
       for (int q = s; q < NN; ++q, ++t) {
-        const long long g = g0 + t / kChunk;
+        const long long g = g0 + t / kCh;
         const int st = (int)(g % kStages);
-        if (t % kChunk == 0) {
+        if (t % kCh == 0) {
           if (!abort_flag && !mbar_wait(&full[st], (uint32_t)((g / kStages) & 1))) abort_flag = 1;
         }
-        const float x = ring[((size_t)st * kChunk + (t % kChunk)) * kTilePts + tid];
+        const TB xr = ring[((size_t)st * kCh + (t % kCh)) * kTilePts + tid];
+        float x;
+        if constexpr (kBF) {
+          x = __uint_as_float((uint32_t)xr << 16);
+        } else {
+          x = xr;
+        }
         va[s] = fmaf(x, vv[q], va[s]);
         if (q != s) va[q] = fmaf(x, vv[s], va[q]);
-        if (t % kChunk == kChunk - 1 || t == NT - 1) {
+        if (t % kCh == kCh - 1 || t == NT - 1) {
           __syncthreads();  // every thread is done with this stage
           if (tid == 0 && !abort_flag && g + kStages < nchunks) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -182,6 +201,11 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
           }
         }
       }
+    }
+    if (kBF && valid) {
+      const float sc = A.vscale[p];
+#pragma unroll
+      for (int s = 0; s < NN; ++s) va[s] *= sc;
     }
     // u = kinetic pair + B l(l+1) v + V v as an FP32 pair.
     // mode 1: the logical vectors are v = sv V and r = sr R; r + H v is kept as
@@ -259,19 +283,19 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
   }
 }
 
-template <int NN>
+template <int NN, bool kBF = false>
 int launch_nn(StreamArgs a, cudaStream_t s) {
   const size_t smem = (size_t)kStages * kChunk * kTilePts * sizeof(float);
-  cudaFuncSetAttribute(k_vstream<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_vstream<NN, kBF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const long long tiles = (a.npts + kTilePts - 1) / kTilePts;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vstream<NN>, kTilePts, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vstream<NN, kBF>, kTilePts, smem);
   const long long slots = (long long)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   a.tiles_per_cta = (tiles + slots - 1) / slots;
   const long long grid = (tiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
-  const cudaError_t e = launch_pdl(k_vstream<NN>, dim3((unsigned)grid), dim3(kTilePts), smem, s, a);
+  const cudaError_t e = launch_pdl(k_vstream<NN, kBF>, dim3((unsigned)grid), dim3(kTilePts), smem, s, a);
   return e == cudaSuccess ? BSL_OK : cuda_fail(e, "potential stream launch");
 }
 
@@ -408,7 +432,30 @@ int launch_update_stream(const float2* V, float2* R, long long L, double* partia
 
 long long vstream_tile_points() { return kTilePts; }
 
+// BF16 blocks: tile-major like the FP32 blocks, each point's elements divided
+// by that point's largest |element| (the FP32 scale), rounded to nearest
+__global__ void k_blocks_bf16(const double* __restrict__ vb64, long long npts, int ntri, uint16_t* vb16,
+                              float* vscale) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npts;
+       p += (long long)gridDim.x * blockDim.x) {
+    double m = 0.0;
+    for (int t = 0; t < ntri; ++t) m = fmax(m, fabs(vb64[(long long)t * npts + p]));
+    const float sc = m > 0.0 ? (float)m : 1.f;
+    vscale[p] = sc;
+    const long long base = (p / kTilePts) * ntri * kTilePts + p % kTilePts;
+    for (int t = 0; t < ntri; ++t) {
+      const __nv_bfloat16 b = __double2bfloat16(vb64[(long long)t * npts + p] / (double)sc);
+      vb16[base + (long long)t * kTilePts] = *reinterpret_cast<const uint16_t*>(&b);
+    }
+  }
+}
+
 int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s) {
+  if (a.vformat == BSL_VFMT_BF16) {
+    if (nn == 15) return launch_nn<15, true>(a, s);
+    if (nn == 21) return launch_nn<21, true>(a, s);
+    return fail(BSL_ERR_UNSUPPORTED, "BF16 potential blocks are built for blocks of 15 and 21 functions");
+  }
 #define BSL_CASE(K)                          \
   case K:                                    \
     if (int rc = launch_nn<K>(a, s)) return rc; \
@@ -431,6 +478,27 @@ int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s) {
   }
 #undef BSL_CASE
   BSL_CUDA(cudaGetLastError());
+  return BSL_OK;
+}
+
+int dev_vblocks_bf16(bsl_handle* h) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  const long long N = t.npts, ntri = (long long)t.nn * (t.nn + 1) / 2;
+  const long long tiled = (N + kTilePts - 1) / kTilePts * kTilePts;
+  if (!d.vb64) return fail(BSL_ERR_STATE, "FP64 potential blocks are not on the device");
+  cudaError_t e;
+  if ((e = cudaMalloc(&d.vb16, (size_t)(ntri * tiled) * sizeof(uint16_t))) != cudaSuccess ||
+      (e = cudaMalloc(&d.vscale, (size_t)tiled * sizeof(float))) != cudaSuccess) {
+    cudaFree(d.vb16);
+    d.vb16 = nullptr;
+    return fail(BSL_ERR_NOMEM, std::string("BF16 potential blocks: ") + cudaGetErrorString(e));
+  }
+  BSL_CUDA(cudaMemsetAsync(d.vb16, 0, (size_t)(ntri * tiled) * sizeof(uint16_t), d.stream));
+  BSL_CUDA(cudaMemsetAsync(d.vscale, 0, (size_t)tiled * sizeof(float), d.stream));
+  k_blocks_bf16<<<grid_for(N), kThreads, 0, d.stream>>>(d.vb64, N, (int)ntri, d.vb16, d.vscale);
+  BSL_CUDA(cudaGetLastError());
+  BSL_CUDA(cudaStreamSynchronize(d.stream));
   return BSL_OK;
 }
 

@@ -131,3 +131,25 @@ CONFIG_CPU = dict(name="15^3 even l<=4 12x24 (para)", n=15, x_max=0.08, l_max=4,
                   sym="Even", cage_seed=0, niter=600, levels=20)
 CONFIG_METRIC = dict(name="54^3 odd l<=5 40x70 (ortho)", n=54, x_max=0.08, l_max=5, theta_points=40,
                      phi_points=35, sym="Odd", cage_seed=1, niter=10000, levels=40)
+
+
+# The batched workload: 16 cages x {ortho, para} = 32 independent problems of
+# uneven size, 24 theta x 48 phi, 3000 iterations each.
+BATCH_EDGES = (27, 33, 41)
+
+
+def batch_problems(ncages=16, edge_seed=3):
+    """The 32 problems of the batched workload, as dicts: cage seeds 0..ncages-1,
+    each cage's circumradius drawn uniformly from [3.85, 4.05] A (generator
+    seeded with (cage seed, 1); the water orientations come from the cage seed
+    as in dodecahedral_cage), each cage in the ortho (odd l <= 5, 21
+    functions) and the para (even l <= 4, 15 functions) block, the grid edge of
+    every run drawn from BATCH_EDGES (generator seeded with edge_seed)."""
+    edges = np.random.default_rng(edge_seed).choice(BATCH_EDGES, size=2 * ncages)
+    out = []
+    for c in range(ncages):
+        radius = float(np.random.default_rng([c, 1]).uniform(3.85, 4.05))
+        for k, (sym, lmax) in enumerate((("Odd", 5), ("Even", 4))):
+            out.append(dict(cage_seed=c, radius=radius, sym=sym, l_max=lmax, n=int(edges[2 * c + k]),
+                            x_max=0.08, theta_points=24, phi_points=24, niter=3000))
+    return out

@@ -170,6 +170,25 @@ int bsl_set_precision(bsl_handle* h, int precision);
 int bsl_set_kinetic_engine(bsl_handle* h, int engine);
 int bsl_kinetic_engine(const bsl_handle* h);
 
+/* Precision variants of BSL_PREC_MIXED, for precision studies; no counterpart
+   in the reference (FP64 throughout).  The defaults are the exact tensor-core
+   kinetic (4 slices) and FP32 blocks.
+
+   Slices of v and of T kept by the tensor-core kinetic (1..4): v and T are cut
+   into 9-bit fixed-point slices and the slice products of classes k + l <
+   slices are accumulated; 4 (the default) is exact to ~2^-36 of each plane's
+   largest value, 2 keeps 3 products of 18-bit halves (a split 3-term product),
+   1 is a plain 9-bit product.  T loses its slices beyond `slices` too, a fixed
+   perturbation of the operator that shifts the levels. */
+int bsl_set_kinetic_slices(bsl_handle* h, int slices);
+
+/* Storage of the potential blocks streamed by BSL_PREC_MIXED. */
+#define BSL_VFMT_FP32 0 /* FP32 (default) */
+#define BSL_VFMT_BF16 1 /* BF16 scaled per grid point by max |block element| (FP32
+                           scale): half the bytes, unit roundoff 2^-9; blocks of
+                           15 and 21 functions */
+int bsl_set_potential_format(bsl_handle* h, int format);
+
 /* uec += H vec with host buffers in the reference layout.  Replaces
    Hv_linRotCartSph_NoQuad (linRotCartSphHvFullVPrepRoutines.cpp:807-822):
    same accumulation contract, same masking of the components outside the
@@ -306,7 +325,10 @@ int bsl_ritz_vectors_start(bsl_handle* h, int niter, int start, unsigned long lo
                            double* ritz);
 
 /* Timing of the last bsl_lanczos_run: average device milliseconds per
-   iteration, measured with CUDA events on the library's stream. */
+   iteration, measured with CUDA events on the library's stream.  After
+   bsl_lanczos_run_batch every handle of the batch reports the batch's device
+   time (first problem's start to last problem's end) divided by niter: the
+   time of one iteration of all the problems. */
 int bsl_last_run_ms_per_iter(const bsl_handle* h, double* ms);
 
 /* Diagnostic: one 128 x 64 x 64 TF32 product through the tensor cores

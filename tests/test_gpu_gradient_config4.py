@@ -1,0 +1,105 @@
+"""Hellmann-Feynman derivatives of the 10 lowest levels of one cage at the
+size the gradient workload names: 41^3 grid over +-0.4 A, odd l <= 5 (21
+functions), 30 theta x 60 phi, the generated SPC/E cage (seed 1), with
+respect to all 182 parameters: 60 site charges, 20 x 6 rigid-body coordinates
+(centre of mass in Angstrom, ZYZ Euler angles) and the 2 Alavi H2 charges.
+
+* Against the FP64 oracle (oracle/bsl_oracle.cpp hf_gradient, pinned on the
+  CPU to central differences of the compiled reference's H in
+  tests/test_oracle_gradient.py) on the same eigenvectors, all 182 parameters
+  and 10 levels.  The GPU kernel forms the angular densities in FP32 (FP64
+  totals per chunk of nodes); the measured deviation is printed and bounded by
+  2e-5 of the largest derivative of each parameter class and level.
+* Against central differences of the FP64 GPU levels, h = 1e-5 (e, Angstrom,
+  rad), on 20 parameters drawn with seed 7: within 1e-4 relative or 1e-5
+  kJ/mol per unit.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import OracleModel, load_inputs, load_package
+
+pytestmark = pytest.mark.gpu
+CALC = "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE"
+NLEV = 10
+NITER = 6000  # eigenvectors converged well enough that the derivatives (first order in their error) hold 1e-4
+FD_STEP = 1e-5
+
+
+def test_gradients_of_ten_levels_at_41_cubed(tmp_path):
+    bsl = load_package()
+    inp = load_inputs()
+    waters = inp.dodecahedral_cage(1)
+    cage = os.path.join(str(tmp_path), "cage.xyz")
+    inp.write_cage_xyz(cage, waters)
+    hv = os.path.join(str(tmp_path), "hv_input.txt")
+    inp.write_hv_input(hv, inp.hv_fields(41, 0.08, 5, 30, 30, cage, "gradient_41_odd_l5", "Odd"))
+    params = bsl.parse_hv_input(hv)
+    cm, ea = bsl.read_cage_xyz(cage)
+    q0 = bsl.cage_sites(cm, ea)[1]
+    qa0 = np.array([0.4932, -0.9864])
+
+    def levels(cm_, ea_, q_, qa_, vectors=False):
+        h = bsl.Hamiltonian.from_cage(params, cm_, ea_, q_, qa_, precision="fp64")
+        try:
+            a, b, b2 = h.lanczos(NITER, start="normal", seed=1)
+            ev, _ = bsl.good_eigenvalues(a, b, b2, -10.0, 10.0)
+            assert len(ev) >= NLEV
+            ev = ev[:NLEV]
+            if not vectors:
+                return ev, None, None
+            rows = bsl.tm_eigenvectors(a, b, b2, ev)
+            psi = h.ritz(NITER, rows, start="normal", seed=1)
+            return ev, psi, h.hf_gradient(psi, 60)
+        finally:
+            h.close()
+
+    ev, psi, (dq, dr, da) = levels(cm, ea, q0, qa0, vectors=True)
+    print("levels (kJ/mol):", ev.tolist(), "smallest gap:", float(np.min(np.diff(ev))))
+    dcm, dea = bsl.rigid_body_gradient(cm, ea, dr)
+    grad = np.concatenate([dq, dcm.reshape(NLEV, -1), dea.reshape(NLEV, -1), da], axis=1)  # [10, 182]
+    assert grad.shape == (NLEV, 182)
+
+    # ---- the FP64 oracle on the same eigenvectors ----
+    m = OracleModel(CALC, hv, threads=os.cpu_count() or 8)
+    try:
+        oq, odr, oa = m.hf_gradient(psi, 60)
+        ocm, oea = m.rigid_body_gradient(odr)
+    finally:
+        m.close()
+    ograd = np.concatenate([oq, ocm.reshape(NLEV, -1), oea.reshape(NLEV, -1), oa], axis=1)
+    classes = {"site charges": slice(0, 60), "centres": slice(60, 120), "Euler angles": slice(120, 180),
+               "Alavi charges": slice(180, 182)}
+    worst = {}
+    for name, sl in classes.items():
+        scale = np.max(np.abs(ograd[:, sl]), axis=1, keepdims=True)
+        worst[name] = float(np.max(np.abs(grad[:, sl] - ograd[:, sl]) / scale))
+    print("GPU vs FP64 oracle, max deviation / largest derivative per class and level:", worst)
+    assert max(worst.values()) <= 2e-5, worst
+
+    # ---- central differences of the FP64 levels on 20 random parameters ----
+    picks = np.sort(np.random.default_rng(7).choice(182, size=20, replace=False))
+
+    def perturbed(k, s):
+        cm2, ea2, q2, qa2 = cm.copy(), ea.copy(), q0.copy(), qa0.copy()
+        if k < 60:
+            q2[k] += s
+        elif k < 120:
+            cm2[(k - 60) // 3, (k - 60) % 3] += s
+        elif k < 180:
+            ea2[(k - 120) // 3, (k - 120) % 3] += s
+        else:
+            qa2[k - 180] += s
+        return cm2, ea2, q2, qa2
+
+    devs = []
+    for k in picks:
+        ep = levels(*perturbed(k, FD_STEP))[0]
+        em = levels(*perturbed(k, -FD_STEP))[0]
+        fd = (ep - em) / (2 * FD_STEP)
+        devs.append(float(np.max(np.abs(fd - grad[:, k]) / np.maximum(np.abs(fd), 0.1))))
+        assert np.allclose(grad[:, k], fd, rtol=1e-4, atol=1e-5), (int(k), grad[:, k], fd)
+    print("GPU vs central differences (h = 1e-5), parameters", picks.tolist(), "max relative deviation",
+          max(devs))

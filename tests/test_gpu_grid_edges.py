@@ -8,8 +8,8 @@ sums, the potential-block stream at the full tile count, the FP64 path) do not
 depend on the angular grid, which only enters the potential blocks.
 
 Tolerances: FP64 H v against the oracle <= 1e-10 relative (max abs / max abs);
-the first 10 FP64 alpha/beta against the oracle's <= 1e-10 of max |alpha|, the
-first 20 <= 1e-9;
+alpha_1 against the oracle's <= 1e-14 and the first 20 FP64 alpha/beta <= 2e-10
+of max |alpha|;
 mixed H v of both kinetic engines against FP64 <= 2e-6; the first 20 mixed
 alpha/beta against FP64 <= 1e-6 of max |alpha|.
 """
@@ -49,12 +49,13 @@ def test_metric_and_batch_grids_match_oracle(tmp_path, n):
         ao, bo, _ = m.lanczos(20)
         scale = np.max(np.abs(ao))
         ea, eb = np.abs(a - ao) / scale, np.abs(b[1:] - bo[1:]) / scale
-        # the first 10 to 1e-10; later ones to 1e-9: the reference's serial FP64
-        # sums over 5.7 M terms (restated in the oracle) carry ~1e-13 relative
-        # rounding per dot product, which the recurrence amplifies (1.1e-10 at
-        # iteration 20 of the 54^3 case, measured)
-        assert ea[:10].max() <= 1e-10 and eb[:10].max() <= 1e-10, (ea, eb)
-        assert ea.max() <= 1e-9 and eb.max() <= 1e-9, (ea, eb)
+        # alpha_1 = v.Hv agrees to rounding (2e-16 measured at 54^3); from the
+        # second iteration on, the recurrence amplifies the rounding differences
+        # of the two FP64 summation orders (FMA-contracted on the GPU, the
+        # reference's serial sums in the oracle) ~1e5-fold from the uniform start
+        # (1.8e-11 at alpha_2, at most 1.1e-10 over the first 20 at 54^3, measured)
+        assert ea[0] <= 1e-14, ea[0]
+        assert ea.max() <= 2e-10 and eb.max() <= 2e-10, (ea, eb)
         h.set_precision("mixed")
         assert h.kinetic_engine() == "tensor"
         for engine in ("tensor", "simt"):
