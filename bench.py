@@ -213,11 +213,18 @@ def measured_peak_hbm():
 # iteration: one-pass ncu capture with the L2 left as the previous kernel left it
 # (profiles/pipeline_traffic_warm_54cubed_odd_l5.md).
 _TRAFFIC_SRC = "profiles/pipeline_traffic_warm_54cubed_odd_l5.md"
-NCU_TRAFFIC = {"k_kin_xy_tc": (12.55e6, _TRAFFIC_SRC),
-               "k_kin_z_tc": (2.82e6, _TRAFFIC_SRC),
+NCU_TRAFFIC = {"k_kin_xy_tc": (13.33e6, _TRAFFIC_SRC),
+               "k_kin_z_tc": (3.17e6, _TRAFFIC_SRC),
+               "k_vstream<NN,coefficients>": (84.45e6, _TRAFFIC_SRC),
                "k_vstream<NN>": (200.97e6, _TRAFFIC_SRC),
-               "k_update_stream": (10.10e6, _TRAFFIC_SRC)}
+               "k_update_stream": (9.05e6, _TRAFFIC_SRC)}
 
+
+# potential values streamed per grid point in the spherical-harmonic form, by
+# block size (csrc/bsl_gaunt.h: L <= 2 l_max of the block's parity)
+GAUNT_ROWS = {21: 66, 15: 45, 10: 28}
+VARIANT = {"gaunt": "V as FP32 spherical-harmonic coefficients (%d per point; blocks rebuilt per point)",
+           "fp32": "V blocks, symmetric-packed FP32 (upper triangle, nn(nn+1)/2 per point)"}
 
 # H v time of the compiled reference against the oracle port on the same input,
 # 8 OpenMP threads, measured in the x86 container that has the reference tree
@@ -254,9 +261,11 @@ def replica_rate(units_per_rank, seconds, world):
     return world * units_per_rank / seconds
 
 
-def stage_bytes(cfg, D, N, nn, mixed):
-    """Algorithmic bytes per launch of each stage of one Lanczos iteration."""
-    ntri = nn * (nn + 1) // 2
+def stage_bytes(cfg, D, N, nn, mixed, rows=None):
+    """Algorithmic bytes per launch of each stage of one Lanczos iteration;
+    `rows` potential values streamed per grid point (default: the upper
+    triangle of the block, nn (nn + 1) / 2)."""
+    ntri = nn * (nn + 1) // 2 if rows is None else rows
     vb = ntri * N * (4 if mixed else 8)
     return [2 * D * 8,              # kinetic x/y: read v, write u_kin
             3 * D * 8,              # kinetic z: read v, read+write u_kin
@@ -278,11 +287,13 @@ def stable_levels(bsl, a, b, b2, drop=200, tol=1e-9, unit=None):
 
 # Precision variants of the metric problem: (name, potential blocks, kinetic
 # engine, tensor-core slices); the Lanczos recurrence is double-float in all.
-SWEEP = [("V fp32, kinetic tensor-core 4 slices (exact, default)", "fp32", "tensor", 4),
-         ("V fp32, kinetic tensor-core 3 slices", "fp32", "tensor", 3),
-         ("V fp32, kinetic tensor-core 2 slices (split 3-term)", "fp32", "tensor", 2),
-         ("V fp32, kinetic tensor-core 1 slice (plain 9-bit)", "fp32", "tensor", 1),
-         ("V fp32, kinetic CUDA-core fp32 head+tail", "fp32", "simt", 4),
+SWEEP = [("V fp32 spherical-harmonic coefficients, kinetic tensor-core 4 slices (exact, default)", "gaunt",
+          "tensor", 4),
+         ("V fp32 blocks, kinetic tensor-core 4 slices (exact)", "fp32", "tensor", 4),
+         ("V fp32 coefficients, kinetic tensor-core 3 slices", "gaunt", "tensor", 3),
+         ("V fp32 coefficients, kinetic tensor-core 2 slices (split 3-term)", "gaunt", "tensor", 2),
+         ("V fp32 coefficients, kinetic tensor-core 1 slice (plain 9-bit)", "gaunt", "tensor", 1),
+         ("V fp32 coefficients, kinetic CUDA-core fp32 head+tail", "gaunt", "simt", 4),
          ("V bf16 per-point scale, kinetic tensor-core 4 slices", "bf16", "tensor", 4),
          ("V bf16 per-point scale, kinetic tensor-core 2 slices", "bf16", "tensor", 2),
          ("V bf16 per-point scale, kinetic tensor-core 1 slice", "bf16", "tensor", 1)]
@@ -307,6 +318,7 @@ def precision_sweep(bsl, h, ref_levels, n_it, fp64_rate, timed=2000):
     recs = [{"variant": "V fp64, kinetic fp64 (the FP64 path)", "iter_s": fp64_rate, "max_abs_dE_cm-1": 0.0,
              "levels_within_1e-3_cm-1": len(ref_levels)}]
     h.set_precision("mixed")
+    default_format = h.potential_format()
     for name, vfmt, engine, slices in SWEEP:
         h.set_potential_format(vfmt)
         h.set_kinetic_engine(engine)
@@ -321,7 +333,7 @@ def precision_sweep(bsl, h, ref_levels, n_it, fp64_rate, timed=2000):
                      "levels_within_1e-3_cm-1": int(np.sum(dev <= 1e-3)),
                      "max_abs_dE_cm-1_fp64_tail_tolerance": float(dev_r.max()),
                      "levels_within_1e-3_cm-1_fp64_tail_tolerance": int(np.sum(dev_r <= 1e-3))})
-    h.set_potential_format("fp32")
+    h.set_potential_format(default_format)
     h.set_kinetic_slices(4)
     h.set_kinetic_engine("tensor")
     return recs
@@ -351,9 +363,13 @@ def batched_workload(bsl, tmp, device, fp64_check=True, nlev=10):
     prep_s = time.perf_counter() - t0
     niter = probs[0]["niter"]
     total = len(probs) * niter
-    bsl.lanczos_batch(hs, 64, start="normal", seed=0)  # warm-up: graphs captured and cached
+    tune = bsl.autotune(hs, 64)  # launch shapes of the grouped batch
+    bsl.lanczos_batch(hs, 64, start="normal", seed=0)  # warm-up
     runs = bsl.lanczos_batch(hs, niter, start="normal", seed=0)
     batch_ms = hs[0].last_ms_per_iter() * niter
+    bsl.lanczos_batch(hs, 64, start="normal", seed=0, grouped=False)  # warm-up: per-problem graphs cached
+    bsl.lanczos_batch(hs, niter, start="normal", seed=0, grouped=False)
+    streams_ms = hs[0].last_ms_per_iter() * niter
     sep_ms = 0.0
     for h in hs:
         h.lanczos(niter, start="normal", seed=0)
@@ -362,9 +378,15 @@ def batched_workload(bsl, tmp, device, fp64_check=True, nlev=10):
            "coefficients_total": int(sum(h.packed_size for h in hs)),
            "edges": [pr["n"] for pr in probs], "blocks": [h.nn for h in hs],
            "batched_iter_s": total / (batch_ms * 1e-3), "batched_ms": batch_ms,
+           "path": "bsl_lanczos_run_batch: four grouped launches per iteration of all the problems "
+                   "(each CTA on one problem), 8-iteration graph",
+           "streams_iter_s": total / (streams_ms * 1e-3), "streams_ms": streams_ms,
+           "streams_path": "bsl_lanczos_run_batch_streams: one stream per problem, 8-iteration graphs "
+                           "interleaved",
            "sequential_iter_s": total / (sep_ms * 1e-3), "sequential_ms": sep_ms,
-           "path": "bsl_lanczos_run_batch (one stream per problem, 8-iteration graphs interleaved)",
-           "prep_seconds": prep_s}
+           "prep_seconds": prep_s,
+           "launch_shapes": {"potential_stream_ctas_per_sm": tune[0], "update_ctas_per_sm": tune[1],
+                             "by": "bsl_autotune"}}
     if fp64_check:
         worst, within, cnt = 0.0, 0, 0
         for h, (am, bm, bm2) in zip(hs, runs):
@@ -446,6 +468,7 @@ def main():
     if args.kinetic != "auto":
         h.set_kinetic_engine(args.kinetic)
     kinetic_engine = h.kinetic_engine()
+    gaunt_resid = h.gaunt_residual()
     D, Df, nn = h.packed_size, h.basis_size, h.nn
     N = D // nn
     if args.profile_iters:
@@ -461,6 +484,8 @@ def main():
         sync_ranks(dist)
 
     # ---- device-resident mixed path (value) ----
+    # launch shapes picked by the library's autotuner (outside the timed region)
+    tune = bsl.autotune([h], 100)
     h.lanczos(max(3, args.warmup))
     barrier()
     with ClockSampler(local) as clk:
@@ -483,7 +508,9 @@ def main():
     nst = bsl.lib().bsl_launches_per_iteration(h.handle)
     stage_names = [names[i].decode() for i in range(nst)] if rc == 0 else []
     stage_ms = stage_ms[:nst]
-    sb = stage_bytes(cfg, D, N, nn, True)[:nst]
+    vfmt = h.potential_format()
+    rows = {"gaunt": GAUNT_ROWS.get(nn), "fp32": None}.get(vfmt)
+    sb = stage_bytes(cfg, D, N, nn, True, rows)[:nst]
     peak, peak_src = measured_peak_hbm()
     dom = int(np.argmax(stage_ms))
     achieved = sb[dom] / (stage_ms[dom] * 1e-3) / 1e9
@@ -583,7 +610,8 @@ def main():
                 "path": "bsl_lanczos_step_host: reference loop body with host (pinned) vec/rvec in the reference "
                         "layout, H2D + Hv + recurrence + D2H per step"},
         "roofline": {"bound": "hbm", "kernel": stage_names[dom] if stage_names else None,
-                     "variant": "V blocks, symmetric-packed FP32 (upper triangle, nn(nn+1)/2 per point)",
+                     "variant": (VARIANT[vfmt] % GAUNT_ROWS[nn]) if vfmt == "gaunt" else VARIANT.get(vfmt, vfmt),
+                     "gaunt_residual_kJ_mol": gaunt_resid,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": (NCU_TRAFFIC[stage_names[dom]][0]
                                  if stage_names and stage_names[dom] in NCU_TRAFFIC else None),
@@ -607,6 +635,8 @@ def main():
                                                     "build container; the port is faster, so the baseline is "
                                                     "conservative"),
         "clocks": clocks, "gpu_launches": nst * args.steps, "prep_seconds": prep_s,
+        "launch_shapes": {"potential_stream_ctas_per_sm": tune[0], "update_ctas_per_sm": tune[1],
+                          "autotune_ms_per_iter": tune[2], "by": "bsl_autotune"},
         "wall_ms_per_step": 1000.0 * wall / args.steps,
     }
     print(json.dumps(line))

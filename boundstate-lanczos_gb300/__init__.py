@@ -25,7 +25,7 @@ POT_POINT_ALAVI_SPCE, POT_POINT_ALAVI_TIP4P, POT_COULOMB = 3, 4, 5
 PREC = {"fp64": 0, "mixed": 1}
 START = {"uniform": 0, "normal": 1}
 KINETIC = {"simt": 0, "tensor": 1}
-VFORMAT = {"fp32": 0, "bf16": 1}
+VFORMAT = {"fp32": 0, "bf16": 1, "gaunt": 2}
 MIXED_UNIT_ROUNDOFF = 4.0e-15  # BSL_MIXED_UNIT_ROUNDOFF
 CALCULATORS = {
     "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE": POT_ALAVI_SPCE,
@@ -94,6 +94,7 @@ def lib():
     L.bsl_lanczos_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong, _P, _P, _P]
     L.bsl_lanczos_run_batch.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_ulonglong,
                                         C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]
+    L.bsl_lanczos_run_batch_streams.argtypes = L.bsl_lanczos_run_batch.argtypes
     L.bsl_lanczos_step_host.argtypes = [C.c_void_p, _P, _P, _P, _P, _P]
     L.bsl_good_eigenvalues.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_int)]
     L.bsl_good_eigenvalues_unit.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, _P, _P,
@@ -116,8 +117,13 @@ def lib():
     L.bsl_parse_coulomb_input.argtypes = [C.c_char_p, C.POINTER(HvParams)]
     L.bsl_calculator_potential.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
     L.bsl_debug_inject_timeout.argtypes = [C.c_void_p, C.c_int]
+    L.bsl_autotune.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                               _P]
     L.bsl_set_kinetic_slices.argtypes = [C.c_void_p, C.c_int]
     L.bsl_set_potential_format.argtypes = [C.c_void_p, C.c_int]
+    L.bsl_potential_format.argtypes = [C.c_void_p]
+    L.bsl_gaunt_residual.argtypes = [C.c_void_p]
+    L.bsl_gaunt_residual.restype = C.c_double
     _lib = L
     return L
 
@@ -165,15 +171,29 @@ def tm_eigenvectors(alpha, beta, beta2, evals):
     return out.reshape(ngood, niter)  # row n = column n of the column-major evtr
 
 
-def lanczos_batch(hamiltonians, niter, start="uniform", seed=0):
-    """Loop 1 for several prepared problems at once (bsl_lanczos_run_batch);
-    returns a list of (alpha, beta, beta2)."""
+def lanczos_batch(hamiltonians, niter, start="uniform", seed=0, grouped=True):
+    """Loop 1 for several prepared problems at once: grouped launches where the
+    problems allow them (bsl_lanczos_run_batch), or with grouped=False one
+    stream per problem (bsl_lanczos_run_batch_streams); returns a list of
+    (alpha, beta, beta2)."""
     n = len(hamiltonians)
     out = [(np.zeros(niter), np.zeros(niter + 1), np.zeros(niter + 1)) for _ in range(n)]
     hs = (C.c_void_p * n)(*[h.handle for h in hamiltonians])
     arr = [(_P * n)(*[_ptr(o[k]) for o in out]) for k in range(3)]
-    _check(lib().bsl_lanczos_run_batch(hs, n, niter, START[start], seed, arr[0], arr[1], arr[2]))
+    f = lib().bsl_lanczos_run_batch if grouped else lib().bsl_lanczos_run_batch_streams
+    _check(f(hs, n, niter, START[start], seed, arr[0], arr[1], arr[2]))
     return out
+
+
+def autotune(hamiltonians, iters=200):
+    """Pick the launch shapes of one problem or a batch by timing
+    (bsl_autotune); returns (potential-stream CTAs per SM, update CTAs per SM,
+    best ms per iteration)."""
+    n = len(hamiltonians)
+    hs = (C.c_void_p * n)(*[h.handle for h in hamiltonians])
+    vs, up, ms = C.c_int(0), C.c_int(0), np.zeros(1)
+    _check(lib().bsl_autotune(hs, n, iters, C.byref(vs), C.byref(up), _ptr(ms)))
+    return vs.value, up.value, float(ms[0])
 
 
 def _f64(x):
@@ -312,8 +332,20 @@ class Hamiltonian:
         _check(lib().bsl_set_kinetic_slices(self._h, slices))
 
     def set_potential_format(self, fmt):
-        """Potential blocks of the mixed path: "fp32" or "bf16" (per-point scale)."""
+        """Potential blocks of the mixed path: "gaunt" (spherical-harmonic
+        coefficients, the default where the basis has them), "fp32" or "bf16"
+        (per-point scale)."""
         _check(lib().bsl_set_potential_format(self._h, VFORMAT[fmt]))
+
+    def potential_format(self):
+        f = lib().bsl_potential_format(self._h)
+        if f < 0:
+            raise BslError(ERR_STATE, "closed handle")
+        return {v: k for k, v in VFORMAT.items()}[f]
+
+    def gaunt_residual(self):
+        """Largest |FP64 block element - its spherical-harmonic expansion| (kJ/mol), -1 if none."""
+        return lib().bsl_gaunt_residual(self._h)
 
     def kinetic_engine(self):
         e = lib().bsl_kinetic_engine(self._h)

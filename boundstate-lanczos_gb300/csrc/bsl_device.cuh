@@ -164,8 +164,11 @@ __device__ __forceinline__ float2 warp_sum_df(float2 v) {
 // reduce_grid for double-float per-thread parts: the block sums run on the
 // FP32 pipe (double-float shuffles), only one FP64 value per block is formed,
 // and the last block adds the per-block values in FP64 in a fixed order.
-__device__ __forceinline__ bool reduce_grid_df(float2 part, double* partials, unsigned int* counter,
-                                               double* total) {
+// The same over `count` blocks that share partials and counter, this block
+// being number `index` of them (a grouped launch reduces each problem over its
+// own blocks); reduce_grid_df is the whole grid.
+__device__ __forceinline__ bool reduce_group_df(float2 part, double* partials, unsigned int* counter,
+                                                unsigned int count, unsigned int index, double* total) {
   __shared__ float2 shd[32];
   __shared__ bool last_df;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -176,16 +179,16 @@ __device__ __forceinline__ bool reduce_grid_df(float2 part, double* partials, un
     const int nw = (blockDim.x + 31) >> 5;
     v = warp_sum_df(lane < nw ? shd[lane] : make_float2(0.f, 0.f));
     if (lane == 0) {
-      partials[blockIdx.x] = f64_of_df(v);
+      partials[index] = f64_of_df(v);
       __threadfence();
-      last_df = (atomicAdd(counter, 1u) == gridDim.x - 1);
+      last_df = (atomicAdd(counter, 1u) == count - 1);
     }
   }
   __syncthreads();
   if (!last_df) return false;
   __threadfence();
   double acc = 0.0;
-  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) acc += __ldcg(partials + b);
+  for (unsigned int b = threadIdx.x; b < count; b += blockDim.x) acc += __ldcg(partials + b);
   acc = block_sum(acc);
   if (threadIdx.x == 0) {
     *total = acc;
@@ -194,28 +197,39 @@ __device__ __forceinline__ bool reduce_grid_df(float2 part, double* partials, un
   return true;
 }
 
-// Stores this block's partial; returns true (in every thread) for the last
-// block, which then holds the grand total in *total (thread 0 only).
-__device__ __forceinline__ bool reduce_grid(double part, double* partials, unsigned int* counter, double* total) {
+__device__ __forceinline__ bool reduce_grid_df(float2 part, double* partials, unsigned int* counter,
+                                               double* total) {
+  return reduce_group_df(part, partials, counter, gridDim.x, blockIdx.x, total);
+}
+
+// Stores this block's partial; returns true (in every thread) for the last of
+// `count` blocks (this one number `index`), which then holds the grand total in
+// *total (thread 0 only).
+__device__ __forceinline__ bool reduce_group(double part, double* partials, unsigned int* counter,
+                                             unsigned int count, unsigned int index, double* total) {
   __shared__ bool last;
   double s = block_sum(part);
   if (threadIdx.x == 0) {
-    partials[blockIdx.x] = s;
+    partials[index] = s;
     __threadfence();
     const unsigned int prev = atomicAdd(counter, 1u);
-    last = (prev == gridDim.x - 1);
+    last = (prev == count - 1);
   }
   __syncthreads();
   if (!last) return false;
   __threadfence();
   double acc = 0.0;
-  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) acc += __ldcg(partials + b);
+  for (unsigned int b = threadIdx.x; b < count; b += blockDim.x) acc += __ldcg(partials + b);
   acc = block_sum(acc);
   if (threadIdx.x == 0) {
     *total = acc;
     *counter = 0u;
   }
   return true;
+}
+
+__device__ __forceinline__ bool reduce_grid(double part, double* partials, unsigned int* counter, double* total) {
+  return reduce_group(part, partials, counter, gridDim.x, blockIdx.x, total);
 }
 
 // ---------------------------------------------------------------------------

@@ -333,6 +333,7 @@ void free_device(DeviceState& d) {
   if (d.jdev) cudaFree(d.jdev);
   if (d.vb16) cudaFree(d.vb16);
   if (d.vscale) cudaFree(d.vscale);
+  if (d.vc32) cudaFree(d.vc32);
   if (d.copy_done) cudaEventDestroy(d.copy_done);
   if (d.vec_in) cudaEventDestroy(d.vec_in);
   if (d.copy_stream) cudaStreamDestroy(d.copy_stream);
@@ -483,6 +484,19 @@ int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
   }
   if (rc) return bail(rc);
   if ((rc = dev_vblocks(h))) return bail(rc);
+  // the mixed path streams the blocks as spherical-harmonic coefficients where
+  // the basis has a generated expansion and the blocks reproduce from them
+  if (gaunt_coefficient_count(h) > 0) {
+    double resid = 0.0, vmax = 0.0;
+    if ((rc = dev_gaunt_coeffs(h, &resid, &vmax))) return bail(rc);
+    h->gaunt_residual = resid;
+    if (resid <= 1e-10 * vmax) {
+      h->vformat = BSL_VFMT_GAUNT;
+    } else {
+      cudaFree(d.vc32);
+      d.vc32 = nullptr;
+    }
+  }
   if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return bail(cuda_fail(e, "HvPrep"));
   // the potential grid is only needed to build the blocks; keep it for
   // inspection (bsl_copy_vgrid) when it is small
@@ -691,6 +705,10 @@ int bsl_set_kinetic_engine(bsl_handle* h, int engine) {
 
 int bsl_kinetic_engine(const bsl_handle* h) { return h ? h->kinetic_engine : -1; }
 
+int bsl_potential_format(const bsl_handle* h) { return h ? h->vformat : -1; }
+
+double bsl_gaunt_residual(const bsl_handle* h) { return h ? h->gaunt_residual : -1.0; }
+
 int bsl_set_kinetic_slices(bsl_handle* h, int slices) {
   if (!h) return fail(BSL_ERR_STATE, "null handle");
   if (slices < 1 || slices > 4) return fail(BSL_ERR_INPUT, "kinetic slices must be 1..4");
@@ -700,7 +718,10 @@ int bsl_set_kinetic_slices(bsl_handle* h, int slices) {
 
 int bsl_set_potential_format(bsl_handle* h, int format) {
   if (!h) return fail(BSL_ERR_STATE, "null handle");
-  if (format != BSL_VFMT_FP32 && format != BSL_VFMT_BF16) return fail(BSL_ERR_INPUT, "unknown block format");
+  if (format != BSL_VFMT_FP32 && format != BSL_VFMT_BF16 && format != BSL_VFMT_GAUNT)
+    return fail(BSL_ERR_INPUT, "unknown block format");
+  if (format == BSL_VFMT_GAUNT && !h->d.vc32)
+    return fail(BSL_ERR_UNSUPPORTED, "no spherical-harmonic expansion of the blocks for this basis");
   if (format == BSL_VFMT_BF16 && h->t.nn != 15 && h->t.nn != 21)
     return fail(BSL_ERR_UNSUPPORTED, "BF16 potential blocks are built for blocks of 15 and 21 functions");
   cudaSetDevice(h->p.device);

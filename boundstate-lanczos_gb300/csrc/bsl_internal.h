@@ -137,11 +137,13 @@ struct DeviceState {
   // something its launches depend on changes (graph_key)
   cudaGraph_t iter_graph = nullptr;
   cudaGraphExec_t iter_exec = nullptr;
-  // precision, kinetic engine, buffer roles, hist, hist_cap, kinetic slices, block format
-  long long graph_key[7] = {0, 0, 0, 0, 0, 0, 0};
+  // precision, kinetic engine, buffer roles, hist, hist_cap, kinetic slices, block format, launch shapes
+  long long graph_key[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   // BF16 potential blocks (tile-major like vb32) and their per-point FP32 scales
   uint16_t* vb16 = nullptr;
   float* vscale = nullptr;
+  // the blocks as spherical-harmonic coefficients, FP32 tile-major [tile][k][128]
+  float* vc32 = nullptr;
   // test hook: status words set again after every reset of the status (host-side
   // injection of a kernel time-out; bit 2: potential stream, bit 3: kinetic)
   int inject_status = 0;
@@ -158,6 +160,10 @@ struct bsl_handle {
   int kinetic_engine = BSL_KIN_SIMT;  // engine of the mixed-precision kinetic (BSL_KIN_*)
   int kin_slices = 4;                 // 9-bit slices of the tensor-core kinetic (4: exact)
   int vformat = BSL_VFMT_FP32;        // storage of the mixed path's potential blocks (BSL_VFMT_*)
+  double gaunt_residual = -1.0;       // largest |block - expansion| at prep (FP64), -1: no expansion
+  // launch shapes picked by bsl_autotune (0: the defaults): resident CTAs per SM
+  // of the potential stream (capped by its occupancy) and of the update
+  int tune_vs = 0, tune_upd = 0;
   double last_ms_per_iter = 0.0;
   int lanczos_flip = 0;           // 0: vec holds v_j and rvec r_j; 1: roles swapped
   int state_pairs = -1;           // Lanczos buffers: 0 FP64, 1 double-float pairs (mixed), -1 not set up
@@ -204,6 +210,13 @@ void kinetic_smem_image(const std::vector<double>& T, int n, bool with_zero_tile
 bool kinetic_tc_supported(const Tables& t);
 int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s);
 int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s);
+// grouped tensor-core kinetic over several problems: per-problem argument
+// records (kin_group_arg_size() bytes each, filled by kin_tc_group_args for the
+// vectors v[b]) and per-CTA work (problem, first pair, end pair, 0)
+size_t kin_group_arg_size();
+long long kin_tc_pairs(const bsl_handle* h, bool xy);
+void kin_tc_group_args(bsl_handle** hs, int n, const float2* const* v, bool xy, void* args);
+int launch_kin_tc_group(bool xy, const void* d_args, const int4* d_work, int nctas, cudaStream_t s);
 
 // potential-block apply (bsl_vapply_f32.cu / bsl_vapply_f64.cu)
 // FP32 blocks in the tile-major layout of bsl_vstream.cu (vstream_tile_points() points per tile)
@@ -217,7 +230,10 @@ struct StreamArgs {
   double* out;          // mode 0: u = H v; mode 1: the Lanczos r buffer (r += c H v)
   const uint16_t* vb16; // BSL_VFMT_BF16: tile-major BF16 blocks, V = vscale[p] * block
   const float* vscale;
+  const float* vc;      // BSL_VFMT_GAUNT: tile-major spherical-harmonic coefficients
   int vformat;
+  int nn, red_count;    // grouped launch: block size, blocks that reduce this problem's alpha
+  int ctas_per_sm;      // 0: as many as fit
   long long npts, dpk;
   long long tiles_per_cta;  // set by the launcher
   int mode, j;          // j > 0: the iteration; j == 0: read it from *jdev
@@ -233,13 +249,35 @@ long long vstream_tile_points();
 // j == 0: the iteration is read from *jdev, which the last block then advances
 int launch_update_stream(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
                          double* scalars, double* hist, int hist_stride, int j, int* jdev, int* status,
-                         cudaStream_t s);
+                         cudaStream_t s, int ctas_per_sm = 0);
+// grouped launches over several problems: per-problem argument records and
+// per-CTA work (problem, first unit, end unit, block index in the problem's
+// reduction); tiles of vstream_tile_points() points, update units of two
+// double-float values
+size_t vstream_group_arg_size();
+size_t update_group_arg_size();
+long long update_units(long long L);
+bool vstream_group_supported(int nn);
+int vstream_group_ctas_per_sm();
+void update_group_arg(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
+                      double* scalars, double* hist, int hist_stride, int* jdev, int* status, int red_count,
+                      void* out);
+int launch_vstream_group(const void* d_args, const int4* d_work, int nctas, cudaStream_t s);
+int launch_update_group(const void* d_args, const int4* d_work, int nctas, cudaStream_t s);
+// the potential stream's arguments for one problem (mode 2, j from the device counter)
+StreamArgs vstream_args(bsl_handle* h, const double* v, double* out);
 int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,
                       const double* rot, double* out, long long N, int mode, double* partials, unsigned int* counter,
                       double* scalars, double* hist, int j, long long dpk);
 
 // BF16 copy of the potential blocks with per-point scales (bsl_vstream.cu)
 int dev_vblocks_bf16(bsl_handle* h);
+// spherical-harmonic coefficients of the potential blocks (bsl_gaunt.cu): the
+// count for the handle's basis (0: no generated expansion), and the prep that
+// recovers them from the FP64 blocks (largest reconstruction residual and
+// largest |block element| returned)
+int gaunt_coefficient_count(const bsl_handle* h);
+int dev_gaunt_coeffs(bsl_handle* h, double* residual, double* vmax);
 
 // the cached iteration graph (bsl_lanczos.cpp)
 void release_iteration_graph(DeviceState& d);

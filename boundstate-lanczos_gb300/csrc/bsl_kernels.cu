@@ -611,27 +611,9 @@ int launch_vapply(bsl_handle* h, const double* v, double* out, int mode, int j, 
   const dim3 g(grid_for(N));
   const long long dpk = N * t.nn;
   if (h->precision == BSL_PREC_MIXED) {
-    StreamArgs a;
-    a.vb = d.vb32;
-    a.v32 = d.v32;
-    a.vec = v;
-    a.ukin = reinterpret_cast<const float2*>(d.ukin);
-    a.rot_hi = d.rot_hi;
-    a.rot_lo = d.rot_lo;
-    a.out = out;
-    a.npts = N;
-    a.dpk = dpk;
+    StreamArgs a = vstream_args(h, v, out);
     a.mode = mode;
     a.j = j;
-    a.jdev = d.jdev;
-    a.partials = d.partials;
-    a.scalars = d.scalars;
-    a.hist = d.hist;
-    a.counter = d.counter;
-    a.status = d.status;
-    a.vb16 = d.vb16;
-    a.vscale = d.vscale;
-    a.vformat = h->vformat;
     return launch_vapply_f32(a, t.nn, s);
   }
   return launch_vapply_f64(d.vb64, g, s, t.nn, v, d.ukin, d.rot, out, N, mode, d.partials, d.counter, d.scalars,
@@ -674,6 +656,37 @@ int launch_kinetic(bsl_handle* h, const double* v, const float2* vpair, cudaStre
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+StreamArgs vstream_args(bsl_handle* h, const double* v, double* out) {
+  DeviceState& d = h->d;
+  const Tables& t = h->t;
+  StreamArgs a{};
+  a.vb = d.vb32;
+  a.v32 = d.v32;
+  a.vec = v;
+  a.ukin = reinterpret_cast<const float2*>(d.ukin);
+  a.rot_hi = d.rot_hi;
+  a.rot_lo = d.rot_lo;
+  a.out = out;
+  a.npts = t.npts;
+  a.dpk = t.npts * t.nn;
+  a.mode = 2;
+  a.j = 0;
+  a.jdev = d.jdev;
+  a.partials = d.partials;
+  a.scalars = d.scalars;
+  a.hist = d.hist;
+  a.counter = d.counter;
+  a.status = d.status;
+  a.vb16 = d.vb16;
+  a.vscale = d.vscale;
+  a.vc = d.vc32;
+  a.vformat = h->vformat;
+  a.nn = t.nn;
+  a.red_count = 0;
+  a.ctas_per_sm = h->tune_vs;
+  return a;
+}
+
 int dev_potential_alavi(bsl_handle* h) {
   DeviceState& d = h->d;
   const Tables& t = h->t;
@@ -927,7 +940,7 @@ int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaS
   DeviceState& d = h->d;
   if (h->state_pairs == 1 && h->kinetic_engine == BSL_KIN_TENSOR)  // nothing reads an FP32 copy of v
     return launch_update_stream(reinterpret_cast<const float2*>(V), reinterpret_cast<float2*>(R), L, d.partials,
-                                d.counter, d.scalars, d.hist, d.hist_cap, j, d.jdev, d.status, s);
+                                d.counter, d.scalars, d.hist, d.hist_cap, j, d.jdev, d.status, s, h->tune_upd);
   if (h->state_pairs == 1)
     BSL_CUDA(launch_pdl(k_update_pair, dim3(d.pair_blocks), dim3(kThreads), 0, s, reinterpret_cast<const float2*>(V),
                         reinterpret_cast<float2*>(R), L, h->kinetic_engine == BSL_KIN_TENSOR ? nullptr : d.v32, L - 1,
@@ -1013,6 +1026,8 @@ const char* dev_stage_name(bsl_handle* h, int i) {
   static const char* nmx[4] = {"k_kin_xy_split", "k_kin_z_split", "k_vstream<NN>", "k_update_pair"};
   static const char* ntc[4] = {"k_kin_xy_tc", "k_kin_z_tc", "k_vstream<NN>", "k_update_stream"};
   if (!mixed) return n64[i];
+  if (i == 2 && h->vformat == BSL_VFMT_GAUNT) return "k_vstream<NN,coefficients>";
+  if (i == 2 && h->vformat == BSL_VFMT_BF16) return "k_vstream<NN,bf16>";
   return h->kinetic_engine == BSL_KIN_TENSOR ? ntc[i] : nmx[i];
 }
 

@@ -166,8 +166,11 @@ struct Planes {
   __device__ __forceinline__ int rows() const { return kXY ? ny : nz; }
 };
 
+// The CTA's plane pairs: p_first, p_first + p_stride, ... below p_end (the
+// single-problem launch strides over the grid; a grouped launch gives each CTA
+// one contiguous range of one problem).
 template <bool kXY>
-__device__ __forceinline__ void kin_ws_body(const KinTC& a) {
+__device__ __forceinline__ void kin_ws_body(const KinTC& a, int p_first, int p_stride, int p_end) {
   extern __shared__ uint8_t smraw[];
   uint8_t* sm = align1024(smraw);
   // T tiles: x/y as Z T0 T1 T2 T3 Z (Z = zero tile), z as T0 T1 T2 T3; then
@@ -182,7 +185,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
   __shared__ int prod_go, failed, skip;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const Planes<kXY> pg{a.nx, a.ny, a.nz, a.nplanes};
-  const int npairs = (a.nplanes + 1) / 2;
+  const int npairs = min((a.nplanes + 1) / 2, p_end);
 
   // a kinetic time-out recorded before this launch (an earlier launch of the
   // run, or the host's injection) makes the CTA leave before it allocates
@@ -253,7 +256,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
       for (int u = 0; u < 8; ++u)
         u0[u] = (valid && c0 + u < c_end) ? a.out[ob + (c0 + u) * cstride] : make_float2(0.f, 0.f);
     };
-    for (int it = 0, pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
+    for (int it = 0, pair = p_first; pair < npairs; pair += p_stride, ++it) {
       const int st = it & 1;
       const uint32_t par = (uint32_t)(it >> 1) & 1u;
       const int plane = 2 * pair + p;
@@ -335,9 +338,9 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
     };
     float2 x[kMaxItems][4];
     pdl_wait();  // v is written by the previous iteration's update
-    load_items(2 * (int)blockIdx.x, x);  // in flight during the setup
+    load_items(2 * p_first, x);  // in flight during the setup
     int slot = 0;
-    for (int it = 0, pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
+    for (int it = 0, pair = p_first; pair < npairs; pair += p_stride, ++it) {
       const int st = it & 1;
       const uint32_t par = (uint32_t)(it >> 1) & 1u;
       if (ptid == 0)
@@ -348,7 +351,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
         break;
       }
       {  // the pair after next into L2
-        const int far = 2 * (pair + 2 * (int)gridDim.x);
+        const int far = 2 * (pair + 2 * p_stride);
         prefetch_plane(far);
         prefetch_plane(far + 1);
       }
@@ -356,7 +359,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
 #pragma unroll 1
       for (int pl = 0; pl < 2; ++pl) {
         float2 y[kMaxItems][4];  // the next plane, in flight while this one is sliced
-        load_items(pl == 0 ? 2 * pair + 1 : 2 * (pair + (int)gridDim.x), y);
+        load_items(pl == 0 ? 2 * pair + 1 : 2 * (pair + p_stride), y);
         float mx = 0.f;
 #pragma unroll
         for (int t = 0; t < kMaxItems; ++t)
@@ -398,7 +401,7 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
     // ---- MMA issue ----
     const uint32_t tb = tc::smem_u32(sm);
     if (!tc::mbar_wait(&t_ready, 0u)) failed = 1;
-    for (int it = 0, pair = blockIdx.x; pair < npairs && !failed; pair += gridDim.x, ++it) {
+    for (int it = 0, pair = p_first; pair < npairs && !failed; pair += p_stride, ++it) {
       const int st = it & 1;
       const uint32_t par = (uint32_t)(it >> 1) & 1u;
       if (!tc::mbar_wait(&v_full[st], par) || !tc::mbar_wait(&acc_empty[st], par ^ 1u)) {
@@ -464,10 +467,29 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a) {
 }
 
 // x and y contractions: out(y, x) = (Tx v + Ty v) as double-float pairs
-__global__ void __launch_bounds__(kWsThreads, 1) k_kin_xy_tc(KinTC a) { kin_ws_body<true>(a); }
+__global__ void __launch_bounds__(kWsThreads, 1) k_kin_xy_tc(KinTC a) {
+  kin_ws_body<true>(a, blockIdx.x, gridDim.x, 1 << 30);
+}
 
 // z contraction added into the pairs: out(z, x) += Tz v
-__global__ void __launch_bounds__(kWsThreads, 1) k_kin_z_tc(KinTC a) { kin_ws_body<false>(a); }
+__global__ void __launch_bounds__(kWsThreads, 1) k_kin_z_tc(KinTC a) {
+  kin_ws_body<false>(a, blockIdx.x, gridDim.x, 1 << 30);
+}
+
+// Grouped launch over several problems (each with its own grid, T image and
+// vectors): CTA c works on problem work[c].x, pairs [work[c].y, work[c].z).
+__global__ void __launch_bounds__(kWsThreads, 1) k_kin_xy_tc_group(const KinTC* __restrict__ probs,
+                                                                    const int4* __restrict__ work) {
+  const int4 w = work[blockIdx.x];
+  const KinTC a = probs[w.x];
+  kin_ws_body<true>(a, w.y, 1, w.z);
+}
+__global__ void __launch_bounds__(kWsThreads, 1) k_kin_z_tc_group(const KinTC* __restrict__ probs,
+                                                                   const int4* __restrict__ work) {
+  const int4 w = work[blockIdx.x];
+  const KinTC a = probs[w.x];
+  kin_ws_body<false>(a, w.y, 1, w.z);
+}
 
 constexpr size_t kSmemXY = 1024 + (kTS + 2) * kTile + kStages * kStage;
 constexpr size_t kSmemZ = 1024 + kTS * kTile + kStages * kStage;
@@ -521,23 +543,58 @@ void kinetic_smem_image(const std::vector<double>& T, int n, bool with_zero_tile
 
 bool kinetic_tc_supported(const Tables& t) { return t.nx <= 64 && t.ny <= 64 && t.nz <= 64 && t.tx == t.ty; }
 
-int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
+namespace {
+// the kernel arguments of one problem's x/y (xy = true) or z contraction of v
+KinTC kin_tc_args(bsl_handle* h, const float2* v, bool xy) {
   const Tables& t = h->t;
   DeviceState& d = h->d;
+  if (xy)
+    return KinTC{reinterpret_cast<const uint4*>(d.kxy_slices), (int)((kTS + 2) * kTile / 16), d.e_txy, v,
+                 reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status, h->kin_slices};
+  return KinTC{reinterpret_cast<const uint4*>(d.kz_slices), (int)(kTS * kTile / 16), d.e_tz, v,
+               reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status, h->kin_slices};
+}
+}  // namespace
+
+size_t kin_group_arg_size() { return sizeof(KinTC); }
+
+// the plane pairs of one problem's x/y or z contraction (the work units)
+long long kin_tc_pairs(const bsl_handle* h, bool xy) {
+  const Tables& t = h->t;
+  return ((long long)(xy ? t.nz : t.ny) * t.nn + 1) / 2;
+}
+
+// fill args[b] (kin_group_arg_size() bytes each) for the problems' vectors v[b]
+void kin_tc_group_args(bsl_handle** hs, int n, const float2* const* v, bool xy, void* args) {
+  KinTC* a = static_cast<KinTC*>(args);
+  for (int b = 0; b < n; ++b) a[b] = kin_tc_args(hs[b], v[b], xy);
+}
+
+int launch_kin_tc_group(bool xy, const void* d_args, const int4* d_work, int nctas, cudaStream_t s) {
+  const size_t smem = xy ? kSmemXY : kSmemZ;
+  if (xy) {
+    cudaFuncSetAttribute(k_kin_xy_tc_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    BSL_CUDA(launch_pdl(k_kin_xy_tc_group, dim3(nctas), dim3(kWsThreads), smem, s,
+                        static_cast<const KinTC*>(d_args), d_work));
+  } else {
+    cudaFuncSetAttribute(k_kin_z_tc_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    BSL_CUDA(launch_pdl(k_kin_z_tc_group, dim3(nctas), dim3(kWsThreads), smem, s,
+                        static_cast<const KinTC*>(d_args), d_work));
+  }
+  return BSL_OK;
+}
+
+int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   cudaFuncSetAttribute(k_kin_xy_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemXY);
-  KinTC a{reinterpret_cast<const uint4*>(d.kxy_slices), (int)((kTS + 2) * kTile / 16), d.e_txy, v,
-          reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status, h->kin_slices};
+  const KinTC a = kin_tc_args(h, v, true);
   BSL_CUDA(launch_pdl(k_kin_xy_tc, dim3(std::min((a.nplanes + 1) / 2, sm_count())), dim3(kWsThreads), kSmemXY, s, a));
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }
 
 int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
-  const Tables& t = h->t;
-  DeviceState& d = h->d;
   cudaFuncSetAttribute(k_kin_z_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemZ);
-  KinTC a{reinterpret_cast<const uint4*>(d.kz_slices), (int)(kTS * kTile / 16), d.e_tz, v,
-          reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status, h->kin_slices};
+  const KinTC a = kin_tc_args(h, v, false);
   BSL_CUDA(launch_pdl(k_kin_z_tc, dim3(std::min((a.nplanes + 1) / 2, sm_count())), dim3(kWsThreads), kSmemZ, s, a));
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;

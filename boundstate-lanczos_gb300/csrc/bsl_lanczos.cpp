@@ -13,6 +13,10 @@
 // one fixed unit vector.  That direction is carried as the single extra
 // coordinate (H acts on it as 0), which reproduces the reference's recurrence
 // -- including its spurious eigenvalue at 0 -- with D_packed + 1 unknowns.
+#include <algorithm>
+#include <array>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -161,8 +165,8 @@ constexpr int kGraphIters = 8;
 // runs) unless the cached graph already matches the current configuration
 int ensure_iteration_graph(bsl_handle* h) {
   DeviceState& d = h->d;
-  const long long key[7] = {h->precision, h->kinetic_engine, h->lanczos_flip, (long long)(uintptr_t)d.hist,
-                            d.hist_cap, h->kin_slices, h->vformat};
+  const long long key[9] = {h->precision, h->kinetic_engine, h->lanczos_flip, (long long)(uintptr_t)d.hist,
+                            d.hist_cap, h->kin_slices, h->vformat, h->tune_vs, h->tune_upd};
   if (d.iter_exec && std::memcmp(key, d.graph_key, sizeof(key)) == 0) return BSL_OK;
   release_iteration_graph(d);
   cudaStream_t s = d.stream;
@@ -232,6 +236,191 @@ int run_iterations(bsl_handle** hs, int n, int niter) {
   return BSL_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Grouped batches: the iteration of every problem in one launch per stage.
+// Each stage kernel takes a table of per-problem arguments and a table of
+// per-CTA work (problem, first unit, end unit, block index within the
+// problem); every CTA works on one problem only, so it uses that problem's
+// grid, T image, vectors, scalars and reduction buffers, and each problem's
+// alpha and beta are reduced over its own CTAs.  Four launches advance all the
+// problems by one iteration; kGraphIters of them are captured into one graph.
+// ---------------------------------------------------------------------------
+
+// Split units[b] work units of each problem over about `slots` CTAs in
+// proportion to the units (at least one CTA per problem), each CTA one
+// contiguous range of one problem; ctas[b] receives problem b's CTA count.
+std::vector<int4> split_work(const std::vector<long long>& units, long long slots, std::vector<int>* ctas) {
+  long long total = 0;
+  for (long long u : units) total += u;
+  std::vector<int4> w;
+  ctas->assign(units.size(), 0);
+  for (size_t b = 0; b < units.size(); ++b) {
+    const long long want = std::max(1LL, total > 0 ? slots * units[b] / total : 1LL);
+    const long long per = std::max(1LL, (units[b] + want - 1) / want);
+    int k = 0;
+    for (long long u0 = 0; u0 < units[b]; u0 += per, ++k)
+      w.push_back(make_int4((int)b, (int)u0, (int)std::min(u0 + per, units[b]), k));
+    (*ctas)[b] = k;
+  }
+  return w;
+}
+
+bool groupable(bsl_handle** hs, int n) {
+  if (n < 2) return false;
+  for (int b = 0; b < n; ++b) {
+    const bsl_handle* h = hs[b];
+    if (h->p.device != hs[0]->p.device || h->precision != BSL_PREC_MIXED || h->kinetic_engine != BSL_KIN_TENSOR ||
+        (h->vformat != BSL_VFMT_FP32 && h->vformat != BSL_VFMT_GAUNT) || !vstream_group_supported(h->t.nn))
+      return false;
+  }
+  return true;
+}
+
+struct GroupedBatch {
+  std::vector<bsl_handle*> hs;
+  cudaStream_t s = nullptr;
+  char* mem = nullptr;  // device: argument tables [stage][parity][problem], then the work tables
+  const void* args[4][2] = {};
+  const int4* work[4] = {};
+  int nctas[4] = {0, 0, 0, 0};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~GroupedBatch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (mem) cudaFree(mem);
+  }
+};
+
+int build_grouped(bsl_handle** hs, int n, GroupedBatch* g) {
+  g->hs.assign(hs, hs + n);
+  g->s = hs[0]->d.stream;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, hs[0]->p.device);
+  sms = std::max(1, sms);
+  // stages: 0 kinetic x/y, 1 kinetic z, 2 potential stream, 3 update
+  std::vector<long long> units[4];
+  for (int b = 0; b < n; ++b) {
+    units[0].push_back(kin_tc_pairs(hs[b], true));
+    units[1].push_back(kin_tc_pairs(hs[b], false));
+    units[2].push_back((hs[b]->t.npts + vstream_tile_points() - 1) / vstream_tile_points());
+    units[3].push_back(update_units(bsl_packed_size(hs[b]) + 1));
+  }
+  const int vs = vstream_group_ctas_per_sm();
+  const long long slots[4] = {sms, sms,
+                              (long long)(hs[0]->tune_vs > 0 && hs[0]->tune_vs < vs ? hs[0]->tune_vs : vs) * sms,
+                              (long long)(hs[0]->tune_upd > 0 ? hs[0]->tune_upd : 2) * sms};
+  std::vector<int4> work[4];
+  std::vector<int> ctas[4];
+  for (int k = 0; k < 4; ++k) {
+    work[k] = split_work(units[k], slots[k], &ctas[k]);
+    g->nctas[k] = (int)work[k].size();
+  }
+  const size_t sz[4] = {kin_group_arg_size(), kin_group_arg_size(), vstream_group_arg_size(),
+                        update_group_arg_size()};
+  std::vector<char> host;
+  size_t off_args[4][2], off_work[4];
+  for (int k = 0; k < 4; ++k)
+    for (int p = 0; p < 2; ++p) {
+      off_args[k][p] = host.size();
+      host.resize(host.size() + (sz[k] * n + 255) / 256 * 256);
+    }
+  for (int k = 0; k < 4; ++k) {
+    off_work[k] = host.size();
+    host.resize(host.size() + (work[k].size() * sizeof(int4) + 255) / 256 * 256);
+    std::memcpy(host.data() + off_work[k], work[k].data(), work[k].size() * sizeof(int4));
+  }
+  for (int p = 0; p < 2; ++p) {
+    std::vector<const float2*> V(n);
+    for (int b = 0; b < n; ++b) V[b] = reinterpret_cast<const float2*>(p ? hs[b]->d.rvec : hs[b]->d.vec);
+    kin_tc_group_args(hs, n, V.data(), true, host.data() + off_args[0][p]);
+    kin_tc_group_args(hs, n, V.data(), false, host.data() + off_args[1][p]);
+    for (int b = 0; b < n; ++b) {
+      bsl_handle* h = hs[b];
+      DeviceState& d = h->d;
+      double* Vd = p ? d.rvec : d.vec;
+      double* Rd = p ? d.vec : d.rvec;
+      StreamArgs a = vstream_args(h, Vd, Rd);
+      a.red_count = ctas[2][b];
+      std::memcpy(host.data() + off_args[2][p] + sz[2] * b, &a, sizeof(a));
+      update_group_arg(reinterpret_cast<const float2*>(Vd), reinterpret_cast<float2*>(Rd),
+                       bsl_packed_size(h) + 1, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, d.jdev,
+                       d.status, ctas[3][b], host.data() + off_args[3][p] + sz[3] * b);
+    }
+  }
+  // every problem's reductions need partials for its CTAs
+  for (int b = 0; b < n; ++b)
+    if (std::max(ctas[2][b], ctas[3][b]) > hs[b]->d.red_blocks)
+      return fail(BSL_ERR_UNSUPPORTED, "grouped batch: more CTAs per problem than reduction slots");
+  BSL_CUDA(cudaMalloc(&g->mem, host.size()));
+  BSL_CUDA(cudaMemcpyAsync(g->mem, host.data(), host.size(), cudaMemcpyHostToDevice, g->s));
+  BSL_CUDA(cudaStreamSynchronize(g->s));
+  for (int k = 0; k < 4; ++k) {
+    for (int p = 0; p < 2; ++p) g->args[k][p] = g->mem + off_args[k][p];
+    g->work[k] = reinterpret_cast<const int4*>(g->mem + off_work[k]);
+  }
+  return BSL_OK;
+}
+
+// one iteration of every problem (buffer roles `parity`)
+int grouped_iteration(GroupedBatch* g, int parity) {
+  int rc;
+  if ((rc = launch_kin_tc_group(true, g->args[0][parity], g->work[0], g->nctas[0], g->s)) ||
+      (rc = launch_kin_tc_group(false, g->args[1][parity], g->work[1], g->nctas[1], g->s)) ||
+      (rc = launch_vstream_group(g->args[2][parity], g->work[2], g->nctas[2], g->s)) ||
+      (rc = launch_update_group(g->args[3][parity], g->work[3], g->nctas[3], g->s)))
+    return rc;
+  return BSL_OK;
+}
+
+// niter grouped iterations on the batch stream, timed with the first
+// problem's events; problems' start states are set up on their own streams
+int run_grouped(bsl_handle** hs, int n, int niter) {
+  GroupedBatch g;
+  int rc;
+  if ((rc = build_grouped(hs, n, &g))) return rc;
+  if (niter >= kGraphIters) {
+    BSL_CUDA(cudaStreamBeginCapture(g.s, cudaStreamCaptureModeRelaxed));
+    for (int i = 0; i < kGraphIters && rc == BSL_OK; ++i) rc = grouped_iteration(&g, i & 1);
+    const cudaError_t e = cudaStreamEndCapture(g.s, &g.graph);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture (grouped batch)");
+    BSL_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+    BSL_CUDA(cudaGraphUpload(g.exec, g.s));
+  }
+  // the problems' start vectors and counters are ready before the first launch
+  cudaEvent_t ready;
+  BSL_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  for (int b = 0; b < n; ++b) {
+    if ((rc = dev_set_iteration(hs[b], 1, hs[b]->d.stream))) break;
+    if (b > 0) {
+      cudaEventRecord(ready, hs[b]->d.stream);
+      cudaStreamWaitEvent(g.s, ready, 0);
+    }
+  }
+  cudaEventDestroy(ready);
+  if (rc) return rc;
+  DeviceState& d0 = hs[0]->d;
+  BSL_CUDA(cudaEventRecord(d0.ev0, g.s));
+  const int nblocks = niter / kGraphIters;
+  for (int k = 0; k < nblocks && rc == BSL_OK; ++k) {
+    const cudaError_t e = cudaGraphLaunch(g.exec, g.s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaGraphLaunch (grouped batch)");
+  }
+  for (int j = nblocks * kGraphIters; j < niter && rc == BSL_OK; ++j) rc = grouped_iteration(&g, j & 1);
+  BSL_CUDA(cudaEventRecord(d0.ev1, g.s));
+  const cudaError_t es = cudaStreamSynchronize(g.s);
+  if (rc) return rc;
+  if (es != cudaSuccess) return cuda_fail(es, "grouped batch");
+  float ms = 0.f;
+  BSL_CUDA(cudaEventElapsedTime(&ms, d0.ev0, d0.ev1));
+  for (int b = 0; b < n; ++b) {
+    hs[b]->last_ms_per_iter = ms / niter;
+    hs[b]->lanczos_flip = niter & 1;
+  }
+  return BSL_OK;
+}
+
 }  // namespace
 
 void release_iteration_graph(DeviceState& d) {
@@ -280,8 +469,16 @@ int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed
   return check_status(h);
 }
 
-int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned long long seed, double** alpha,
-                          double** beta, double** beta2) {
+}  // extern "C"
+
+namespace bsl {
+namespace {
+
+// bsl_lanczos_run_batch(_streams): grouped launches when `grouped` and the
+// problems allow them, else blocks of iterations interleaved across the
+// problems' streams
+int run_batch(bsl_handle** hs, int n, int niter, int start, unsigned long long seed, double** alpha, double** beta,
+              double** beta2, bool grouped) {
   if (!hs || n < 1 || niter < 1 || !alpha || !beta || !beta2) return fail(BSL_ERR_INPUT, "bad arguments");
   for (int b = 0; b < n; ++b) {
     if (!hs[b]) return fail(BSL_ERR_STATE, "null handle in the batch");
@@ -294,32 +491,40 @@ int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned
     cudaSetDevice(hs[b]->p.device);
     if ((rc = ensure_hist(hs[b], niter)) || (rc = init_state(hs[b], start, seed))) return rc;
   }
-  // blocks of iterations interleaved across the problems' streams, so the
-  // kernels of different problems overlap
-  if ((rc = prepare_iterations(hs, n, niter))) return rc;
-  for (int b = 0; b < n; ++b) {
-    cudaSetDevice(hs[b]->p.device);
-    BSL_CUDA(cudaEventRecord(hs[b]->d.ev0, hs[b]->d.stream));
+  if (grouped && groupable(hs, n)) {
+    cudaSetDevice(hs[0]->p.device);
+    if ((rc = run_grouped(hs, n, niter))) {
+      for (int b = 0; b < n; ++b) cudaStreamSynchronize(hs[b]->d.stream);
+      return rc;
+    }
+  } else {
+    // blocks of iterations interleaved across the problems' streams, so the
+    // kernels of different problems overlap
+    if ((rc = prepare_iterations(hs, n, niter))) return rc;
+    for (int b = 0; b < n; ++b) {
+      cudaSetDevice(hs[b]->p.device);
+      BSL_CUDA(cudaEventRecord(hs[b]->d.ev0, hs[b]->d.stream));
+    }
+    if ((rc = run_iterations(hs, n, niter))) {
+      for (int b = 0; b < n; ++b) cudaStreamSynchronize(hs[b]->d.stream);
+      return rc;
+    }
+    for (int b = 0; b < n; ++b) {
+      cudaSetDevice(hs[b]->p.device);
+      BSL_CUDA(cudaEventRecord(hs[b]->d.ev1, hs[b]->d.stream));
+    }
+    // the batch's device time: from the first problem's start to the last end
+    // (events of one device compare across streams)
+    float batch_ms = 0.f;
+    for (int b = 0; b < n; ++b) {
+      cudaSetDevice(hs[b]->p.device);
+      BSL_CUDA(cudaEventSynchronize(hs[b]->d.ev1));
+      float ms = 0.f;
+      if (hs[b]->p.device == hs[0]->p.device && cudaEventElapsedTime(&ms, hs[0]->d.ev0, hs[b]->d.ev1) == cudaSuccess)
+        batch_ms = ms > batch_ms ? ms : batch_ms;
+    }
+    for (int b = 0; b < n; ++b) hs[b]->last_ms_per_iter = batch_ms / niter;
   }
-  if ((rc = run_iterations(hs, n, niter))) {
-    for (int b = 0; b < n; ++b) cudaStreamSynchronize(hs[b]->d.stream);
-    return rc;
-  }
-  for (int b = 0; b < n; ++b) {
-    cudaSetDevice(hs[b]->p.device);
-    BSL_CUDA(cudaEventRecord(hs[b]->d.ev1, hs[b]->d.stream));
-  }
-  // the batch's device time: from the first problem's start to the last end
-  // (events of one device compare across streams)
-  float batch_ms = 0.f;
-  for (int b = 0; b < n; ++b) {
-    cudaSetDevice(hs[b]->p.device);
-    BSL_CUDA(cudaEventSynchronize(hs[b]->d.ev1));
-    float ms = 0.f;
-    if (hs[b]->p.device == hs[0]->p.device && cudaEventElapsedTime(&ms, hs[0]->d.ev0, hs[b]->d.ev1) == cudaSuccess)
-      batch_ms = ms > batch_ms ? ms : batch_ms;
-  }
-  for (int b = 0; b < n; ++b) hs[b]->last_ms_per_iter = batch_ms / niter;
   for (int b = 0; b < n; ++b) {
     bsl_handle* h = hs[b];
     cudaSetDevice(h->p.device);
@@ -336,6 +541,77 @@ int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned
     }
     if ((rc = check_status(h))) return rc;
   }
+  return BSL_OK;
+}
+
+}  // namespace
+}  // namespace bsl
+
+extern "C" {
+
+int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned long long seed, double** alpha,
+                          double** beta, double** beta2) {
+  return run_batch(hs, n, niter, start, seed, alpha, beta, beta2, true);
+}
+
+int bsl_lanczos_run_batch_streams(bsl_handle** hs, int n, int niter, int start, unsigned long long seed,
+                                  double** alpha, double** beta, double** beta2) {
+  return run_batch(hs, n, niter, start, seed, alpha, beta, beta2, false);
+}
+
+int bsl_autotune(bsl_handle** hs, int n, int iters, int* vs_per_sm, int* upd_per_sm, double* ms_per_iter) {
+  if (!hs || n < 1 || iters < 8) return fail(BSL_ERR_INPUT, "bad arguments");
+  for (int b = 0; b < n; ++b)
+    if (!hs[b]) return fail(BSL_ERR_STATE, "null handle");
+  // the choice is cached for the same problem set (block sizes, grids, formats)
+  std::string key = std::to_string(n);
+  for (int b = 0; b < n; ++b) {
+    const bsl_handle* h = hs[b];
+    key += "|" + std::to_string(h->t.nn) + ":" + std::to_string(h->t.nx) + "x" + std::to_string(h->t.ny) + "x" +
+           std::to_string(h->t.nz) + ":" + std::to_string(h->precision) + ":" + std::to_string(h->kinetic_engine) +
+           ":" + std::to_string(h->vformat) + ":" + std::to_string(h->kin_slices);
+  }
+  static std::mutex mu;
+  static std::map<std::string, std::array<double, 3>> cache;
+  std::array<double, 3> best = {0, 0, 1e300};
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) best = it->second;
+  }
+  if (best[2] >= 1e300) {
+    const int wv = iters + 1;
+    std::vector<double> a((size_t)n * wv), bb((size_t)n * (wv + 1)), b2((size_t)n * (wv + 1));
+    std::vector<double*> pa(n), pb(n), pb2(n);
+    for (int b = 0; b < n; ++b) {
+      pa[b] = a.data() + (size_t)b * wv;
+      pb[b] = bb.data() + (size_t)b * (wv + 1);
+      pb2[b] = b2.data() + (size_t)b * (wv + 1);
+    }
+    for (int vs = 1; vs <= 3; ++vs)
+      for (int up = 1; up <= 3; ++up) {
+        for (int b = 0; b < n; ++b) {
+          hs[b]->tune_vs = vs;
+          hs[b]->tune_upd = up;
+        }
+        int rc = BSL_OK;
+        for (int rep = 0; rep < 2 && rc == BSL_OK; ++rep)  // the first run captures the graphs
+          rc = n == 1 ? bsl_lanczos_run(hs[0], iters, BSL_START_UNIFORM, 0, pa[0], pb[0], pb2[0])
+                      : run_batch(hs, n, iters, BSL_START_UNIFORM, 0, pa.data(), pb.data(), pb2.data(), true);
+        if (rc) return rc;
+        const double ms = hs[0]->last_ms_per_iter;
+        if (ms < best[2]) best = {(double)vs, (double)up, ms};
+      }
+    std::lock_guard<std::mutex> lock(mu);
+    cache[key] = best;
+  }
+  for (int b = 0; b < n; ++b) {
+    hs[b]->tune_vs = (int)best[0];
+    hs[b]->tune_upd = (int)best[1];
+  }
+  if (vs_per_sm) *vs_per_sm = (int)best[0];
+  if (upd_per_sm) *upd_per_sm = (int)best[1];
+  if (ms_per_iter) *ms_per_iter = best[2];
   return BSL_OK;
 }
 

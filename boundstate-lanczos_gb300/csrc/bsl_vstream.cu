@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "bsl_device.cuh"
+#include "bsl_gaunt.h"
 
 namespace bsl {
 namespace {
@@ -92,13 +93,29 @@ __host__ __device__ constexpr int vstream_load_group(int nn) { return nn >= 21 &
 // Persistent: CTA b owns the contiguous tiles [b * A.tiles_per_cta, ...), and
 // its copy ring runs across tile boundaries, so the next tile's blocks are in
 // flight while the current tile finishes its epilogue.
-// kBF: BF16 blocks (A.vb16) scaled per point by A.vscale, twice the rows per
-// copy so that a copy still moves 8 KiB.
-template <int NN, bool kBF>
-__global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(const StreamArgs A) {
+// Formats (kFmt): 0 FP32 blocks; 1 BF16 blocks (A.vb16) scaled per point by
+// A.vscale, twice the rows per copy so that a copy still moves 8 KiB; 2 FP32
+// spherical-harmonic coefficients (A.vc), from which each thread rebuilds its
+// point's block elements (bsl_gaunt.h).
+template <int NN, int kFmt>
+__host__ __device__ constexpr int rows_per_tile() {
+  if constexpr (kFmt == 2) {
+    return gaunt::Apply<NN>::kNC;
+  } else {
+    return NN * (NN + 1) / 2;
+  }
+}
+
+// The CTA's tiles are [t0, t1); it is block `index` of the `count` blocks that
+// reduce alpha together (the grid for one problem; a problem's blocks in a
+// grouped launch).
+template <int NN, int kFmt>
+__device__ __forceinline__ void vstream_body(const StreamArgs& A, long long t0, long long t1_arg, unsigned int index,
+                                             unsigned int count) {
+  constexpr bool kBF = kFmt == 1;
   using TB = typename std::conditional<kBF, uint16_t, float>::type;
-  constexpr int NT = NN * (NN + 1) / 2;
-  constexpr int kCh = kBF ? 2 * kChunk : kChunk;  // block rows per copy
+  constexpr int NT = rows_per_tile<NN, kFmt>();  // rows streamed per tile
+  constexpr int kCh = kBF ? 2 * kChunk : kChunk;  // rows per copy
   constexpr int NCH = (NT + kCh - 1) / kCh;
   extern __shared__ float4 ring4[];
   TB* ring = reinterpret_cast<TB*>(ring4);  // [kStages][kCh][kTilePts]
@@ -108,10 +125,10 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
   const int tid = threadIdx.x;
   const long long npts = A.npts;
   const long long ntiles = (npts + kTilePts - 1) / kTilePts;
-  const long long t0 = (long long)blockIdx.x * A.tiles_per_cta;
-  const long long t1 = t0 + A.tiles_per_cta < ntiles ? t0 + A.tiles_per_cta : ntiles;
+  const long long t1 = t1_arg < ntiles ? t1_arg : ntiles;
   const long long nchunks = (t1 > t0 ? t1 - t0 : 0) * NCH;
-  const TB* src0 = reinterpret_cast<const TB*>(kBF ? (const void*)A.vb16 : (const void*)A.vb) +
+  const TB* src0 = reinterpret_cast<const TB*>(kFmt == 1 ? (const void*)A.vb16
+                                                : kFmt == 2 ? (const void*)A.vc : (const void*)A.vb) +
                    t0 * (long long)NT * kTilePts;
   const uint64_t pol = evict_first_policy();
   if (tid == 0) {
@@ -174,30 +191,53 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
       }
       va[s] = 0.f;
     }
-    int t = 0;
+    if constexpr (kFmt == 2) {
+      // the point's coefficients, chunk by chunk from the ring, then the block
+      // elements rebuilt and multiplied in registers
+      float cf[NT];
 #pragma unroll
-    for (int s = 0; s < NN; ++s) {
-#pragma unroll
-      for (int q = s; q < NN; ++q, ++t) {
-        const long long g = g0 + t / kCh;
+      for (int k = 0; k < NT; ++k) {
+        const long long g = g0 + k / kCh;
         const int st = (int)(g % kStages);
-        if (t % kCh == 0) {
+        if (k % kCh == 0) {
           if (!abort_flag && !mbar_wait(&full[st], (uint32_t)((g / kStages) & 1))) abort_flag = 1;
         }
-        const TB xr = ring[((size_t)st * kCh + (t % kCh)) * kTilePts + tid];
-        float x;
-        if constexpr (kBF) {
-          x = __uint_as_float((uint32_t)xr << 16);
-        } else {
-          x = xr;
-        }
-        va[s] = fmaf(x, vv[q], va[s]);
-        if (q != s) va[q] = fmaf(x, vv[s], va[q]);
-        if (t % kCh == kCh - 1 || t == NT - 1) {
+        cf[k] = ring[((size_t)st * kCh + (k % kCh)) * kTilePts + tid];
+        if (k % kCh == kCh - 1 || k == NT - 1) {
           __syncthreads();  // every thread is done with this stage
           if (tid == 0 && !abort_flag && g + kStages < nchunks) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(g + kStages);
+          }
+        }
+      }
+      gaunt::Apply<NN>::run(cf, vv, va);
+    } else {
+      int t = 0;
+  #pragma unroll
+      for (int s = 0; s < NN; ++s) {
+  #pragma unroll
+        for (int q = s; q < NN; ++q, ++t) {
+          const long long g = g0 + t / kCh;
+          const int st = (int)(g % kStages);
+          if (t % kCh == 0) {
+            if (!abort_flag && !mbar_wait(&full[st], (uint32_t)((g / kStages) & 1))) abort_flag = 1;
+          }
+          const TB xr = ring[((size_t)st * kCh + (t % kCh)) * kTilePts + tid];
+          float x;
+          if constexpr (kBF) {
+            x = __uint_as_float((uint32_t)xr << 16);
+          } else {
+            x = xr;
+          }
+          va[s] = fmaf(x, vv[q], va[s]);
+          if (q != s) va[q] = fmaf(x, vv[s], va[q]);
+          if (t % kCh == kCh - 1 || t == NT - 1) {
+            __syncthreads();  // every thread is done with this stage
+            if (tid == 0 && !abort_flag && g + kStages < nchunks) {
+              asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+              issue(g + kStages);
+            }
           }
         }
       }
@@ -265,15 +305,15 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
   }
   if (A.mode != 0) {
     // extra coordinate: H acts as 0, R' = R
-    if (blockIdx.x == 0 && tid == 0) {
+    if (index == 0 && tid == 0) {
       if (A.mode == 2)
         dacc = df_fma(Vp[A.dpk], Rp[A.dpk], dacc);
       else
         dot = fma(A.vec[A.dpk], A.out[A.dpk], dot);
     }
     double total;
-    const bool last = A.mode == 2 ? reduce_grid_df(dacc, A.partials, A.counter, &total)
-                                  : reduce_grid(dot, A.partials, A.counter, &total);
+    const bool last = A.mode == 2 ? reduce_group_df(dacc, A.partials, A.counter, count, index, &total)
+                                  : reduce_group(dot, A.partials, A.counter, count, index, &total);
     if (last && threadIdx.x == 0) {
       const double alpha = A.scalars[7] * total;
       A.scalars[0] = alpha;
@@ -283,19 +323,46 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
   }
 }
 
-template <int NN, bool kBF = false>
+template <int NN, int kFmt>
+__global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(const StreamArgs A) {
+  const long long t0 = (long long)blockIdx.x * A.tiles_per_cta;
+  vstream_body<NN, kFmt>(A, t0, t0 + A.tiles_per_cta, blockIdx.x, gridDim.x);
+}
+
+// Grouped launch over problems with blocks of 15 or 21 functions: CTA c streams
+// tiles [work[c].y, work[c].z) of problem work[c].x and is block work[c].w of
+// that problem's alpha reduction (over probs[].red_count blocks).
+__global__ void __launch_bounds__(kTilePts, 3) k_vstream_group(const StreamArgs* __restrict__ probs,
+                                                               const int4* __restrict__ work) {
+  const int4 w = work[blockIdx.x];
+  const StreamArgs A = probs[w.x];
+  if (A.vformat == BSL_VFMT_GAUNT) {
+    if (A.nn == 21)
+      vstream_body<21, 2>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
+    else
+      vstream_body<15, 2>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
+  } else {
+    if (A.nn == 21)
+      vstream_body<21, 0>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
+    else
+      vstream_body<15, 0>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
+  }
+}
+
+template <int NN, int kFmt = 0>
 int launch_nn(StreamArgs a, cudaStream_t s) {
   const size_t smem = (size_t)kStages * kChunk * kTilePts * sizeof(float);
-  cudaFuncSetAttribute(k_vstream<NN, kBF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_vstream<NN, kFmt>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const long long tiles = (a.npts + kTilePts - 1) / kTilePts;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vstream<NN, kBF>, kTilePts, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vstream<NN, kFmt>, kTilePts, smem);
+  if (a.ctas_per_sm > 0 && a.ctas_per_sm < per_sm) per_sm = a.ctas_per_sm;
   const long long slots = (long long)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   a.tiles_per_cta = (tiles + slots - 1) / slots;
   const long long grid = (tiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
-  const cudaError_t e = launch_pdl(k_vstream<NN, kBF>, dim3((unsigned)grid), dim3(kTilePts), smem, s, a);
+  const cudaError_t e = launch_pdl(k_vstream<NN, kFmt>, dim3((unsigned)grid), dim3(kTilePts), smem, s, a);
   return e == cudaSuccess ? BSL_OK : cuda_fail(e, "potential stream launch");
 }
 
@@ -323,18 +390,40 @@ __device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t 
   asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const float4* __restrict__ V4, float4* __restrict__ R4,
-                                                                  long long L, long long units_per_cta,
-                                                                  double* partials, unsigned int* counter,
-                                                                  double* scalars, double* hist, int hist_stride,
-                                                                  int j_arg, int* jdev, int* status) {
+struct UpdArgs {
+  const float4* V4;
+  float4* R4;
+  long long L;
+  double* partials;
+  unsigned int* counter;
+  double* scalars;
+  double* hist;
+  int hist_stride;
+  int* jdev;
+  int* status;
+  int red_count;  // grouped launch: blocks that reduce this problem's beta
+};
+
+// The CTA's 16-byte units are [u0, u1_arg); it is block `index` of the
+// `count` blocks that reduce beta together.
+__device__ __forceinline__ void update_body(const UpdArgs& a, long long u0, long long u1_arg, unsigned int index,
+                                            unsigned int count, int j_arg) {
+  const float4* __restrict__ V4 = a.V4;
+  float4* __restrict__ R4 = a.R4;
+  const long long L = a.L;
+  double* partials = a.partials;
+  unsigned int* counter = a.counter;
+  double* scalars = a.scalars;
+  double* hist = a.hist;
+  const int hist_stride = a.hist_stride;
+  int* jdev = a.jdev;
+  int* status = a.status;
   extern __shared__ float4 upd[];  // [stage][V, R][kUpdUnits]
   __shared__ uint64_t full[kUpdStages];
   __shared__ int failed;
   const int tid = threadIdx.x;
   const long long L2 = L / 2;
-  const long long u0 = (long long)blockIdx.x * units_per_cta;
-  const long long u1 = u0 + units_per_cta < L2 ? u0 + units_per_cta : L2;
+  const long long u1 = u1_arg < L2 ? u1_arg : L2;
   const long long nchunks = u1 > u0 ? (u1 - u0 + kUpdUnits - 1) / kUpdUnits : 0;
   if (tid == 0) {
     for (int s = 0; s < kUpdStages; ++s) mbar_init(&full[s], 1);
@@ -396,7 +485,7 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const float4* 
     }
     asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
-  if ((L & 1) && blockIdx.x == 0 && tid == 0) {  // the coordinate outside the symmetry block
+  if ((L & 1) && index == 0 && tid == 0) {  // the coordinate outside the symmetry block
     const long long i = L - 1;
     const float2* V = reinterpret_cast<const float2*>(V4);
     float2* R = reinterpret_cast<float2*>(R4);
@@ -405,28 +494,82 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const float4* 
     acc = df_add_fast(df_sqr(r), acc);
   }
   double total;
-  if (reduce_grid_df(acc, partials, counter, &total) && tid == 0) {
+  if (reduce_group_df(acc, partials, counter, count, index, &total) && tid == 0) {
     finish_update_pair(total, e, scalars, hist, hist_stride, j, status);
     if (j_arg <= 0) *jdev = j + 1;  // every block has read j before the last one gets here
   }
+}
+
+__global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const UpdArgs a, long long units_per_cta, int j_arg) {
+  const long long u0 = (long long)blockIdx.x * units_per_cta;
+  update_body(a, u0, u0 + units_per_cta, blockIdx.x, gridDim.x, j_arg);
+}
+
+// Grouped launch: CTA c updates units [work[c].y, work[c].z) of problem
+// work[c].x, block work[c].w of that problem's beta reduction; j from the
+// problems' device counters.
+__global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream_group(const UpdArgs* __restrict__ probs,
+                                                                        const int4* __restrict__ work) {
+  const int4 w = work[blockIdx.x];
+  const UpdArgs a = probs[w.x];
+  update_body(a, w.y, w.z, (unsigned)w.w, (unsigned)a.red_count, 0);
 }
 
 }  // namespace
 
 int launch_update_stream(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
                          double* scalars, double* hist, int hist_stride, int j, int* jdev, int* status,
-                         cudaStream_t s) {
+                         cudaStream_t s, int ctas_per_sm) {
   const size_t smem = (size_t)kUpdStages * 2 * kUpdUnits * sizeof(float4);
   cudaFuncSetAttribute(k_update_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long grid = 2LL * (sms > 0 ? sms : 1);
+  const long long grid = (long long)(ctas_per_sm > 0 ? ctas_per_sm : 2) * (sms > 0 ? sms : 1);
   const long long L2 = L / 2;
   const long long per = (L2 + grid - 1) / grid;
-  BSL_CUDA(launch_pdl(k_update_stream, dim3((unsigned)grid), dim3(kUpdThreads), smem, s,
-                      reinterpret_cast<const float4*>(V), reinterpret_cast<float4*>(R), L, per, partials, counter,
-                      scalars, hist, hist_stride, j, jdev, status));
+  const UpdArgs a{reinterpret_cast<const float4*>(V), reinterpret_cast<float4*>(R), L, partials, counter, scalars,
+                  hist, hist_stride, jdev, status, 0};
+  BSL_CUDA(launch_pdl(k_update_stream, dim3((unsigned)grid), dim3(kUpdThreads), smem, s, a, per, j));
+  return BSL_OK;
+}
+
+// ---- grouped launches of the potential stream and the update ---------------
+size_t vstream_group_arg_size() { return sizeof(StreamArgs); }
+size_t update_group_arg_size() { return sizeof(UpdArgs); }
+
+long long update_units(long long L) { return L / 2; }
+
+void update_group_arg(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
+                      double* scalars, double* hist, int hist_stride, int* jdev, int* status, int red_count,
+                      void* out) {
+  *static_cast<UpdArgs*>(out) = UpdArgs{reinterpret_cast<const float4*>(V), reinterpret_cast<float4*>(R), L,
+                                        partials, counter, scalars, hist, hist_stride, jdev, status, red_count};
+}
+
+bool vstream_group_supported(int nn) { return nn == 15 || nn == 21; }
+
+int vstream_group_ctas_per_sm() {
+  const size_t smem = (size_t)kStages * kChunk * kTilePts * sizeof(float);
+  cudaFuncSetAttribute(k_vstream_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vstream_group, kTilePts, smem);
+  return per_sm > 0 ? per_sm : 1;
+}
+
+int launch_vstream_group(const void* d_args, const int4* d_work, int nctas, cudaStream_t s) {
+  const size_t smem = (size_t)kStages * kChunk * kTilePts * sizeof(float);
+  cudaFuncSetAttribute(k_vstream_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  BSL_CUDA(launch_pdl(k_vstream_group, dim3(nctas), dim3(kTilePts), smem, s,
+                      static_cast<const StreamArgs*>(d_args), d_work));
+  return BSL_OK;
+}
+
+int launch_update_group(const void* d_args, const int4* d_work, int nctas, cudaStream_t s) {
+  const size_t smem = (size_t)kUpdStages * 2 * kUpdUnits * sizeof(float4);
+  cudaFuncSetAttribute(k_update_stream_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  BSL_CUDA(launch_pdl(k_update_stream_group, dim3(nctas), dim3(kUpdThreads), smem, s,
+                      static_cast<const UpdArgs*>(d_args), d_work));
   return BSL_OK;
 }
 
@@ -452,9 +595,15 @@ __global__ void k_blocks_bf16(const double* __restrict__ vb64, long long npts, i
 
 int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s) {
   if (a.vformat == BSL_VFMT_BF16) {
-    if (nn == 15) return launch_nn<15, true>(a, s);
-    if (nn == 21) return launch_nn<21, true>(a, s);
+    if (nn == 15) return launch_nn<15, 1>(a, s);
+    if (nn == 21) return launch_nn<21, 1>(a, s);
     return fail(BSL_ERR_UNSUPPORTED, "BF16 potential blocks are built for blocks of 15 and 21 functions");
+  }
+  if (a.vformat == BSL_VFMT_GAUNT) {
+    if (nn == 10) return launch_nn<10, 2>(a, s);
+    if (nn == 15) return launch_nn<15, 2>(a, s);
+    if (nn == 21) return launch_nn<21, 2>(a, s);
+    return fail(BSL_ERR_UNSUPPORTED, "no spherical-harmonic stream for this block size");
   }
 #define BSL_CASE(K)                          \
   case K:                                    \

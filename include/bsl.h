@@ -183,11 +183,25 @@ int bsl_kinetic_engine(const bsl_handle* h);
 int bsl_set_kinetic_slices(bsl_handle* h, int slices);
 
 /* Storage of the potential blocks streamed by BSL_PREC_MIXED. */
-#define BSL_VFMT_FP32 0 /* FP32 (default) */
-#define BSL_VFMT_BF16 1 /* BF16 scaled per grid point by max |block element| (FP32
-                           scale): half the bytes, unit roundoff 2^-9; blocks of
-                           15 and 21 functions */
+#define BSL_VFMT_FP32 0  /* FP32 upper triangles, nn (nn + 1) / 2 values per point */
+#define BSL_VFMT_BF16 1  /* BF16 scaled per grid point by max |block element| (FP32
+                            scale): half the bytes, unit roundoff 2^-9; blocks of
+                            15 and 21 functions */
+#define BSL_VFMT_GAUNT 2 /* FP32 coefficients c_k(p) of real spherical harmonics of
+                            degree <= 2 l_max: every product of two basis functions
+                            is a finite sum of them, so the quadrature blocks are
+                            exactly <s|V|s'>(p) = sum_k G[s s'][k] c_k(p) and the
+                            stream rebuilds them per point (66 values instead of 231
+                            for odd l <= 5, 45 instead of 120 for even l <= 4, 28
+                            instead of 55 for odd l <= 3).  bsl_hv_prep selects it
+                            for those bases when the FP64 blocks reproduce from the
+                            coefficients to 1e-10 of their largest element. */
 int bsl_set_potential_format(bsl_handle* h, int format);
+int bsl_potential_format(const bsl_handle* h);
+
+/* Largest |block element - its spherical-harmonic expansion| of the prepared
+   FP64 blocks (kJ/mol), or -1 when the basis has no generated expansion. */
+double bsl_gaunt_residual(const bsl_handle* h);
 
 /* uec += H vec with host buffers in the reference layout.  Replaces
    Hv_linRotCartSph_NoQuad (linRotCartSphHvFullVPrepRoutines.cpp:807-822):
@@ -208,14 +222,27 @@ int bsl_lanczos_run(bsl_handle* h, int niter, int start, unsigned long long seed
                     double* beta2);
 
 /* bsl_lanczos_run for n independent problems (different cages, symmetry
-   blocks or grids, each prepared by its own bsl_hv_prep) in one call: iteration
-   j of every problem is queued before iteration j + 1 of any, each problem on
-   its own stream, so the kernels of small problems that do not fill the GPU
-   overlap.  alpha[b], beta[b], beta2[b] as in bsl_lanczos_run for problem b;
-   the results are bit-identical to separate bsl_lanczos_run calls.  No
-   counterpart in the reference (one problem per process there). */
+   blocks or grids, each prepared by its own bsl_hv_prep) in one call, as one
+   batch on the first problem's device; alpha[b], beta[b], beta2[b] as in
+   bsl_lanczos_run for problem b.  No counterpart in the reference (one problem
+   per process there).
+   When every problem runs BSL_PREC_MIXED with the tensor-core kinetic, FP32
+   blocks and blocks of 15 or 21 functions, the iteration of all the problems
+   is four grouped launches (kinetic x/y, kinetic z, potential stream, update),
+   each CTA working on one problem in proportion to its size, replayed from a
+   CUDA graph: alpha and beta are reduced over each problem's own CTAs, so they
+   agree with separate runs to rounding, not bit for bit.  Otherwise it runs
+   as bsl_lanczos_run_batch_streams.  bsl_last_run_ms_per_iter reports the
+   device time of one iteration of all the problems. */
 int bsl_lanczos_run_batch(bsl_handle** hs, int n, int niter, int start, unsigned long long seed, double** alpha,
                           double** beta, double** beta2);
+
+/* The same with each problem on its own stream and blocks of iterations
+   interleaved across the streams (iteration j of every problem is queued
+   before iteration j + 1 of any), so the kernels of small problems overlap;
+   the results are bit-identical to separate bsl_lanczos_run calls. */
+int bsl_lanczos_run_batch_streams(bsl_handle** hs, int n, int niter, int start, unsigned long long seed,
+                                  double** alpha, double** beta, double** beta2);
 
 /* One iteration of the reference loop body (lanczosEigenValuesVectors.cpp:191-238)
    with the Lanczos state on the host in the reference layout: on return vec
@@ -344,6 +371,18 @@ int bsl_selftest_tensor_core(double* max_abs_err);
    update + beta, normalise + swap} into ms[0..4]; names[i] (optional) receives
    the kernel name of stage i (static strings). */
 int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names);
+
+/* Launch-shape autotuner, with no counterpart in the reference: times
+   `iters` Lanczos iterations of the problem (n = 1, bsl_lanczos_run) or of the
+   batch (n > 1, bsl_lanczos_run_batch) for each launch shape that the
+   problem's size does not fix -- resident CTAs per SM of the potential stream
+   (1-3, capped by its occupancy) and of the update (1-3) -- and keeps the
+   fastest in the handles for later runs.  The choice is cached per problem
+   set (block sizes, grids, precision, kinetic engine, block format, slices),
+   so a later call with the same sizes reuses it without timing.  Outputs (any
+   may be NULL): the chosen shapes and the best device ms per iteration (of the
+   whole batch for n > 1).  Overwrites the handles' Lanczos state. */
+int bsl_autotune(bsl_handle** hs, int n, int iters, int* vs_per_sm, int* upd_per_sm, double* ms_per_iter);
 
 /* Test hook for the failure paths, with no counterpart in the reference.
    Every bounded wait of the potential-block stream and of the tensor-core

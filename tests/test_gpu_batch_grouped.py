@@ -1,0 +1,82 @@
+"""Batched problems of uneven size in grouped launches (bsl_lanczos_run_batch):
+four launches per iteration of all the problems, each CTA working on one
+problem.  Four generated problems (SPC/E cage seeds 2-5, edges 9-14 points,
+odd l <= 5 with 21 functions and even l <= 4 with 15, 8 theta x 16 phi),
+mixed precision with the tensor-core kinetic, against separate
+bsl_lanczos_run calls with the same start vector:
+
+* the first 10 alpha/beta within 1e-12 of max |alpha| (alpha and beta are
+  reduced over each problem's own CTAs, a different split of the same sums);
+* after 301 iterations (37 graph blocks of 8 and a remainder of 5), every
+  level the separate run has converged (unchanged to 1e-7 kJ/mol over its
+  last 40 iterations, at least 2 per problem) within 1e-6 kJ/mol of a level of
+  the grouped run (the mixed H v's rounding enters through different Krylov
+  vectors: 6e-8 kJ/mol measured);
+* the stream-interleaved batch (bsl_lanczos_run_batch_streams) bit-identical
+  to the separate runs.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_inputs, load_package
+
+pytestmark = pytest.mark.gpu
+CALC = "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE"
+PROBLEMS = [(12, 5, "Odd", 2), (10, 4, "Even", 3), (14, 5, "Odd", 4), (9, 4, "Even", 5)]
+
+
+def make_problems(bsl, tmp):
+    inp = load_inputs()
+    hs = []
+    for k, (n, lmax, sym, seed) in enumerate(PROBLEMS):
+        cage = os.path.join(tmp, "cage%d.xyz" % seed)
+        inp.write_cage_xyz(cage, inp.dodecahedral_cage(seed))
+        hv = os.path.join(tmp, "hv%d.txt" % k)
+        inp.write_hv_input(hv, inp.hv_fields(n, 0.08, lmax, 8, 8, cage, "batch%d" % k, sym))
+        h = bsl.Hamiltonian(hv, CALC, precision="mixed")
+        assert h.kinetic_engine() == "tensor" and h.nn in (15, 21)
+        hs.append(h)
+    return hs
+
+
+def levels(bsl, a, b, b2):
+    ev, _ = bsl.good_eigenvalues(a, b, b2, -10.0, 10.0, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF)
+    return np.sort(ev)
+
+
+def converged_levels(bsl, a, b, b2, drop=40, tol=1e-7):
+    """Levels below 10 kJ/mol that the run without its last `drop` iterations
+    already has to within tol (kJ/mol)."""
+    ev = levels(bsl, a, b, b2)
+    n = len(a) - drop
+    ev2 = levels(bsl, a[:n], b[:n + 1], b2[:n + 1])
+    return np.array([e for e in ev if len(ev2) and np.min(np.abs(ev2 - e)) <= tol])
+
+
+def test_grouped_batch_matches_separate_runs(tmp_path):
+    bsl = load_package()
+    hs = make_problems(bsl, str(tmp_path))
+    try:
+        niter = 301
+        sep = [h.lanczos(niter, start="normal", seed=3) for h in hs]
+        grp = bsl.lanczos_batch(hs, niter, start="normal", seed=3)
+        for (a, b, b2), (ag, bg, b2g) in zip(sep, grp):
+            scale = np.max(np.abs(a))
+            assert np.max(np.abs(a[:10] - ag[:10])) <= 1e-12 * scale
+            assert np.max(np.abs(b[:11] - bg[:11])) <= 1e-12 * scale
+            conv = converged_levels(bsl, a, b, b2)
+            lg = levels(bsl, ag, bg, b2g)
+            assert len(conv) >= 2
+            dev = np.array([np.min(np.abs(lg - e)) for e in conv])
+            assert dev.max() <= 1e-6, (conv, dev)
+        stm = bsl.lanczos_batch(hs, niter, start="normal", seed=3, grouped=False)
+        for (a, b, b2), (ab, bb, b2b) in zip(sep, stm):
+            assert np.array_equal(a, ab) and np.array_equal(b, bb) and np.array_equal(b2, b2b)
+        # a single problem after the batch runs as before (its state and graph are its own)
+        a2, b2_, _ = hs[0].lanczos(niter, start="normal", seed=3)
+        assert np.array_equal(a2, sep[0][0]) and np.array_equal(b2_, sep[0][1])
+    finally:
+        for h in hs:
+            h.close()

@@ -1,8 +1,9 @@
 """Precision variants of the mixed path (bsl_set_kinetic_slices,
 bsl_set_potential_format) on reference fixtures: H v against the FP64 path
-with 1-4 tensor-core kinetic slices and with BF16 potential blocks, the
-default configuration unchanged by a round trip through the variants (the
-cached iteration graph follows every switch), and the refusals."""
+with 1-4 tensor-core kinetic slices, with BF16 potential blocks and with FP32
+blocks instead of the default spherical-harmonic coefficients, the default
+configuration unchanged by a round trip through the variants (the cached
+iteration graph follows every switch), and the refusals."""
 import os
 
 import numpy as np
@@ -35,6 +36,8 @@ def test_kinetic_slices_and_bf16_blocks():
         u64 = np.zeros(h.basis_size)
         h.hv(v, u64)
         h.set_precision("mixed")
+        default_format = h.potential_format()
+        assert default_format == "gaunt" and 0 <= h.gaunt_residual() <= 1e-12
         a0, b0, _ = h.lanczos(40)
         err = {}
         for sl in (1, 2, 3, 4):
@@ -53,6 +56,10 @@ def test_kinetic_slices_and_bf16_blocks():
         assert 1e-5 < eb <= 1e-2, eb
         h.lanczos(24)
         h.set_potential_format("fp32")
+        uf = np.zeros(h.basis_size)
+        h.hv(v, uf)
+        assert rel(uf, u64) <= 1e-7, rel(uf, u64)
+        h.set_potential_format(default_format)
         a1, b1, _ = h.lanczos(40)
         assert np.array_equal(a0, a1) and np.array_equal(b0, b1)
         with pytest.raises(bsl.BslError):
