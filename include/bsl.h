@@ -57,12 +57,18 @@ extern "C" {
 
 /* arithmetic of the Hv application */
 #define BSL_PREC_FP64 0  /* every step in FP64 */
-#define BSL_PREC_MIXED 1 /* FP32 potential blocks, FP32 kinetic with split
-                            coefficients and FP64 combination, FP64 rotor
-                            diagonal and FP64 Lanczos recurrence */
+#define BSL_PREC_MIXED 1 /* FP32 potential values, an FP32 / tensor-core kinetic
+                            exact to ~2^-36 (or FP32 head and tail coefficients
+                            on the CUDA cores), double-float rotor diagonal and
+                            double-float (~48-bit) Lanczos recurrence; grids of
+                            at most 64 points per axis (the kinetic engines) */
 
 /* engine of the FP32 kinetic contractions in BSL_PREC_MIXED */
-#define BSL_KIN_SIMT 0   /* FP32 head/tail coefficients on the CUDA cores */
+#define BSL_KIN_SIMT 0   /* FP32 head/tail coefficients on the CUDA cores; grids of
+                            at most 64 points per axis: one thread owns a 4 x 4
+                            tile of a plane's output and a CTA of at most 256
+                            threads a whole plane, with the next plane held in
+                            16 registers per thread */
 #define BSL_KIN_TENSOR 1 /* fixed-point FP16 slices on the tensor cores
                             (tcgen05.mma), exact FP32 accumulation in tensor
                             memory; grids of at most 64 points per axis with
