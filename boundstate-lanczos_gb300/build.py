@@ -48,10 +48,10 @@ def build(verbose=False, extra_nvcc=()):
         obj = os.path.join(BUILD, f + ".o")
         if f.endswith(".cu"):
             jobs.append([nvcc, "-c", src, "-o", obj] + ARCH +
-                        ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
+                        ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O3,-fvisibility=hidden",
                          "-Xptxas", "-v"] + list(extra_nvcc) + inc)
         elif f.endswith(".cpp"):
-            jobs.append(["g++", "-c", src, "-o", obj, "-O3", "-fPIC", "-std=c++17", "-Wall",
+            jobs.append(["g++", "-c", src, "-o", obj, "-O3", "-fPIC", "-fvisibility=hidden", "-std=c++17", "-Wall",
                          "-I", os.path.join(cuda, "include")] + inc)
     with ThreadPoolExecutor(max_workers=max(2, len(jobs))) as ex:
         logs = list(ex.map(_run, jobs))

@@ -29,6 +29,12 @@
 extern "C" {
 #endif
 
+/* The library is built with hidden symbol visibility; the entry points
+   declared here are its exported interface. */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
 /* status codes */
 #define BSL_OK 0
 #define BSL_ERR_INPUT 1       /* bad or missing input file / parameter */
@@ -414,6 +420,10 @@ long long bsl_vgrid_size(const bsl_handle* h);
 int bsl_copy_vgrid(const bsl_handle* h, double* v1, double* v2);
 long long bsl_vblock_size(const bsl_handle* h);
 int bsl_copy_vblocks(const bsl_handle* h, double* out);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
 
 #ifdef __cplusplus
 }

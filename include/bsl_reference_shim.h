@@ -26,6 +26,10 @@ struct generalStor {
 };
 #endif
 
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
 /* Storage for one of the GB300 HvCalculators, the reference's NoQuad names
    with the suffix "_GB300":
      "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE_GB300"
@@ -51,5 +55,9 @@ void Hv_Prep_linRotCartSph_NoQuad_GB300(int argc, char** argv, generalStor* gene
    buffers of total_basis_size doubles in the reference layout. */
 void Hv_linRotCartSph_NoQuad_GB300(int argc, char** argv, generalStor* general_data, lanczosStor* lanczos_data,
                                    double* vec, double* uec);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
 
 #endif

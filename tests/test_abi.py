@@ -342,7 +342,8 @@ def test_input_writers_round_trip_through_the_parser(bsl, tmp_path):
 def test_every_exported_c_symbol_is_declared(bsl):
     """The library's extern "C" exports are exactly the entry points that
     include/bsl.h declares (no undeclared C API); the three reference-signature
-    functions of include/bsl_reference_shim.h are exported with C++ linkage."""
+    functions of include/bsl_reference_shim.h are exported with C++ linkage,
+    and nothing else (internal helpers have hidden visibility)."""
     import shutil
     import subprocess
     nm = shutil.which("nm")
@@ -353,6 +354,9 @@ def test_every_exported_c_symbol_is_declared(bsl):
     text = [ln.split()[-1] for ln in out.splitlines() if len(ln.split()) == 3 and ln.split()[1] == "T"]
     c_exports = {s for s in text if s.startswith("bsl_")}
     assert c_exports == set(header_functions())
-    cpp = " ".join(s for s in text if s.startswith("_Z"))
+    cpp = [s for s in text if s.startswith("_Z")]
     for name in ("bsl_reference_storage", "Hv_Prep_linRotCartSph_NoQuad_GB300", "Hv_linRotCartSph_NoQuad_GB300"):
-        assert name in cpp, name
+        assert sum(name in s for s in cpp) == 1, name
+    # internal helpers are built with hidden visibility: nothing else is exported
+    assert len(cpp) == 3, cpp
+    assert not [s for s in text if not s.startswith("bsl_") and not s.startswith("_Z")]
