@@ -19,9 +19,15 @@ the reference's Hv and loop on the host cores, bounded sample).  Defaults:
 10,000 timed iterations after 20, so that the timed region (about 1 s) spans
 several 200 ms nvidia-smi clock samples; the working set (145 MB of potential
 blocks) is larger than L2, so no flush is needed between iterations.
+The launch shapes that the problem's size does not fix are picked by the
+library's autotuner before the timed region.
 --impl reference: only the CPU implementation, on the same workload: K
 iterations after W warm-up ones (at most 3), on every host thread, bounded to
 about a minute; rank 0 only.
+--batched: only the batched workload (32 problems of uneven size, 3000
+iterations each, inputs.batch_problems): total iterations/s of the grouped
+batch, of one stream per problem and of one problem after another, and every
+problem's levels against its FP64 run.
 """
 import argparse
 import ctypes as C
