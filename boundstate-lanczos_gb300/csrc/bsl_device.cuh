@@ -264,6 +264,68 @@ __device__ __forceinline__ void finish_update_pair(double total, int e, double* 
 }
 
 // ---------------------------------------------------------------------------
+// Deferred Lanczos reductions (graph-replayed iterations of the double-float
+// path).  Instead of the last CTA of a kernel summing everyone's partial sum
+// while the rest of the GPU idles, the CTAs only store their block totals; the
+// total is formed by a later kernel that runs anyway: alpha by every CTA of
+// the update (each the same fixed-order sum, so all agree), beta by one CTA
+// of the next iteration's x/y kinetic (or a one-CTA kernel after the last
+// iteration).  Layout in the partials buffer: alpha's block totals from
+// index 0, beta's from kBetaPartials; scalars' int slots: the pending flag of
+// a deferred beta and the count of alpha's block totals.
+// ---------------------------------------------------------------------------
+constexpr int kPendingSlot = 24;     // int slot of scalars: 1 while a beta total is deferred
+constexpr int kAlphaCountSlot = 25;  // int slot of scalars: alpha's block totals
+
+// this block's double-float total (all threads call; the value in thread 0)
+__device__ __forceinline__ double block_total_df(float2 part) {
+  __shared__ float2 shb[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2 v = warp_sum_df(part);
+  __syncthreads();
+  if (lane == 0) shb[wid] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  v = (wid == 0 && lane < nw) ? shb[lane] : make_float2(0.f, 0.f);
+  if (wid == 0) v = warp_sum_df(v);
+  return f64_of_df(v);
+}
+
+// sum of parts[0..count) in a fixed order by `nthreads` threads (thread index
+// t) that synchronise on named barrier `bar`; the total in every thread
+__device__ __forceinline__ double sum_partials(const double* parts, int count, int t, int nthreads, int bar,
+                                               double* shared8) {
+  double acc = 0.0;
+  for (int b = t; b < count; b += nthreads) acc += __ldcg(parts + b);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((t & 31) == 0) shared8[t >> 5] = acc;
+  asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthreads) : "memory");
+  double total = 0.0;
+  for (int w = 0; w < nthreads / 32; ++w) total += shared8[w];
+  asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthreads) : "memory");
+  return total;
+}
+
+// The deferred beta of the last update, if one is pending: its block totals
+// summed, then beta, its history and the next scales (finish_update_pair) and
+// the iteration counter advanced.  Called by `nthreads` threads (index t) that
+// synchronise on named barrier `bar`.
+__device__ __forceinline__ void finish_deferred_beta(const double* parts, int count, double* scalars, double* hist,
+                                                     int hist_stride, int* jdev, int* status, int t, int nthreads,
+                                                     int bar, double* shared8) {
+  int* si = reinterpret_cast<int*>(scalars);
+  if (!*(volatile int*)(si + kPendingSlot)) return;  // the same value in every thread
+  const double total = sum_partials(parts, count, t, nthreads, bar, shared8);
+  if (t == 0) {
+    const int j = *jdev;
+    finish_update_pair(total, si[20], scalars, hist, hist_stride, j, status);
+    *jdev = j + 1;
+    si[kPendingSlot] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Programmatic dependent launch: the kernels of the Lanczos iteration are
 // launched with programmatic stream serialization, so a kernel's CTAs may start
 // (and run their prologue) while the previous kernel's last CTAs finish.

@@ -465,8 +465,9 @@ int hv_prep(const bsl_hv_params* params, const Cage* cage, bsl_handle** out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
     d.pair_blocks = 3 * (sms > 0 ? sms : 152);  // 3 resident 256-thread blocks per SM (80 registers)
   }
-  // one partial per block of the widest reducing launch (the per-point potential apply)
-  const size_t nparts = std::max((size_t)d.red_blocks, (N + 63) / 64) + 64;
+  // one partial per block of the widest reducing launch (the per-point potential
+  // apply); deferred beta totals from kBetaPartials on
+  const size_t nparts = std::max({(size_t)d.red_blocks, (N + 63) / 64, (size_t)(kBetaPartials + d.red_blocks)}) + 64;
   if ((rc = dalloc(&d.partials, nparts, "reduction scratch")) ||
       (rc = dalloc(&d.counter, 4, "reduction counter")) || (rc = dalloc(&d.scalars, 16, "scalars")) ||
       (rc = dalloc(&d.status, 4, "status")) || (rc = dalloc(&d.jdev, 1, "iteration counter")))

@@ -164,6 +164,8 @@ struct bsl_handle {
   // launch shapes picked by bsl_autotune (0: the defaults): resident CTAs per SM
   // of the potential stream (capped by its occupancy) and of the update
   int tune_vs = 0, tune_upd = 0;
+  // the iteration being launched defers its reductions (graph-replayed iterations)
+  int defer_reductions = 0;
   double last_ms_per_iter = 0.0;
   int lanczos_flip = 0;           // 0: vec holds v_j and rvec r_j; 1: roles swapped
   int state_pairs = -1;           // Lanczos buffers: 0 FP64, 1 double-float pairs (mixed), -1 not set up
@@ -177,6 +179,8 @@ int dev_potential_alavi(bsl_handle* h);
 int dev_potential_iso(bsl_handle* h);
 int dev_set_iteration(bsl_handle* h, int j, cudaStream_t s);
 bool device_counted_iterations(const bsl_handle* h);
+// after the last device-counted iteration of a run: its deferred beta
+int dev_finish_iterations(bsl_handle* h, cudaStream_t s);
 int dev_potential_point_alavi(bsl_handle* h);
 int dev_potential_coulomb(bsl_handle* h);
 int dev_vblocks(bsl_handle* h);
@@ -215,7 +219,9 @@ int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s);
 // vectors v[b]) and per-CTA work (problem, first pair, end pair, 0)
 size_t kin_group_arg_size();
 long long kin_tc_pairs(const bsl_handle* h, bool xy);
-void kin_tc_group_args(bsl_handle** hs, int n, const float2* const* v, bool xy, void* args);
+// fin_counts (x/y, or null): per problem, the block totals of the deferred beta
+// its first CTA finishes
+void kin_tc_group_args(bsl_handle** hs, int n, const float2* const* v, bool xy, const int* fin_counts, void* args);
 int launch_kin_tc_group(bool xy, const void* d_args, const int4* d_work, int nctas, cudaStream_t s);
 
 // potential-block apply (bsl_vapply_f32.cu / bsl_vapply_f64.cu)
@@ -233,6 +239,7 @@ struct StreamArgs {
   const float* vc;      // BSL_VFMT_GAUNT: tile-major spherical-harmonic coefficients
   int vformat;
   int nn, red_count;    // grouped launch: block size, blocks that reduce this problem's alpha
+  int defer;            // mode 2: store the block totals of alpha only (the update forms alpha)
   int ctas_per_sm;      // 0: as many as fit
   long long npts, dpk;
   long long tiles_per_cta;  // set by the launcher
@@ -247,9 +254,18 @@ long long vstream_tile_points();
 // double-float update R = g (R - alpha c V), beta and the next scales, streamed
 // with bulk copies (V, R 16-byte aligned; partials sized for 2 CTAs per SM)
 // j == 0: the iteration is read from *jdev, which the last block then advances
+// defer: alpha from the stream's block totals, beta's block totals left for
+// the next x/y kinetic or launch_finish_beta (graph-replayed iterations)
 int launch_update_stream(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
                          double* scalars, double* hist, int hist_stride, int j, int* jdev, int* status,
-                         cudaStream_t s, int ctas_per_sm = 0);
+                         cudaStream_t s, int ctas_per_sm = 0, int defer = 0);
+int update_stream_ctas(int ctas_per_sm);
+// index of the first of the deferred beta's block totals in the partials
+// buffer (alpha's block totals start at 0)
+constexpr int kBetaPartials = 2048;
+// the deferred beta after the last iteration of a run (`count` block totals)
+int launch_finish_beta(double* partials, int count, double* scalars, double* hist, int hist_stride, int* jdev,
+                       int* status, cudaStream_t s);
 // grouped launches over several problems: per-problem argument records and
 // per-CTA work (problem, first unit, end unit, block index in the problem's
 // reduction); tiles of vstream_tile_points() points, update units of two

@@ -614,6 +614,7 @@ int launch_vapply(bsl_handle* h, const double* v, double* out, int mode, int j, 
     StreamArgs a = vstream_args(h, v, out);
     a.mode = mode;
     a.j = j;
+    a.defer = mode == 2 ? h->defer_reductions : 0;
     return launch_vapply_f32(a, t.nn, s);
   }
   return launch_vapply_f64(d.vb64, g, s, t.nn, v, d.ukin, d.rot, out, N, mode, d.partials, d.counter, d.scalars,
@@ -940,7 +941,8 @@ int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaS
   DeviceState& d = h->d;
   if (h->state_pairs == 1 && h->kinetic_engine == BSL_KIN_TENSOR)  // nothing reads an FP32 copy of v
     return launch_update_stream(reinterpret_cast<const float2*>(V), reinterpret_cast<float2*>(R), L, d.partials,
-                                d.counter, d.scalars, d.hist, d.hist_cap, j, d.jdev, d.status, s, h->tune_upd);
+                                d.counter, d.scalars, d.hist, d.hist_cap, j, d.jdev, d.status, s, h->tune_upd,
+                                h->defer_reductions);
   if (h->state_pairs == 1)
     BSL_CUDA(launch_pdl(k_update_pair, dim3(d.pair_blocks), dim3(kThreads), 0, s, reinterpret_cast<const float2*>(V),
                         reinterpret_cast<float2*>(R), L, h->kinetic_engine == BSL_KIN_TENSOR ? nullptr : d.v32, L - 1,
@@ -953,12 +955,16 @@ int launch_update(bsl_handle* h, double* V, double* R, long long L, int j, cudaS
 }
 
 namespace {
-__global__ void k_set_int(int* p, int v) { *p = v; }
+__global__ void k_set_iteration(int* jdev, int j, double* scalars) {
+  *jdev = j;
+  reinterpret_cast<int*>(scalars)[kPendingSlot] = 0;
+}
 }  // namespace
 
 // the iteration counter read by the kernels of an iteration launched with j = 0
+// (and no deferred beta pending)
 int dev_set_iteration(bsl_handle* h, int j, cudaStream_t s) {
-  k_set_int<<<1, 1, 0, s>>>(h->d.jdev, j);
+  k_set_iteration<<<1, 1, 0, s>>>(h->d.jdev, j, h->d.scalars);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
 }
@@ -970,22 +976,39 @@ bool device_counted_iterations(const bsl_handle* h) {
   return h->precision == BSL_PREC_MIXED && h->state_pairs == 1 && h->kinetic_engine == BSL_KIN_TENSOR;
 }
 
+// Device-counted iterations (j = 0) defer their reductions: alpha's block
+// totals are summed by the update's CTAs, beta's by the next iteration's x/y
+// kinetic or dev_finish_iterations.
 int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s) {
   DeviceState& d = h->d;
   const long long L = bsl_packed_size(h) + 1;  // + the coordinate outside the symmetry block
   double* V = h->lanczos_flip ? d.rvec : d.vec;
   double* R = h->lanczos_flip ? d.vec : d.rvec;
+  h->defer_reductions = j == 0 && device_counted_iterations(h) ? 1 : 0;
   int rc = launch_kinetic(h, V, reinterpret_cast<const float2*>(V), s);
+  if (!rc) rc = launch_vapply(h, V, R, h->state_pairs == 1 ? 2 : 1, j, s);
+  if (!rc) rc = launch_update(h, V, R, L, j, s);
+  h->defer_reductions = 0;
   if (rc) return rc;
-  if ((rc = launch_vapply(h, V, R, h->state_pairs == 1 ? 2 : 1, j, s))) return rc;
-  if ((rc = launch_update(h, V, R, L, j, s))) return rc;
   h->lanczos_flip ^= 1;
   return BSL_OK;
+}
+
+// the beta left pending by the last device-counted iteration
+int dev_finish_iterations(bsl_handle* h, cudaStream_t s) {
+  DeviceState& d = h->d;
+  return launch_finish_beta(d.partials, update_stream_ctas(h->tune_upd), d.scalars, d.hist, d.hist_cap, d.jdev,
+                            d.status, s);
 }
 
 // The same iteration with an event recorded after every kernel (ev[0] before).
 int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_t* ev) {
   DeviceState& d = h->d;
+  struct Reset {
+    bsl_handle* h;
+    ~Reset() { h->defer_reductions = 0; }
+  } reset{h};
+  h->defer_reductions = j == 0 && device_counted_iterations(h) ? 1 : 0;
   const Tables& t = h->t;
   const long long L = bsl_packed_size(h) + 1;
   const bool mixed = h->precision == BSL_PREC_MIXED;

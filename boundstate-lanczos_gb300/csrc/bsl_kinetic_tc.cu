@@ -80,6 +80,13 @@ struct KinTC {
   int nx, ny, nz, nplanes;
   int* status;
   int nslices;              // slices of v and of T kept (1-4; 4 = exact), classes k + l < nslices
+  // x/y of a graph-replayed iteration: the first CTA's epilogue warps finish
+  // the previous update's deferred beta (null: nothing deferred)
+  double* fin_partials;
+  double* scalars;
+  double* hist;
+  int* jdev;
+  int fin_count, hist_stride;
 };
 
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
@@ -250,6 +257,11 @@ __device__ __forceinline__ void kin_ws_body(const KinTC& a, int p_first, int p_s
       tc::mbar_arrive(&t_ready);
     }
     pdl_wait();  // the output (and, for z, the values added to) belong to earlier kernels
+    if (kXY && a.fin_partials && p_first == 0) {
+      __shared__ double fin8[kEpiWarps];
+      finish_deferred_beta(a.fin_partials + kBetaPartials, a.fin_count, a.scalars, a.hist, a.hist_stride, a.jdev,
+                           a.status, tid, kEpiThreads, 2, fin8);
+    }
     // z: the values the epilogue adds to, 8 columns of this thread's x
     auto load8 = [&](long long ob, bool valid, int c0, float2 (&u0)[8]) {
 #pragma unroll
@@ -545,14 +557,38 @@ bool kinetic_tc_supported(const Tables& t) { return t.nx <= 64 && t.ny <= 64 && 
 
 namespace {
 // the kernel arguments of one problem's x/y (xy = true) or z contraction of v
-KinTC kin_tc_args(bsl_handle* h, const float2* v, bool xy) {
+// (fin_count > 0: the x/y launch finishes a deferred beta of that many block totals)
+KinTC kin_tc_args(bsl_handle* h, const float2* v, bool xy, int fin_count) {
   const Tables& t = h->t;
   DeviceState& d = h->d;
-  if (xy)
-    return KinTC{reinterpret_cast<const uint4*>(d.kxy_slices), (int)((kTS + 2) * kTile / 16), d.e_txy, v,
-                 reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.nz * t.nn, d.status, h->kin_slices};
-  return KinTC{reinterpret_cast<const uint4*>(d.kz_slices), (int)(kTS * kTile / 16), d.e_tz, v,
-               reinterpret_cast<float2*>(d.ukin), t.nx, t.ny, t.nz, t.ny * t.nn, d.status, h->kin_slices};
+  KinTC a{};
+  a.v = v;
+  a.out = reinterpret_cast<float2*>(d.ukin);
+  a.nx = t.nx;
+  a.ny = t.ny;
+  a.nz = t.nz;
+  a.status = d.status;
+  a.nslices = h->kin_slices;
+  if (xy) {
+    a.timage = reinterpret_cast<const uint4*>(d.kxy_slices);
+    a.timage16 = (int)((kTS + 2) * kTile / 16);
+    a.e_t = d.e_txy;
+    a.nplanes = t.nz * t.nn;
+    if (fin_count > 0) {
+      a.fin_partials = d.partials;
+      a.scalars = d.scalars;
+      a.hist = d.hist;
+      a.jdev = d.jdev;
+      a.fin_count = fin_count;
+      a.hist_stride = d.hist_cap;
+    }
+  } else {
+    a.timage = reinterpret_cast<const uint4*>(d.kz_slices);
+    a.timage16 = (int)(kTS * kTile / 16);
+    a.e_t = d.e_tz;
+    a.nplanes = t.ny * t.nn;
+  }
+  return a;
 }
 }  // namespace
 
@@ -565,9 +601,9 @@ long long kin_tc_pairs(const bsl_handle* h, bool xy) {
 }
 
 // fill args[b] (kin_group_arg_size() bytes each) for the problems' vectors v[b]
-void kin_tc_group_args(bsl_handle** hs, int n, const float2* const* v, bool xy, void* args) {
+void kin_tc_group_args(bsl_handle** hs, int n, const float2* const* v, bool xy, const int* fin_counts, void* args) {
   KinTC* a = static_cast<KinTC*>(args);
-  for (int b = 0; b < n; ++b) a[b] = kin_tc_args(hs[b], v[b], xy);
+  for (int b = 0; b < n; ++b) a[b] = kin_tc_args(hs[b], v[b], xy, fin_counts ? fin_counts[b] : 0);
 }
 
 int launch_kin_tc_group(bool xy, const void* d_args, const int4* d_work, int nctas, cudaStream_t s) {
@@ -586,7 +622,7 @@ int launch_kin_tc_group(bool xy, const void* d_args, const int4* d_work, int nct
 
 int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   cudaFuncSetAttribute(k_kin_xy_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemXY);
-  const KinTC a = kin_tc_args(h, v, true);
+  const KinTC a = kin_tc_args(h, v, true, h->defer_reductions ? update_stream_ctas(h->tune_upd) : 0);
   BSL_CUDA(launch_pdl(k_kin_xy_tc, dim3(std::min((a.nplanes + 1) / 2, sm_count())), dim3(kWsThreads), kSmemXY, s, a));
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;
@@ -594,7 +630,7 @@ int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
 
 int launch_kin_z_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   cudaFuncSetAttribute(k_kin_z_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemZ);
-  const KinTC a = kin_tc_args(h, v, false);
+  const KinTC a = kin_tc_args(h, v, false, 0);
   BSL_CUDA(launch_pdl(k_kin_z_tc, dim3(std::min((a.nplanes + 1) / 2, sm_count())), dim3(kWsThreads), kSmemZ, s, a));
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;

@@ -233,6 +233,11 @@ int run_iterations(bsl_handle** hs, int n, int niter) {
       cudaSetDevice(hs[b]->p.device);
       if ((rc = dev_lanczos_iteration(hs[b], counted[b] ? 0 : j, hs[b]->d.stream))) return rc;
     }
+  for (int b = 0; b < n; ++b)
+    if (counted[b]) {
+      cudaSetDevice(hs[b]->p.device);
+      if ((rc = dev_finish_iterations(hs[b], hs[b]->d.stream))) return rc;
+    }
   return BSL_OK;
 }
 
@@ -283,6 +288,7 @@ struct GroupedBatch {
   const void* args[4][2] = {};
   const int4* work[4] = {};
   int nctas[4] = {0, 0, 0, 0};
+  std::vector<int> upd_ctas;  // per problem: the update's CTAs (block totals of its deferred beta)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   ~GroupedBatch() {
@@ -333,8 +339,8 @@ int build_grouped(bsl_handle** hs, int n, GroupedBatch* g) {
   for (int p = 0; p < 2; ++p) {
     std::vector<const float2*> V(n);
     for (int b = 0; b < n; ++b) V[b] = reinterpret_cast<const float2*>(p ? hs[b]->d.rvec : hs[b]->d.vec);
-    kin_tc_group_args(hs, n, V.data(), true, host.data() + off_args[0][p]);
-    kin_tc_group_args(hs, n, V.data(), false, host.data() + off_args[1][p]);
+    kin_tc_group_args(hs, n, V.data(), true, ctas[3].data(), host.data() + off_args[0][p]);
+    kin_tc_group_args(hs, n, V.data(), false, nullptr, host.data() + off_args[1][p]);
     for (int b = 0; b < n; ++b) {
       bsl_handle* h = hs[b];
       DeviceState& d = h->d;
@@ -342,6 +348,7 @@ int build_grouped(bsl_handle** hs, int n, GroupedBatch* g) {
       double* Rd = p ? d.vec : d.rvec;
       StreamArgs a = vstream_args(h, Vd, Rd);
       a.red_count = ctas[2][b];
+      a.defer = 1;
       std::memcpy(host.data() + off_args[2][p] + sz[2] * b, &a, sizeof(a));
       update_group_arg(reinterpret_cast<const float2*>(Vd), reinterpret_cast<float2*>(Rd),
                        bsl_packed_size(h) + 1, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, d.jdev,
@@ -352,6 +359,7 @@ int build_grouped(bsl_handle** hs, int n, GroupedBatch* g) {
   for (int b = 0; b < n; ++b)
     if (std::max(ctas[2][b], ctas[3][b]) > hs[b]->d.red_blocks)
       return fail(BSL_ERR_UNSUPPORTED, "grouped batch: more CTAs per problem than reduction slots");
+  g->upd_ctas = ctas[3];
   BSL_CUDA(cudaMalloc(&g->mem, host.size()));
   BSL_CUDA(cudaMemcpyAsync(g->mem, host.data(), host.size(), cudaMemcpyHostToDevice, g->s));
   BSL_CUDA(cudaStreamSynchronize(g->s));
@@ -408,6 +416,10 @@ int run_grouped(bsl_handle** hs, int n, int niter) {
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaGraphLaunch (grouped batch)");
   }
   for (int j = nblocks * kGraphIters; j < niter && rc == BSL_OK; ++j) rc = grouped_iteration(&g, j & 1);
+  for (int b = 0; b < n && rc == BSL_OK; ++b) {  // the last iteration's deferred betas
+    DeviceState& d = hs[b]->d;
+    rc = launch_finish_beta(d.partials, g.upd_ctas[b], d.scalars, d.hist, d.hist_cap, d.jdev, d.status, g.s);
+  }
   BSL_CUDA(cudaEventRecord(d0.ev1, g.s));
   const cudaError_t es = cudaStreamSynchronize(g.s);
   if (rc) return rc;
@@ -748,8 +760,11 @@ int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names) {
   for (int i = 0; i < 6; ++i) BSL_CUDA(cudaEventCreate(&ev[i]));
   const int nst = 4;
   double acc[5] = {0, 0, 0, 0, 0};
+  // device-counted iterations are timed as they run in a Lanczos run (reductions deferred)
+  const bool counted = device_counted_iterations(h);
+  if (counted && (rc = dev_set_iteration(h, 1, d.stream))) return rc;
   for (int j = 1; j <= iters && !rc; ++j) {
-    rc = dev_lanczos_iteration_timed(h, j, d.stream, ev);
+    rc = dev_lanczos_iteration_timed(h, counted ? 0 : j, d.stream, ev);
     if (rc) break;
     cudaError_t e = cudaEventSynchronize(ev[nst]);
     if (e != cudaSuccess) {
@@ -762,6 +777,7 @@ int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names) {
       acc[i] += x;
     }
   }
+  if (!rc && counted) rc = dev_finish_iterations(h, d.stream);
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   if (rc) return rc;
   for (int i = 0; i < 5; ++i) {

@@ -311,6 +311,14 @@ __device__ __forceinline__ void vstream_body(const StreamArgs& A, long long t0, 
       else
         dot = fma(A.vec[A.dpk], A.out[A.dpk], dot);
     }
+    if (A.defer && A.mode == 2) {  // the update forms alpha from the block totals
+      const double bt = block_total_df(dacc);
+      if (tid == 0) {
+        A.partials[index] = bt;
+        if (index == 0) reinterpret_cast<int*>(A.scalars)[kAlphaCountSlot] = (int)count;
+      }
+      return;
+    }
     double total;
     const bool last = A.mode == 2 ? reduce_group_df(dacc, A.partials, A.counter, count, index, &total)
                                   : reduce_group(dot, A.partials, A.counter, count, index, &total);
@@ -402,6 +410,7 @@ struct UpdArgs {
   int* jdev;
   int* status;
   int red_count;  // grouped launch: blocks that reduce this problem's beta
+  int defer;      // alpha from the stream's block totals here, beta's block totals left for the next kinetic
 };
 
 // The CTA's 16-byte units are [u0, u1_arg); it is block `index` of the
@@ -434,7 +443,6 @@ __device__ __forceinline__ void update_body(const UpdArgs& a, long long u0, long
   pdl_launch_dependents();
   pdl_wait();  // R and alpha come from the potential stream
   const int j = j_arg > 0 ? j_arg : *jdev;
-  const float2 na = reinterpret_cast<const float2*>(scalars)[9];  // -alpha c
   const int e = reinterpret_cast<const int*>(scalars)[20];
   const float g = ldexpf(1.f, e);
   auto chunk_units = [&](long long k) { return (int)(u1 - (u0 + k * kUpdUnits) < kUpdUnits ? u1 - (u0 + k * kUpdUnits) : kUpdUnits); };
@@ -450,6 +458,24 @@ __device__ __forceinline__ void update_body(const UpdArgs& a, long long u0, long
   };
   if (tid == 0)
     for (long long k = 0; k < nchunks && k < kUpdStages; ++k) issue(k);
+  // -alpha c: from the stream's scalars, or (deferred) summed here from its
+  // block totals while the first copies are in flight -- every CTA the same
+  // fixed-order sum
+  float2 na;
+  if (a.defer) {
+    __shared__ double sh8[kUpdThreads / 32];
+    const double total = sum_partials(partials, reinterpret_cast<const int*>(scalars)[kAlphaCountSlot], tid,
+                                      kUpdThreads, 1, sh8);
+    const double alpha = scalars[7] * total;
+    na = df_of(-alpha * scalars[6]);
+    if (index == 0 && tid == 0) {
+      scalars[0] = alpha;
+      hist[j - 1] = alpha;
+      reinterpret_cast<float2*>(scalars)[9] = na;
+    }
+  } else {
+    na = reinterpret_cast<const float2*>(scalars)[9];
+  }
   float2 acc = make_float2(0.f, 0.f);
   for (long long k = 0; k < nchunks; ++k) {
     const int st = (int)(k % kUpdStages);
@@ -493,11 +519,28 @@ __device__ __forceinline__ void update_body(const UpdArgs& a, long long u0, long
     R[i] = r;
     acc = df_add_fast(df_sqr(r), acc);
   }
+  if (a.defer) {  // beta is formed by the next kinetic (or the closing kernel)
+    const double bt = block_total_df(acc);
+    if (tid == 0) {
+      partials[kBetaPartials + index] = bt;
+      if (index == 0) reinterpret_cast<int*>(scalars)[kPendingSlot] = 1;
+    }
+    return;
+  }
   double total;
   if (reduce_group_df(acc, partials, counter, count, index, &total) && tid == 0) {
     finish_update_pair(total, e, scalars, hist, hist_stride, j, status);
     if (j_arg <= 0) *jdev = j + 1;  // every block has read j before the last one gets here
   }
+}
+
+// the deferred beta after the last iteration (one CTA of kUpdThreads threads)
+__global__ void __launch_bounds__(kUpdThreads) k_finish_beta(double* partials, int count, double* scalars,
+                                                             double* hist, int hist_stride, int* jdev, int* status) {
+  __shared__ double sh8[kUpdThreads / 32];
+  pdl_wait();
+  finish_deferred_beta(partials + kBetaPartials, count, scalars, hist, hist_stride, jdev, status, threadIdx.x,
+                       kUpdThreads, 1, sh8);
 }
 
 __global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const UpdArgs a, long long units_per_cta, int j_arg) {
@@ -517,19 +560,23 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream_group(const Up
 
 }  // namespace
 
-int launch_update_stream(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
-                         double* scalars, double* hist, int hist_stride, int j, int* jdev, int* status,
-                         cudaStream_t s, int ctas_per_sm) {
-  const size_t smem = (size_t)kUpdStages * 2 * kUpdUnits * sizeof(float4);
-  cudaFuncSetAttribute(k_update_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+int update_stream_ctas(int ctas_per_sm) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long grid = (long long)(ctas_per_sm > 0 ? ctas_per_sm : 2) * (sms > 0 ? sms : 1);
+  return (ctas_per_sm > 0 ? ctas_per_sm : 2) * (sms > 0 ? sms : 1);
+}
+
+int launch_update_stream(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
+                         double* scalars, double* hist, int hist_stride, int j, int* jdev, int* status,
+                         cudaStream_t s, int ctas_per_sm, int defer) {
+  const size_t smem = (size_t)kUpdStages * 2 * kUpdUnits * sizeof(float4);
+  cudaFuncSetAttribute(k_update_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const long long grid = update_stream_ctas(ctas_per_sm);
   const long long L2 = L / 2;
   const long long per = (L2 + grid - 1) / grid;
   const UpdArgs a{reinterpret_cast<const float4*>(V), reinterpret_cast<float4*>(R), L, partials, counter, scalars,
-                  hist, hist_stride, jdev, status, 0};
+                  hist, hist_stride, jdev, status, 0, defer};
   BSL_CUDA(launch_pdl(k_update_stream, dim3((unsigned)grid), dim3(kUpdThreads), smem, s, a, per, j));
   return BSL_OK;
 }
@@ -544,7 +591,14 @@ void update_group_arg(const float2* V, float2* R, long long L, double* partials,
                       double* scalars, double* hist, int hist_stride, int* jdev, int* status, int red_count,
                       void* out) {
   *static_cast<UpdArgs*>(out) = UpdArgs{reinterpret_cast<const float4*>(V), reinterpret_cast<float4*>(R), L,
-                                        partials, counter, scalars, hist, hist_stride, jdev, status, red_count};
+                                        partials, counter, scalars, hist, hist_stride, jdev, status, red_count, 1};
+}
+
+int launch_finish_beta(double* partials, int count, double* scalars, double* hist, int hist_stride, int* jdev,
+                       int* status, cudaStream_t s) {
+  BSL_CUDA(launch_pdl(k_finish_beta, dim3(1), dim3(kUpdThreads), 0, s, partials, count, scalars, hist, hist_stride,
+                      jdev, status));
+  return BSL_OK;
 }
 
 bool vstream_group_supported(int nn) { return nn == 15 || nn == 21; }
