@@ -267,12 +267,20 @@ def replica_rate(units_per_rank, seconds, world):
     return world * units_per_rank / seconds
 
 
-def stage_bytes(cfg, D, N, nn, mixed, rows=None):
+def stage_bytes(cfg, D, N, nn, mixed, rows=None, names=()):
     """Algorithmic bytes per launch of each stage of one Lanczos iteration;
     `rows` potential values streamed per grid point (default: the upper
-    triangle of the block, nn (nn + 1) / 2)."""
+    triangle of the block, nn (nn + 1) / 2); `names` the stage kernels
+    (bsl_stage_times), which tell the layout of the iteration."""
     ntri = nn * (nn + 1) // 2 if rows is None else rows
     vb = ntri * N * (4 if mixed else 8)
+    if any("k_vapply_light" in n for n in names):
+        # graph-replayed iterations with the fused update: the block product
+        # of the next v (FP32) is formed by the update and read by the apply
+        return [2 * D * 8,          # kinetic x/y: read v, write u_kin
+                3 * D * 8,          # kinetic z: read v, read+write u_kin
+                4 * D * 8 + D * 4,  # light apply: v, u_kin, r (read+write), the product
+                vb + 3 * D * 8 + D * 4]  # update + next product: coefficients, v, r (read+write), product write
     return [2 * D * 8,              # kinetic x/y: read v, write u_kin
             3 * D * 8,              # kinetic z: read v, read+write u_kin
             vb + 4 * D * 8,         # potential apply: blocks, v, u_kin, r (read+write)
@@ -307,8 +315,9 @@ SWEEP = [("V fp32 spherical-harmonic coefficients, kinetic tensor-core 4 slices 
 
 def level_errors(bsl, ref_levels, a, b, b2):
     """Per reference level, the distance (cm^-1) to the nearest level of a run,
-    through the tail with the mixed unit roundoff and with the FP64 one."""
-    evm, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF)
+    through the tail with the mixed path's tolerances and with the FP64 ones."""
+    evm, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF,
+                                  rel_noise=bsl.MIXED_REL_NOISE)
     evr, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3)
     dev = np.array([np.min(np.abs(evm - e)) for e in ref_levels]) * KJ_TO_CM if len(evm) else np.full(
         len(ref_levels), np.inf)
@@ -516,7 +525,7 @@ def main():
     stage_ms = stage_ms[:nst]
     vfmt = h.potential_format()
     rows = {"gaunt": GAUNT_ROWS.get(nn), "fp32": None}.get(vfmt)
-    sb = stage_bytes(cfg, D, N, nn, True, rows)[:nst]
+    sb = stage_bytes(cfg, D, N, nn, True, rows, stage_names)[:nst]
     peak, peak_src = measured_peak_hbm()
     dom = int(np.argmax(stage_ms))
     achieved = sb[dom] / (stage_ms[dom] * 1e-3) / 1e9
@@ -573,8 +582,8 @@ def main():
         if args.dump_lanczos:
             np.savez(args.dump_lanczos, a64=a64, b64=b64, b264=b264, am=am, bm=bm, bm2=bm2)
         ref_levels = np.sort(stable_levels(bsl, a64, b64, b264))[:cfg["levels"]]
-        # the mixed levels through the tail with the mixed path's unit roundoff
-        # (bsl_good_eigenvalues_unit); the reference tail's FP64 tolerance is reported beside
+        # the mixed levels through the tail with the mixed path's tolerances
+        # (bsl_good_eigenvalues_noise); the reference tail's FP64 tolerance is reported beside
         dev, dev_r = level_errors(bsl, ref_levels, am, bm, bm2)
         worst = int(np.argmax(dev)) if len(dev) else -1
         acc = {"iterations": n_it, "levels_compared": int(len(ref_levels)),
@@ -584,7 +593,7 @@ def main():
                "median_abs_dE_cm-1": float(np.median(dev)) if len(dev) else None,
                "worst_level_kJ_mol": float(ref_levels[worst]) if worst >= 0 else None,
                "dE_cm-1_per_level": [float("%.3g" % x) for x in dev],
-               "tail_unit_roundoff_mixed": bsl.MIXED_UNIT_ROUNDOFF,
+               "tail_unit_roundoff_mixed": bsl.MIXED_UNIT_ROUNDOFF, "tail_rel_noise_mixed": bsl.MIXED_REL_NOISE,
                "levels_within_1e-3_cm-1_fp64_tail_tolerance": int(np.sum(dev_r <= 1e-3)),
                "min_level_gap_cm-1": float(np.min(np.diff(ref_levels)) * KJ_TO_CM) if len(ref_levels) > 1 else None,
                "lowest_levels_kJ_mol": [float(x) for x in ref_levels[:5]], "start": "normal seed 0"}

@@ -27,6 +27,7 @@ START = {"uniform": 0, "normal": 1}
 KINETIC = {"simt": 0, "tensor": 1}
 VFORMAT = {"fp32": 0, "bf16": 1, "gaunt": 2}
 MIXED_UNIT_ROUNDOFF = 4.0e-15  # BSL_MIXED_UNIT_ROUNDOFF
+MIXED_REL_NOISE = 1.0e-9  # BSL_MIXED_REL_NOISE
 CALCULATORS = {
     "linRotCartSph_NoQuad_ContGrid_Alavi_SPCE": POT_ALAVI_SPCE,
     "linRotCartSph_NoQuad_IsoHarmOsc": POT_ISOHARMOSC,
@@ -99,6 +100,8 @@ def lib():
     L.bsl_good_eigenvalues.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_int)]
     L.bsl_good_eigenvalues_unit.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, _P, _P,
                                             C.POINTER(C.c_int)]
+    L.bsl_good_eigenvalues_noise.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, C.c_double,
+                                             _P, _P, C.POINTER(C.c_int)]
     L.bsl_write_boundstates.argtypes = [C.c_char_p, C.c_char_p, C.c_int, _P, _P]
     L.bsl_write_tm_vectors.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, _P]
     L.bsl_write_ritz_vectors.argtypes = [C.c_char_p, C.c_char_p, C.c_longlong, C.c_int, _P]
@@ -144,17 +147,24 @@ def parse_hv_input(path):
     return p
 
 
-def good_eigenvalues(alpha, beta, beta2, emin=-10.0, emax=10.0, unit_roundoff=None):
+def good_eigenvalues(alpha, beta, beta2, emin=-10.0, emax=10.0, unit_roundoff=None, rel_noise=None):
     """Cullum-Willoughby good eigenvalues in (emin, emax] and error estimates.
 
     unit_roundoff: None for the reference's FP64 tolerances, else the unit
-    roundoff the multiplicity tolerances are built on (bsl_good_eigenvalues_unit)."""
+    roundoff the multiplicity tolerances are built on (bsl_good_eigenvalues_unit);
+    rel_noise: a floor under the multiplicity window relative to max|T|
+    (bsl_good_eigenvalues_noise).  For runs of the mixed path pass
+    unit_roundoff=MIXED_UNIT_ROUNDOFF, rel_noise=MIXED_REL_NOISE."""
     alpha, beta, beta2 = (np.ascontiguousarray(x, dtype=np.float64) for x in (alpha, beta, beta2))
     niter = len(alpha)
     ev = np.zeros(niter)
     er = np.zeros(niter)
     ng = C.c_int(0)
-    if unit_roundoff is None:
+    if rel_noise is not None:
+        unit = unit_roundoff if unit_roundoff is not None else 2.0 ** -52
+        _check(lib().bsl_good_eigenvalues_noise(niter, _ptr(alpha), _ptr(beta), _ptr(beta2), emin, emax, unit,
+                                                rel_noise, _ptr(ev), _ptr(er), C.byref(ng)))
+    elif unit_roundoff is None:
         _check(lib().bsl_good_eigenvalues(niter, _ptr(alpha), _ptr(beta), _ptr(beta2), emin, emax, _ptr(ev),
                                           _ptr(er), C.byref(ng)))
     else:
@@ -479,8 +489,9 @@ def cage_levels_function():
                                       device=setup.get("device", 0), potential=pot)
             try:
                 a, b, b2 = h.lanczos(niter, start="normal", seed=setup.get("seed", 0))
-                unit = MIXED_UNIT_ROUNDOFF if precision == "mixed" else None
-                ev, _ = good_eigenvalues(a, b, b2, setup.get("emin", -1e3), setup.get("emax", 1e3), unit)
+                mixed = precision == "mixed"
+                ev, _ = good_eigenvalues(a, b, b2, setup.get("emin", -1e3), setup.get("emax", 1e3),
+                                         MIXED_UNIT_ROUNDOFF if mixed else None, MIXED_REL_NOISE if mixed else None)
                 if len(ev) < nlev:
                     raise BslError(ERR_INPUT, "only %d good eigenvalues, %d requested" % (len(ev), nlev))
                 ev = ev[:nlev]

@@ -334,6 +334,7 @@ void free_device(DeviceState& d) {
   if (d.vb16) cudaFree(d.vb16);
   if (d.vscale) cudaFree(d.vscale);
   if (d.vc32) cudaFree(d.vc32);
+  if (d.vprod) cudaFree(d.vprod);
   if (d.copy_done) cudaEventDestroy(d.copy_done);
   if (d.vec_in) cudaEventDestroy(d.vec_in);
   if (d.copy_stream) cudaStreamDestroy(d.copy_stream);
@@ -829,6 +830,15 @@ int bsl_good_eigenvalues_unit(int niter, const double* alpha, const double* beta
   if (niter < 1 || !alpha || !beta || !beta2 || !eval || !err || !ngood || !(unit_roundoff > 0.0))
     return fail(BSL_ERR_INPUT, "bad arguments");
   return cw_good_eigenvalues(niter, alpha, beta, beta2, emin, emax, eval, err, ngood, unit_roundoff);
+}
+
+int bsl_good_eigenvalues_noise(int niter, const double* alpha, const double* beta, const double* beta2,
+                               double emin, double emax, double unit_roundoff, double rel_noise, double* eval,
+                               double* err, int* ngood) {
+  if (niter < 1 || !alpha || !beta || !beta2 || !eval || !err || !ngood || !(unit_roundoff > 0.0) ||
+      !(rel_noise >= 0.0))
+    return fail(BSL_ERR_INPUT, "bad arguments");
+  return cw_good_eigenvalues(niter, alpha, beta, beta2, emin, emax, eval, err, ngood, unit_roundoff, rel_noise);
 }
 
 int bsl_tm_eigenvectors(int niter, const double* alpha, const double* beta, const double* beta2,

@@ -144,6 +144,9 @@ struct DeviceState {
   float* vscale = nullptr;
   // the blocks as spherical-harmonic coefficients, FP32 tile-major [tile][k][128]
   float* vc32 = nullptr;
+  // graph-replayed iterations with the fused update: the potential block
+  // product of the next v, FP32 [s][p] (allocated by prepare_iterations)
+  float* vprod = nullptr;
   // test hook: status words set again after every reset of the status (host-side
   // injection of a kernel time-out; bit 2: potential stream, bit 3: kinetic)
   int inject_status = 0;
@@ -181,6 +184,15 @@ int dev_set_iteration(bsl_handle* h, int j, cudaStream_t s);
 bool device_counted_iterations(const bsl_handle* h);
 // after the last device-counted iteration of a run: its deferred beta
 int dev_finish_iterations(bsl_handle* h, cudaStream_t s);
+// device-counted iterations that use the fused update (and its product buffer)
+bool fused_iterations(const bsl_handle* h);
+// before the first device-counted iteration of a run: the product buffer and,
+// for the fused update, the block product of the current v
+int dev_begin_iterations(bsl_handle* h, cudaStream_t s);
+// the product buffer alone (before an iteration graph is captured)
+int ensure_product_buffer(bsl_handle* h);
+// the block totals of the beta an iteration of h leaves pending
+int deferred_beta_count(bsl_handle* h);
 int dev_potential_point_alavi(bsl_handle* h);
 int dev_potential_coulomb(bsl_handle* h);
 int dev_vblocks(bsl_handle* h);
@@ -196,8 +208,9 @@ int dev_hv_full(bsl_handle* h, const double* full, double* out, cudaStream_t s);
 int dev_full_step_fused(bsl_handle* h, double* v, double* r, long long L, const double* hv, int j, cudaStream_t s,
                         double* v_out = nullptr, double* r_out = nullptr);
 int dev_scatter_full(bsl_handle* h, const double* packed, double* full_accum, cudaStream_t s);
+// previous: the v of the iteration just launched (the buffer roles have flipped)
 int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, int ngood, double* ritz,
-                        cudaStream_t s);
+                        cudaStream_t s, bool previous);
 
 // mixed-precision kinetic (bsl_kinetic.cu)
 void kinetic_split_tables(const std::vector<double>& T, int n, bool transpose, std::vector<float>* head,
@@ -237,6 +250,7 @@ struct StreamArgs {
   const uint16_t* vb16; // BSL_VFMT_BF16: tile-major BF16 blocks, V = vscale[p] * block
   const float* vscale;
   const float* vc;      // BSL_VFMT_GAUNT: tile-major spherical-harmonic coefficients
+  float* vprod;         // fused update: the block product of the next v (FP32 [s][p])
   int vformat;
   int nn, red_count;    // grouped launch: block size, blocks that reduce this problem's alpha
   int defer;            // mode 2: store the block totals of alpha only (the update forms alpha)
@@ -250,6 +264,14 @@ struct StreamArgs {
   int* status;
 };
 int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s);
+// Graph-replayed iterations with the fused update: the light H v apply
+// (R += c H v with the block product from a.vprod; alpha's block totals) and
+// the update fused with the next block product (role 1), or that product
+// alone (role 2, before the first iteration).
+bool fused_update_supported(int vformat, int nn);
+int fused_update_ctas(const StreamArgs& a, int nn);
+int launch_update_fused(const StreamArgs& a, int nn, int role, cudaStream_t s);
+int launch_vapply_light(const StreamArgs& a, int nn, cudaStream_t s);
 long long vstream_tile_points();
 // double-float update R = g (R - alpha c V), beta and the next scales, streamed
 // with bulk copies (V, R 16-byte aligned; partials sized for 2 CTAs per SM)
@@ -299,9 +321,10 @@ int dev_gaunt_coeffs(bsl_handle* h, double* residual, double* vmax);
 void release_iteration_graph(DeviceState& d);
 
 // ---- Cullum-Willoughby tail (bsl_tail.cpp) --------------------------------
-// unit <= 0: the reference's 2^-52
+// unit <= 0: the reference's 2^-52; noise > 0: floor of the multiplicity
+// window relative to max|T|
 int cw_good_eigenvalues(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
-                        double emax, double* eval, double* err, int* ngood, double unit = 0.0);
+                        double emax, double* eval, double* err, int* ngood, double unit = 0.0, double noise = 0.0);
 int cw_tm_eigenvectors(int niter, const double* alpha, const double* beta, const double* beta2,
                        const double* eval, int ngood, double* evtr);
 

@@ -681,6 +681,7 @@ StreamArgs vstream_args(bsl_handle* h, const double* v, double* out) {
   a.vb16 = d.vb16;
   a.vscale = d.vscale;
   a.vc = d.vc32;
+  a.vprod = d.vprod;
   a.vformat = h->vformat;
   a.nn = t.nn;
   a.red_count = 0;
@@ -986,19 +987,58 @@ int dev_lanczos_iteration(bsl_handle* h, int j, cudaStream_t s) {
   double* R = h->lanczos_flip ? d.vec : d.rvec;
   h->defer_reductions = j == 0 && device_counted_iterations(h) ? 1 : 0;
   int rc = launch_kinetic(h, V, reinterpret_cast<const float2*>(V), s);
-  if (!rc) rc = launch_vapply(h, V, R, h->state_pairs == 1 ? 2 : 1, j, s);
-  if (!rc) rc = launch_update(h, V, R, L, j, s);
+  if (h->defer_reductions && fused_iterations(h)) {
+    // the block product of V was formed by the previous update (or
+    // dev_begin_iterations); this update forms the next one
+    StreamArgs a = vstream_args(h, V, R);
+    if (!rc) rc = launch_vapply_light(a, h->t.nn, s);
+    if (!rc) rc = launch_update_fused(a, h->t.nn, 1, s);
+  } else {
+    if (!rc) rc = launch_vapply(h, V, R, h->state_pairs == 1 ? 2 : 1, j, s);
+    if (!rc) rc = launch_update(h, V, R, L, j, s);
+  }
   h->defer_reductions = 0;
   if (rc) return rc;
   h->lanczos_flip ^= 1;
   return BSL_OK;
 }
 
+bool fused_iterations(const bsl_handle* h) {
+  return device_counted_iterations(h) && fused_update_supported(h->vformat, h->t.nn);
+}
+
+int deferred_beta_count(bsl_handle* h) {
+  if (fused_iterations(h)) return fused_update_ctas(vstream_args(h, h->d.vec, h->d.rvec), h->t.nn);
+  return update_stream_ctas(h->tune_upd);
+}
+
+int ensure_product_buffer(bsl_handle* h) {
+  DeviceState& d = h->d;
+  if (!fused_iterations(h) || d.vprod) return BSL_OK;
+  const size_t n = (size_t)h->t.npts * h->t.nn;
+  const cudaError_t e = cudaMalloc(&d.vprod, n * sizeof(float));
+  if (e != cudaSuccess) {
+    d.vprod = nullptr;
+    return fail(BSL_ERR_NOMEM, std::string("block product buffer: ") + cudaGetErrorString(e));
+  }
+  release_iteration_graph(d);  // no captured launch may hold the missing buffer
+  return BSL_OK;
+}
+
+int dev_begin_iterations(bsl_handle* h, cudaStream_t s) {
+  DeviceState& d = h->d;
+  if (!fused_iterations(h)) return BSL_OK;
+  if (int rc = ensure_product_buffer(h)) return rc;
+  double* V = h->lanczos_flip ? d.rvec : d.vec;
+  double* R = h->lanczos_flip ? d.vec : d.rvec;
+  return launch_update_fused(vstream_args(h, V, R), h->t.nn, 2, s);
+}
+
 // the beta left pending by the last device-counted iteration
 int dev_finish_iterations(bsl_handle* h, cudaStream_t s) {
   DeviceState& d = h->d;
-  return launch_finish_beta(d.partials, update_stream_ctas(h->tune_upd), d.scalars, d.hist, d.hist_cap, d.jdev,
-                            d.status, s);
+  return launch_finish_beta(d.partials, deferred_beta_count(h), d.scalars, d.hist, d.hist_cap, d.jdev, d.status,
+                            s);
 }
 
 // The same iteration with an event recorded after every kernel (ev[0] before).
@@ -1034,9 +1074,12 @@ int dev_lanczos_iteration_timed(bsl_handle* h, int j, cudaStream_t s, cudaEvent_
     k_kin_z_f64<<<gz, kThreads, sm_z, s>>>(V, d.ukin, d.tz, t.nx, t.ny, t.nz);
   }
   cudaEventRecord(ev[2], s);
-  if ((rc = launch_vapply(h, V, R, h->state_pairs == 1 ? 2 : 1, j, s))) return rc;
+  const bool fused = h->defer_reductions && fused_iterations(h);
+  const StreamArgs fa = vstream_args(h, V, R);
+  if ((rc = fused ? launch_vapply_light(fa, t.nn, s) : launch_vapply(h, V, R, h->state_pairs == 1 ? 2 : 1, j, s)))
+    return rc;
   cudaEventRecord(ev[3], s);
-  if ((rc = launch_update(h, V, R, L, j, s))) return rc;
+  if ((rc = fused ? launch_update_fused(fa, t.nn, 1, s) : launch_update(h, V, R, L, j, s))) return rc;
   cudaEventRecord(ev[4], s);
   BSL_CUDA(cudaGetLastError());
   h->lanczos_flip ^= 1;
@@ -1049,6 +1092,9 @@ const char* dev_stage_name(bsl_handle* h, int i) {
   static const char* nmx[4] = {"k_kin_xy_split", "k_kin_z_split", "k_vstream<NN>", "k_update_pair"};
   static const char* ntc[4] = {"k_kin_xy_tc", "k_kin_z_tc", "k_vstream<NN>", "k_update_stream"};
   if (!mixed) return n64[i];
+  if (fused_iterations(h) && i >= 2)
+    return i == 2 ? "k_vapply_light<NN>" : h->vformat == BSL_VFMT_GAUNT ? "k_vstream<NN,coefficients,update>"
+                                                                        : "k_vstream<NN,fp32,update>";
   if (i == 2 && h->vformat == BSL_VFMT_GAUNT) return "k_vstream<NN,coefficients>";
   if (i == 2 && h->vformat == BSL_VFMT_BF16) return "k_vstream<NN,bf16>";
   return h->kinetic_engine == BSL_KIN_TENSOR ? ntc[i] : nmx[i];
@@ -1122,9 +1168,9 @@ int dev_full_step_fused(bsl_handle* h, double* v, double* r, long long L, const 
 }
 
 int dev_ritz_accumulate(bsl_handle* h, const double* coef, const int* active, int ngood, double* ritz,
-                        cudaStream_t s) {
+                        cudaStream_t s, bool previous) {
   const long long L = bsl_packed_size(h) + 1;  // with the coordinate outside the symmetry block
-  const double* V = h->lanczos_flip ? h->d.rvec : h->d.vec;
+  const double* V = (h->lanczos_flip ^ (previous ? 1 : 0)) ? h->d.rvec : h->d.vec;
   k_ritz<<<1024, kThreads, 0, s>>>(V, L, coef, active, ngood, ritz, h->d.scalars, h->state_pairs == 1);
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;

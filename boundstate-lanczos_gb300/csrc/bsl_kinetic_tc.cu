@@ -622,7 +622,7 @@ int launch_kin_tc_group(bool xy, const void* d_args, const int4* d_work, int nct
 
 int launch_kin_xy_tc(bsl_handle* h, const float2* v, cudaStream_t s) {
   cudaFuncSetAttribute(k_kin_xy_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemXY);
-  const KinTC a = kin_tc_args(h, v, true, h->defer_reductions ? update_stream_ctas(h->tune_upd) : 0);
+  const KinTC a = kin_tc_args(h, v, true, h->defer_reductions ? deferred_beta_count(h) : 0);
   BSL_CUDA(launch_pdl(k_kin_xy_tc, dim3(std::min((a.nplanes + 1) / 2, sm_count())), dim3(kWsThreads), kSmemXY, s, a));
   BSL_CUDA(cudaGetLastError());
   return BSL_OK;

@@ -200,7 +200,9 @@ int prepare_iterations(bsl_handle** hs, int n, int niter) {
   for (int b = 0; b < n; ++b) {
     bsl_handle* h = hs[b];
     cudaSetDevice(h->p.device);
-    if (device_counted_iterations(h) && niter >= kGraphIters && (rc = ensure_iteration_graph(h))) return rc;
+    if (device_counted_iterations(h) && ((rc = ensure_product_buffer(h)) ||
+                                         (niter >= kGraphIters && (rc = ensure_iteration_graph(h)))))
+      return rc;
   }
   return BSL_OK;
 }
@@ -214,7 +216,8 @@ int run_iterations(bsl_handle** hs, int n, int niter) {
     bsl_handle* h = hs[b];
     cudaSetDevice(h->p.device);
     counted[b] = device_counted_iterations(h) ? 1 : 0;
-    if (counted[b] && (rc = dev_set_iteration(h, 1, h->d.stream))) return rc;
+    if (counted[b] && ((rc = dev_set_iteration(h, 1, h->d.stream)) || (rc = dev_begin_iterations(h, h->d.stream))))
+      return rc;
   }
   const int nblocks = niter / kGraphIters;
   for (int k = 0; k < nblocks; ++k)
@@ -715,13 +718,35 @@ int bsl_ritz_vectors_start(bsl_handle* h, int niter, int start, unsigned long lo
   cudaMemcpyAsync(dcoef, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(dact, active.data(), active.size() * sizeof(int), cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(dritz, 0, (size_t)ngood * L * sizeof(double), s);
+  // The iterations regenerate loop 1's vectors with loop 1's kernels: where
+  // bsl_lanczos_run counts iterations on the device (deferred reductions, the
+  // fused update), v_j and its scale are complete only once iteration j's x/y
+  // kinetic has finished the previous beta, so v_j is taken after iteration j
+  // (it is that iteration's V, unchanged by it).
+  const bool counted = device_counted_iterations(h);
+  if (counted && ((rc = ensure_product_buffer(h)) || (rc = dev_set_iteration(h, 1, s)) ||
+                  (rc = dev_begin_iterations(h, s)))) {
+    cleanup();
+    return rc;
+  }
   for (int j = 1; j <= niter; ++j) {
-    rc = dev_ritz_accumulate(h, dcoef + (size_t)(j - 1) * ngood, dact + (size_t)(j - 1) * ngood, ngood, dritz, s);
-    if (!rc) rc = dev_lanczos_iteration(h, j, s);
+    const double* cj = dcoef + (size_t)(j - 1) * ngood;
+    const int* aj = dact + (size_t)(j - 1) * ngood;
+    if (counted) {
+      rc = dev_lanczos_iteration(h, 0, s);
+      if (!rc) rc = dev_ritz_accumulate(h, cj, aj, ngood, dritz, s, true);
+    } else {
+      rc = dev_ritz_accumulate(h, cj, aj, ngood, dritz, s, false);
+      if (!rc) rc = dev_lanczos_iteration(h, j, s);
+    }
     if (rc) {
       cleanup();
       return rc;
     }
+  }
+  if (counted && (rc = dev_finish_iterations(h, s))) {
+    cleanup();
+    return rc;
   }
   std::vector<double> host((size_t)ngood * L);
   e = cudaMemcpyAsync(host.data(), dritz, host.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -762,7 +787,7 @@ int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names) {
   double acc[5] = {0, 0, 0, 0, 0};
   // device-counted iterations are timed as they run in a Lanczos run (reductions deferred)
   const bool counted = device_counted_iterations(h);
-  if (counted && (rc = dev_set_iteration(h, 1, d.stream))) return rc;
+  if (counted && ((rc = dev_set_iteration(h, 1, d.stream)) || (rc = dev_begin_iterations(h, d.stream)))) return rc;
   for (int j = 1; j <= iters && !rc; ++j) {
     rc = dev_lanczos_iteration_timed(h, counted ? 0 : j, d.stream, ev);
     if (rc) break;

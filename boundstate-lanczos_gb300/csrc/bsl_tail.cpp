@@ -75,13 +75,19 @@ void count_above_backward(const Tri& T, double x, int* all, int* hat) {
 // Distinct eigenvalues in (lo, hi] with multiplicities (0 = spurious).
 // `unit` is the unit roundoff behind the multiplicity tolerances: 2^-52 (kEps)
 // as in BISEC, or the effective unit roundoff of an inexact H v.
-void bisect(const Tri& T, double lo, double hi, double unit, std::vector<double>* vs, std::vector<int>* mp) {
+// `noise` (relative to max|T|, 0 for none) is a floor under the multiplicity
+// window only: copies of a level closer than noise * max|T| count as one
+// (a multiple eigenvalue, good), while an eigenvalue alone in that window is
+// still tested against T without its first row in the window built on `unit`.
+void bisect(const Tri& T, double lo, double hi, double unit, double noise, std::vector<double>* vs,
+            std::vector<int>* mp) {
   const int m = T.m;
   double tkmax = 0.0;
   for (int i = 0; i < m; ++i) tkmax = std::max(std::max(std::fabs(T.a[i]), T.b[i]), tkmax);
   const double ttol = unit * tkmax;
   const double big = double(m + 1000);
   const double ep0 = big * ttol, ep1 = std::sqrt(big) * ttol;
+  const double epm = std::max(ep0, noise * tkmax);  // multiplicity window
   const int above_hi = count_above(T, hi);
   const int mt = count_above(T, lo) - above_hi;
   vs->clear();
@@ -108,21 +114,25 @@ void bisect(const Tri& T, double lo, double hi, double unit, std::vector<double>
     }
     vs->push_back(x);
     int kl, jl, ku, ju;
-    count_above_backward(T, xl - ep0, &kl, &jl);
+    count_above_backward(T, xl - epm, &kl, &jl);
     kl -= above_hi;
     jl -= above_hi;
-    x = xu + ep0;
+    x = xu + epm;
     count_above_backward(T, x, &ku, &ju);
     ku -= above_hi;
     ju -= above_hi;
     int mult, knew;
     if (kl - ku - 1 == 0) {
+      if (epm > ep0) {  // alone in the multiplicity window: the spurious test in the unit window
+        count_above_backward(T, xl - ep0, &kl, &jl);
+        count_above_backward(T, xu + ep0, &ku, &ju);
+      }
       mult = (ju < jl) ? 0 : 1;
       knew = k - 1;
     } else {
       if (ku != nu) {
         while (true) {
-          x = x + ep0;
+          x = x + epm;
           const int c = count_above(T, x) - above_hi;
           const int diff = ku - c;
           ku = c;
@@ -225,8 +235,9 @@ void normalise(std::vector<double>& u, int mev) {
 }  // namespace
 
 int cw_good_eigenvalues(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
-                        double emax, double* eval, double* err, int* ngood, double unit) {
+                        double emax, double* eval, double* err, int* ngood, double unit, double noise) {
   if (!(unit > 0.0)) unit = kEps;
+  if (!(noise > 0.0)) noise = 0.0;
   (void)beta2;  // recomputed from beta, as BISEC does
   Tri T;
   T.a = alpha;
@@ -238,7 +249,7 @@ int cw_good_eigenvalues(int niter, const double* alpha, const double* beta, cons
   for (int i = 0; i <= niter; ++i) T.b2[i] = T.b[i] * T.b[i];
   std::vector<double> vs;
   std::vector<int> mp;
-  bisect(T, emin, emax, unit, &vs, &mp);
+  bisect(T, emin, emax, unit, noise, &vs, &mp);
   flag_isolation(vs, &mp);
   // error estimates for isolated good eigenvalues
   const int nd = (int)vs.size();

@@ -93,6 +93,12 @@ __host__ __device__ constexpr int vstream_load_group(int nn) { return nn >= 21 &
 // Persistent: CTA b owns the contiguous tiles [b * A.tiles_per_cta, ...), and
 // its copy ring runs across tile boundaries, so the next tile's blocks are in
 // flight while the current tile finishes its epilogue.
+// Roles (kRole): 0 the H v apply of the modes above; 1 the Lanczos update of a
+// graph-replayed iteration fused with the next iteration's block product:
+// R = g (R - alpha c V) (alpha from the light apply's block totals, beta's
+// block totals deferred), and A.vprod = V_blocks hi(R), hi(R) being the FP32
+// head of the next v; 2 A.vprod = V_blocks hi(V) only (before the first
+// iteration of a run).
 // Formats (kFmt): 0 FP32 blocks; 1 BF16 blocks (A.vb16) scaled per point by
 // A.vscale, twice the rows per copy so that a copy still moves 8 KiB; 2 FP32
 // spherical-harmonic coefficients (A.vc), from which each thread rebuilds its
@@ -109,7 +115,7 @@ __host__ __device__ constexpr int rows_per_tile() {
 // The CTA's tiles are [t0, t1); it is block `index` of the `count` blocks that
 // reduce alpha together (the grid for one problem; a problem's blocks in a
 // grouped launch).
-template <int NN, int kFmt>
+template <int NN, int kFmt, int kRole = 0>
 __device__ __forceinline__ void vstream_body(const StreamArgs& A, long long t0, long long t1_arg, unsigned int index,
                                              unsigned int count) {
   constexpr bool kBF = kFmt == 1;
@@ -164,11 +170,28 @@ __device__ __forceinline__ void vstream_body(const StreamArgs& A, long long t0, 
   const float2 cc = reinterpret_cast<const float2*>(A.scalars)[8];  // c as a pair (mode 2)
   double dot = 0.0;
   float2 dacc = make_float2(0.f, 0.f);
+  // role 1: -alpha c from the light apply's block totals (every CTA the same
+  // fixed-order sum) and the update's scale g = 2^e
+  float2 na = make_float2(0.f, 0.f);
+  float gs = 1.f;
+  if constexpr (kRole == 1) {
+    __shared__ double sh4[kTilePts / 32];
+    const int* si = reinterpret_cast<const int*>(A.scalars);
+    const double total = sum_partials(A.partials, si[kAlphaCountSlot], tid, kTilePts, 1, sh4);
+    const double alpha = A.scalars[7] * total;
+    na = df_of(-alpha * A.scalars[6]);
+    gs = ldexpf(1.f, si[20]);
+    if (index == 0 && tid == 0) {
+      A.scalars[0] = alpha;
+      A.hist[*A.jdev - 1] = alpha;
+      reinterpret_cast<float2*>(A.scalars)[9] = na;
+    }
+  }
   long long g0 = 0;  // first chunk of the current tile
   for (long long tile = t0; tile < t1; ++tile, g0 += NCH) {
     const long long p = tile * kTilePts + tid;
     const bool valid = p < npts;
-    if (valid) {
+    if (kRole == 0 && valid) {
 #pragma unroll
       for (int s = 0; s < NN; ++s) {
         asm volatile("prefetch.global.L2 [%0];" ::"l"(A.ukin + s * npts + p));
@@ -179,9 +202,37 @@ __device__ __forceinline__ void vstream_body(const StreamArgs& A, long long t0, 
     // mode 2 reads the pair of v once: its head is the FP32 copy (the block
     // product's operand) and its tail is kept for alpha
     float vv[NN], va[NN], vlo[NN];
+    if constexpr (kRole == 1) {
+      // R = g (R - alpha c V) (the arithmetic of the streamed update), stored;
+      // its head is the operand of the next iteration's block product
+      constexpr int kGroup = vstream_load_group(NN);
+#pragma unroll
+      for (int s0 = 0; s0 < NN; s0 += kGroup) {
+        float2 vx[kGroup], rx[kGroup];
+#pragma unroll
+        for (int u = 0; u < kGroup; ++u)
+          if (s0 + u < NN) {
+            vx[u] = valid ? Vp[(s0 + u) * npts + p] : make_float2(0.f, 0.f);
+            rx[u] = valid ? Rp[(s0 + u) * npts + p] : make_float2(0.f, 0.f);
+          }
+#pragma unroll
+        for (int u = 0; u < kGroup; ++u)
+          if (s0 + u < NN) {
+            const float2 r = df_scale2(df_fma_fast(na, vx[u], rx[u]), gs);
+            if (valid) Rp[(s0 + u) * npts + p] = r;
+            dacc = df_add_fast(df_sqr(r), dacc);
+            vv[s0 + u] = r.x;
+            vlo[s0 + u] = 0.f;
+            va[s0 + u] = 0.f;
+          }
+      }
+    } else {
 #pragma unroll
     for (int s = 0; s < NN; ++s) {
-      if (A.mode == 2) {
+      if (kRole == 2) {
+        vv[s] = valid ? Vp[s * npts + p].x : 0.f;
+        vlo[s] = 0.f;
+      } else if (A.mode == 2) {
         const float2 x = valid ? Vp[s * npts + p] : make_float2(0.f, 0.f);
         vv[s] = x.x;
         vlo[s] = x.y;
@@ -190,6 +241,7 @@ __device__ __forceinline__ void vstream_body(const StreamArgs& A, long long t0, 
         vlo[s] = 0.f;
       }
       va[s] = 0.f;
+    }
     }
     if constexpr (kFmt == 2) {
       // the point's coefficients, chunk by chunk from the ring, then the block
@@ -247,6 +299,13 @@ __device__ __forceinline__ void vstream_body(const StreamArgs& A, long long t0, 
 #pragma unroll
       for (int s = 0; s < NN; ++s) va[s] *= sc;
     }
+    if (kRole != 0) {
+      if (valid) {
+#pragma unroll
+        for (int s = 0; s < NN; ++s) A.vprod[s * npts + p] = va[s];
+      }
+      continue;
+    }
     // u = kinetic pair + B l(l+1) v + V v as an FP32 pair.
     // mode 1: the logical vectors are v = sv V and r = sr R; r + H v is kept as
     // sr (R + (sv/sr) H V), so R' = R + c H V and alpha = sv sr (V . R').
@@ -303,7 +362,22 @@ __device__ __forceinline__ void vstream_body(const StreamArgs& A, long long t0, 
     for (long long g = issued - kStages; g < issued; ++g)
       if (g >= 0) mbar_wait(&full[g % kStages], (uint32_t)((g / kStages) & 1));
   }
-  if (A.mode != 0) {
+  if constexpr (kRole == 1) {
+    // the coordinate outside the symmetry block, then beta's block total for
+    // the next x/y kinetic (or the closing kernel)
+    if (index == 0 && tid == 0) {
+      const float2 r = df_scale2(df_fma_fast(na, Vp[A.dpk], Rp[A.dpk]), gs);
+      Rp[A.dpk] = r;
+      dacc = df_add_fast(df_sqr(r), dacc);
+    }
+    const double bt = block_total_df(dacc);
+    if (tid == 0) {
+      A.partials[kBetaPartials + index] = bt;
+      if (index == 0) reinterpret_cast<int*>(A.scalars)[kPendingSlot] = 1;
+    }
+    return;
+  }
+  if (kRole == 0 && A.mode != 0) {
     // extra coordinate: H acts as 0, R' = R
     if (index == 0 && tid == 0) {
       if (A.mode == 2)
@@ -331,10 +405,64 @@ __device__ __forceinline__ void vstream_body(const StreamArgs& A, long long t0, 
   }
 }
 
-template <int NN, int kFmt>
+template <int NN, int kFmt, int kRole = 0>
 __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(const StreamArgs A) {
   const long long t0 = (long long)blockIdx.x * A.tiles_per_cta;
-  vstream_body<NN, kFmt>(A, t0, t0 + A.tiles_per_cta, blockIdx.x, gridDim.x);
+  vstream_body<NN, kFmt, kRole>(A, t0, t0 + A.tiles_per_cta, blockIdx.x, gridDim.x);
+}
+
+// The H v apply of a graph-replayed iteration whose block product was formed
+// by the previous update (A.vprod): R += c (u_kin + B l(l+1) v + V_blocks hi(v))
+// with the arithmetic of the stream's mode 2, one thread per grid point, and
+// alpha's block totals stored for the update.
+constexpr int kLightThreads = 256;
+template <int NN>
+__global__ void __launch_bounds__(kLightThreads) k_vapply_light(const StreamArgs A) {
+  const int tid = threadIdx.x;
+  const long long npts = A.npts;
+  const long long p = (long long)blockIdx.x * kLightThreads + tid;
+  pdl_launch_dependents();
+  pdl_wait();
+  const float2* Vp = reinterpret_cast<const float2*>(A.vec);
+  float2* Rp = reinterpret_cast<float2*>(A.out);
+  const float2 cc = reinterpret_cast<const float2*>(A.scalars)[8];
+  float2 dacc = make_float2(0.f, 0.f);
+  if (p < npts) {
+    constexpr int kGroup = 7;
+#pragma unroll
+    for (int s0 = 0; s0 < NN; s0 += kGroup) {
+      float2 vx[kGroup], uk[kGroup], rr[kGroup];
+      float va[kGroup];
+#pragma unroll
+      for (int u = 0; u < kGroup; ++u)
+        if (s0 + u < NN) {
+          const long long i = (s0 + u) * npts + p;
+          vx[u] = Vp[i];
+          uk[u] = A.ukin[i];
+          rr[u] = Rp[i];
+          va[u] = A.vprod[i];
+        }
+#pragma unroll
+      for (int u = 0; u < kGroup; ++u)
+        if (s0 + u < NN) {
+          const int s = s0 + u;
+          const float a = fmaf(__ldg(A.rot_hi + s), vx[u].x, va[u]);
+          float hi, e, lo;
+          two_sum(uk[u].x, a, hi, e);
+          two_sum(hi, uk[u].y + e + __ldg(A.rot_lo + s) * vx[u].x, hi, lo);
+          const float2 r = df_fma_fast(cc, make_float2(hi, lo), rr[u]);
+          Rp[s * npts + p] = r;
+          dacc = df_fma_fast(vx[u], r, dacc);
+        }
+    }
+  }
+  // extra coordinate: H acts as 0, R' = R
+  if (blockIdx.x == 0 && tid == 0) dacc = df_fma(Vp[A.dpk], Rp[A.dpk], dacc);
+  const double bt = block_total_df(dacc);
+  if (tid == 0) {
+    A.partials[blockIdx.x] = bt;
+    if (blockIdx.x == 0) reinterpret_cast<int*>(A.scalars)[kAlphaCountSlot] = (int)gridDim.x;
+  }
 }
 
 // Grouped launch over problems with blocks of 15 or 21 functions: CTA c streams
@@ -357,20 +485,27 @@ __global__ void __launch_bounds__(kTilePts, 3) k_vstream_group(const StreamArgs*
   }
 }
 
-template <int NN, int kFmt = 0>
-int launch_nn(StreamArgs a, cudaStream_t s) {
+// the grid of k_vstream<NN, kFmt, kRole> for a (and its tiles per CTA)
+template <int NN, int kFmt, int kRole = 0>
+long long vstream_grid(const StreamArgs& a, long long* tiles_per_cta) {
   const size_t smem = (size_t)kStages * kChunk * kTilePts * sizeof(float);
-  cudaFuncSetAttribute(k_vstream<NN, kFmt>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_vstream<NN, kFmt, kRole>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const long long tiles = (a.npts + kTilePts - 1) / kTilePts;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vstream<NN, kFmt>, kTilePts, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vstream<NN, kFmt, kRole>, kTilePts, smem);
   if (a.ctas_per_sm > 0 && a.ctas_per_sm < per_sm) per_sm = a.ctas_per_sm;
   const long long slots = (long long)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
-  a.tiles_per_cta = (tiles + slots - 1) / slots;
-  const long long grid = (tiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
-  const cudaError_t e = launch_pdl(k_vstream<NN, kFmt>, dim3((unsigned)grid), dim3(kTilePts), smem, s, a);
+  *tiles_per_cta = (tiles + slots - 1) / slots;
+  return (tiles + *tiles_per_cta - 1) / *tiles_per_cta;
+}
+
+template <int NN, int kFmt = 0, int kRole = 0>
+int launch_nn(StreamArgs a, cudaStream_t s) {
+  const size_t smem = (size_t)kStages * kChunk * kTilePts * sizeof(float);
+  const long long grid = vstream_grid<NN, kFmt, kRole>(a, &a.tiles_per_cta);
+  const cudaError_t e = launch_pdl(k_vstream<NN, kFmt, kRole>, dim3((unsigned)grid), dim3(kTilePts), smem, s, a);
   return e == cudaSuccess ? BSL_OK : cuda_fail(e, "potential stream launch");
 }
 
@@ -645,6 +780,70 @@ __global__ void k_blocks_bf16(const double* __restrict__ vb64, long long npts, i
       vb16[base + (long long)t * kTilePts] = *reinterpret_cast<const uint16_t*>(&b);
     }
   }
+}
+
+// ---- the fused update path of graph-replayed iterations --------------------
+// Supported block sizes and formats: the spherical-harmonic coefficients at 10,
+// 15 and 21 functions, FP32 blocks at 15 and 21.
+bool fused_update_supported(int vformat, int nn) {
+  if (vformat == BSL_VFMT_GAUNT) return nn == 10 || nn == 15 || nn == 21;
+  if (vformat == BSL_VFMT_FP32) return nn == 15 || nn == 21;
+  return false;
+}
+
+#define BSL_FUSED_DISPATCH(ROLE, CALL)                                  \
+  if (a.vformat == BSL_VFMT_GAUNT) {                                    \
+    if (nn == 10) return CALL<10, 2, ROLE>(a, s);                             \
+    if (nn == 15) return CALL<15, 2, ROLE>(a, s);                             \
+    if (nn == 21) return CALL<21, 2, ROLE>(a, s);                             \
+  } else if (a.vformat == BSL_VFMT_FP32) {                              \
+    if (nn == 15) return CALL<15, 0, ROLE>(a, s);                             \
+    if (nn == 21) return CALL<21, 0, ROLE>(a, s);                             \
+  }
+
+// CTAs of the fused update (the block totals of its deferred beta)
+int fused_update_ctas(const StreamArgs& a, int nn) {
+  long long tpc = 0;
+#define BSL_GRID(NN_, F_, R_) (int)vstream_grid<NN_, F_, R_>(a, &tpc)
+  if (a.vformat == BSL_VFMT_GAUNT) {
+    if (nn == 10) return BSL_GRID(10, 2, 1);
+    if (nn == 15) return BSL_GRID(15, 2, 1);
+    if (nn == 21) return BSL_GRID(21, 2, 1);
+  } else if (a.vformat == BSL_VFMT_FP32) {
+    if (nn == 15) return BSL_GRID(15, 0, 1);
+    if (nn == 21) return BSL_GRID(21, 0, 1);
+  }
+#undef BSL_GRID
+  return 0;
+}
+
+// role 1: the fused update; role 2: the block product of V alone
+int launch_update_fused(const StreamArgs& a, int nn, int role, cudaStream_t s) {
+  if (!a.vprod) return fail(BSL_ERR_STATE, "fused update: no product buffer");
+  if (role == 1) {
+    if (fused_update_ctas(a, nn) > kBetaPartials) return fail(BSL_ERR_UNSUPPORTED, "fused update: too many CTAs");
+    BSL_FUSED_DISPATCH(1, launch_nn)
+  } else {
+    BSL_FUSED_DISPATCH(2, launch_nn)
+  }
+  return fail(BSL_ERR_UNSUPPORTED, "fused update: unsupported block size or format");
+}
+#undef BSL_FUSED_DISPATCH
+
+int launch_vapply_light(const StreamArgs& a, int nn, cudaStream_t s) {
+  const long long grid = (a.npts + kLightThreads - 1) / kLightThreads;
+  if (grid > kBetaPartials) return fail(BSL_ERR_UNSUPPORTED, "light apply: too many CTAs for the reduction slots");
+  if (!a.vprod) return fail(BSL_ERR_STATE, "light apply: no product buffer");
+  cudaError_t e;
+  if (nn == 10)
+    e = launch_pdl(k_vapply_light<10>, dim3((unsigned)grid), dim3(kLightThreads), 0, s, a);
+  else if (nn == 15)
+    e = launch_pdl(k_vapply_light<15>, dim3((unsigned)grid), dim3(kLightThreads), 0, s, a);
+  else if (nn == 21)
+    e = launch_pdl(k_vapply_light<21>, dim3((unsigned)grid), dim3(kLightThreads), 0, s, a);
+  else
+    return fail(BSL_ERR_UNSUPPORTED, "light apply: unsupported block size");
+  return e == cudaSuccess ? BSL_OK : cuda_fail(e, "light apply launch");
 }
 
 int launch_vapply_f32(const StreamArgs& a, int nn, cudaStream_t s) {

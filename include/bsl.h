@@ -314,6 +314,22 @@ int bsl_good_eigenvalues(int niter, const double* alpha, const double* beta, con
 int bsl_good_eigenvalues_unit(int niter, const double* alpha, const double* beta, const double* beta2, double emin,
                               double emax, double unit_roundoff, double* eval, double* err, int* ngood);
 
+/* The same with a floor under the multiplicity window: eigenvalues of T_m
+   closer than max((niter + 1000) * unit_roundoff, rel_noise) * max|T| count as
+   one multiple (good) eigenvalue; an eigenvalue alone in that window is tested
+   against T without its first row in the window built on unit_roundoff, as in
+   bsl_good_eigenvalues_unit.  The copies of a converged level that an inexact
+   H v produces scatter by about the relative error of H v times max|T|
+   however long the run, while the window built on a unit roundoff grows with
+   niter; in short runs it can be narrower than the scatter, every copy then
+   looks simple and each sits next to a copy in T without its first row, so
+   the level is lost as spurious.  BSL_MIXED_REL_NOISE is the floor for
+   BSL_PREC_MIXED (rel_noise = 0: bsl_good_eigenvalues_unit). */
+#define BSL_MIXED_REL_NOISE 1.0e-9
+int bsl_good_eigenvalues_noise(int niter, const double* alpha, const double* beta, const double* beta2,
+                               double emin, double emax, double unit_roundoff, double rel_noise, double* eval,
+                               double* err, int* ngood);
+
 /* Tm eigenvectors for the first ngood good eigenvalues (lanczosvectors +
    TRIVEC, lanczosEigenValuesVectors.cpp:509-561): evtr is column-major
    [niter x ngood]. */

@@ -45,7 +45,8 @@ def make_problems(bsl, tmp):
 
 
 def levels(bsl, a, b, b2):
-    ev, _ = bsl.good_eigenvalues(a, b, b2, -10.0, 10.0, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF)
+    ev, _ = bsl.good_eigenvalues(a, b, b2, -10.0, 10.0, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF,
+                                rel_noise=bsl.MIXED_REL_NOISE)
     return np.sort(ev)
 
 

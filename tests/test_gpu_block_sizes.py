@@ -79,7 +79,8 @@ def check_case(bsl, hv, engines, niter):
             assert np.max(np.abs(am[:6] - a[:6])) <= 1e-6 * scale, engine
             assert np.max(np.abs(bm[1:7] - b[1:7])) <= 1e-6 * scale, engine
             if low is not None:
-                evm, _ = bsl.good_eigenvalues(am, bm, bm2, -10.0, 40.0, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF)
+                evm, _ = bsl.good_eigenvalues(am, bm, bm2, -10.0, 40.0, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF,
+                                               rel_noise=bsl.MIXED_REL_NOISE)
                 dev = np.array([np.min(np.abs(evm - e)) for e in low])
                 assert dev.max() <= CM_TOL_MIXED, (engine, dev.max() * 83.5935)
         return h

@@ -161,7 +161,8 @@ def test_lanczos_mixed_levels_within_1e3_cm(bsl, engine):
     h.set_precision("mixed")
     h.set_kinetic_engine(engine)
     am, bm, bm2 = h.lanczos(niter, start="normal", seed=0)
-    evm, _ = bsl.good_eigenvalues(am, bm, bm2, -10.0, 40.0, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF)
+    evm, _ = bsl.good_eigenvalues(am, bm, bm2, -10.0, 40.0, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF,
+                                  rel_noise=bsl.MIXED_REL_NOISE)
     low = np.sort(stable)[:20]
     assert len(low) >= 8
     dev = np.array([np.min(np.abs(evm - e)) for e in low])
@@ -273,8 +274,9 @@ def test_ritz_vectors_mixed_are_eigenvectors(bsl):
     def ritz_pair(precision):
         h.set_precision(precision)
         a, b, b2 = h.lanczos(niter)
-        unit = bsl.MIXED_UNIT_ROUNDOFF if precision == "mixed" else None
-        ev, _ = bsl.good_eigenvalues(a, b, b2, unit_roundoff=unit)
+        mixed = precision == "mixed"
+        ev, _ = bsl.good_eigenvalues(a, b, b2, unit_roundoff=bsl.MIXED_UNIT_ROUNDOFF if mixed else None,
+                                     rel_noise=bsl.MIXED_REL_NOISE if mixed else None)
         rows = bsl.tm_eigenvectors(a, b, b2, ev[:1])
         x = h.ritz(niter, rows)[0]
         return ev[0], x / np.linalg.norm(x)
