@@ -217,10 +217,14 @@ def measured_peak_hbm():
 
 # DRAM bytes (read + write) per launch of each mixed-path kernel in the running
 # iteration: one-pass ncu capture with the L2 left as the previous kernel left it
-# (profiles/pipeline_traffic_warm_54cubed_odd_l5.md).
+# (the fused iteration of a run; the four-kernel iteration's potential stream
+# and update from the earlier capture).
 _TRAFFIC_SRC = "profiles/pipeline_traffic_warm_54cubed_odd_l5.md"
-NCU_TRAFFIC = {"k_kin_xy_tc": (13.33e6, _TRAFFIC_SRC),
-               "k_kin_z_tc": (3.17e6, _TRAFFIC_SRC),
+_FUSED_SRC = "profiles/fused_iteration_54cubed_odd_l5.md"
+NCU_TRAFFIC = {"k_kin_xy_tc": (17.29e6, _FUSED_SRC),
+               "k_kin_z_tc": (4.34e6, _FUSED_SRC),
+               "k_vapply_light<NN>": (49.85e6, _FUSED_SRC),
+               "k_vstream<NN,coefficients,update>": (68.43e6, _FUSED_SRC),
                "k_vstream<NN,coefficients>": (84.45e6, _TRAFFIC_SRC),
                "k_vstream<NN>": (200.97e6, _TRAFFIC_SRC),
                "k_update_stream": (9.05e6, _TRAFFIC_SRC)}
