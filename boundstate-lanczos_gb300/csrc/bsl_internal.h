@@ -288,20 +288,17 @@ constexpr int kBetaPartials = 2048;
 // the deferred beta after the last iteration of a run (`count` block totals)
 int launch_finish_beta(double* partials, int count, double* scalars, double* hist, int hist_stride, int* jdev,
                        int* status, cudaStream_t s);
-// grouped launches over several problems: per-problem argument records and
-// per-CTA work (problem, first unit, end unit, block index in the problem's
-// reduction); tiles of vstream_tile_points() points, update units of two
-// double-float values
+// grouped launches of the fused iteration over several problems: per-problem
+// argument records (StreamArgs) and per-CTA work (problem, first unit, end
+// unit, block index in the problem's reduction); the light apply in blocks of
+// light_points_per_cta() points (one block per CTA), the fused update in tiles
+// of vstream_tile_points() points
 size_t vstream_group_arg_size();
-size_t update_group_arg_size();
-long long update_units(long long L);
+long long light_points_per_cta();
 bool vstream_group_supported(int nn);
 int vstream_group_ctas_per_sm();
-void update_group_arg(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
-                      double* scalars, double* hist, int hist_stride, int* jdev, int* status, int red_count,
-                      void* out);
+int launch_light_group(const void* d_args, const int4* d_work, int nctas, cudaStream_t s);
 int launch_vstream_group(const void* d_args, const int4* d_work, int nctas, cudaStream_t s);
-int launch_update_group(const void* d_args, const int4* d_work, int nctas, cudaStream_t s);
 // the potential stream's arguments for one problem (mode 2, j from the device counter)
 StreamArgs vstream_args(bsl_handle* h, const double* v, double* out);
 int launch_vapply_f64(const double* vb, dim3 g, cudaStream_t s, int nn, const double* v, const double* uk,

@@ -250,7 +250,8 @@ int run_iterations(bsl_handle** hs, int n, int niter) {
 // per-CTA work (problem, first unit, end unit, block index within the
 // problem); every CTA works on one problem only, so it uses that problem's
 // grid, T image, vectors, scalars and reduction buffers, and each problem's
-// alpha and beta are reduced over its own CTAs.  Four launches advance all the
+// alpha and beta are reduced over its own CTAs.  Four launches (the fused
+// iteration: x/y and z kinetic, light apply, fused update) advance all the
 // problems by one iteration; kGraphIters of them are captured into one graph.
 // ---------------------------------------------------------------------------
 
@@ -307,18 +308,22 @@ int build_grouped(bsl_handle** hs, int n, GroupedBatch* g) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, hs[0]->p.device);
   sms = std::max(1, sms);
-  // stages: 0 kinetic x/y, 1 kinetic z, 2 potential stream, 3 update
+  // stages of the fused iteration: 0 kinetic x/y, 1 kinetic z, 2 light apply
+  // (one block of points per CTA), 3 fused update (tiles)
   std::vector<long long> units[4];
+  long long light_blocks = 0;
   for (int b = 0; b < n; ++b) {
+    int rc;
+    if ((rc = ensure_product_buffer(hs[b]))) return rc;
     units[0].push_back(kin_tc_pairs(hs[b], true));
     units[1].push_back(kin_tc_pairs(hs[b], false));
-    units[2].push_back((hs[b]->t.npts + vstream_tile_points() - 1) / vstream_tile_points());
-    units[3].push_back(update_units(bsl_packed_size(hs[b]) + 1));
+    units[2].push_back((hs[b]->t.npts + light_points_per_cta() - 1) / light_points_per_cta());
+    units[3].push_back((hs[b]->t.npts + vstream_tile_points() - 1) / vstream_tile_points());
+    light_blocks += units[2].back();
   }
   const int vs = vstream_group_ctas_per_sm();
-  const long long slots[4] = {sms, sms,
-                              (long long)(hs[0]->tune_vs > 0 && hs[0]->tune_vs < vs ? hs[0]->tune_vs : vs) * sms,
-                              (long long)(hs[0]->tune_upd > 0 ? hs[0]->tune_upd : 2) * sms};
+  const long long slots[4] = {sms, sms, light_blocks,
+                              (long long)(hs[0]->tune_vs > 0 && hs[0]->tune_vs < vs ? hs[0]->tune_vs : vs) * sms};
   std::vector<int4> work[4];
   std::vector<int> ctas[4];
   for (int k = 0; k < 4; ++k) {
@@ -326,7 +331,7 @@ int build_grouped(bsl_handle** hs, int n, GroupedBatch* g) {
     g->nctas[k] = (int)work[k].size();
   }
   const size_t sz[4] = {kin_group_arg_size(), kin_group_arg_size(), vstream_group_arg_size(),
-                        update_group_arg_size()};
+                        vstream_group_arg_size()};
   std::vector<char> host;
   size_t off_args[4][2], off_work[4];
   for (int k = 0; k < 4; ++k)
@@ -350,12 +355,10 @@ int build_grouped(bsl_handle** hs, int n, GroupedBatch* g) {
       double* Vd = p ? d.rvec : d.vec;
       double* Rd = p ? d.vec : d.rvec;
       StreamArgs a = vstream_args(h, Vd, Rd);
-      a.red_count = ctas[2][b];
-      a.defer = 1;
+      a.red_count = ctas[2][b];  // the light apply's blocks: alpha's block totals
       std::memcpy(host.data() + off_args[2][p] + sz[2] * b, &a, sizeof(a));
-      update_group_arg(reinterpret_cast<const float2*>(Vd), reinterpret_cast<float2*>(Rd),
-                       bsl_packed_size(h) + 1, d.partials, d.counter, d.scalars, d.hist, d.hist_cap, d.jdev,
-                       d.status, ctas[3][b], host.data() + off_args[3][p] + sz[3] * b);
+      a.red_count = ctas[3][b];  // the fused update's CTAs: beta's block totals
+      std::memcpy(host.data() + off_args[3][p] + sz[3] * b, &a, sizeof(a));
     }
   }
   // every problem's reductions need partials for its CTAs
@@ -378,8 +381,8 @@ int grouped_iteration(GroupedBatch* g, int parity) {
   int rc;
   if ((rc = launch_kin_tc_group(true, g->args[0][parity], g->work[0], g->nctas[0], g->s)) ||
       (rc = launch_kin_tc_group(false, g->args[1][parity], g->work[1], g->nctas[1], g->s)) ||
-      (rc = launch_vstream_group(g->args[2][parity], g->work[2], g->nctas[2], g->s)) ||
-      (rc = launch_update_group(g->args[3][parity], g->work[3], g->nctas[3], g->s)))
+      (rc = launch_light_group(g->args[2][parity], g->work[2], g->nctas[2], g->s)) ||
+      (rc = launch_vstream_group(g->args[3][parity], g->work[3], g->nctas[3], g->s)))
     return rc;
   return BSL_OK;
 }
@@ -403,7 +406,9 @@ int run_grouped(bsl_handle** hs, int n, int niter) {
   cudaEvent_t ready;
   BSL_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
   for (int b = 0; b < n; ++b) {
-    if ((rc = dev_set_iteration(hs[b], 1, hs[b]->d.stream))) break;
+    // the counter and the block product of the start vector
+    if ((rc = dev_set_iteration(hs[b], 1, hs[b]->d.stream)) || (rc = dev_begin_iterations(hs[b], hs[b]->d.stream)))
+      break;
     if (b > 0) {
       cudaEventRecord(ready, hs[b]->d.stream);
       cudaStreamWaitEvent(g.s, ready, 0);

@@ -414,13 +414,14 @@ __global__ void __launch_bounds__(kTilePts, vstream_min_ctas(NN)) k_vstream(cons
 // The H v apply of a graph-replayed iteration whose block product was formed
 // by the previous update (A.vprod): R += c (u_kin + B l(l+1) v + V_blocks hi(v))
 // with the arithmetic of the stream's mode 2, one thread per grid point, and
-// alpha's block totals stored for the update.
+// alpha's block totals stored for the update.  Point p of the problem; the CTA
+// is block `index` of the `count` that reduce alpha.
 constexpr int kLightThreads = 256;
 template <int NN>
-__global__ void __launch_bounds__(kLightThreads) k_vapply_light(const StreamArgs A) {
+__device__ __forceinline__ void light_body(const StreamArgs& A, long long p, unsigned int index,
+                                           unsigned int count) {
   const int tid = threadIdx.x;
   const long long npts = A.npts;
-  const long long p = (long long)blockIdx.x * kLightThreads + tid;
   pdl_launch_dependents();
   pdl_wait();
   const float2* Vp = reinterpret_cast<const float2*>(A.vec);
@@ -457,31 +458,49 @@ __global__ void __launch_bounds__(kLightThreads) k_vapply_light(const StreamArgs
     }
   }
   // extra coordinate: H acts as 0, R' = R
-  if (blockIdx.x == 0 && tid == 0) dacc = df_fma(Vp[A.dpk], Rp[A.dpk], dacc);
+  if (index == 0 && tid == 0) dacc = df_fma(Vp[A.dpk], Rp[A.dpk], dacc);
   const double bt = block_total_df(dacc);
   if (tid == 0) {
-    A.partials[blockIdx.x] = bt;
-    if (blockIdx.x == 0) reinterpret_cast<int*>(A.scalars)[kAlphaCountSlot] = (int)gridDim.x;
+    A.partials[index] = bt;
+    if (index == 0) reinterpret_cast<int*>(A.scalars)[kAlphaCountSlot] = (int)count;
   }
 }
 
-// Grouped launch over problems with blocks of 15 or 21 functions: CTA c streams
-// tiles [work[c].y, work[c].z) of problem work[c].x and is block work[c].w of
-// that problem's alpha reduction (over probs[].red_count blocks).
+template <int NN>
+__global__ void __launch_bounds__(kLightThreads) k_vapply_light(const StreamArgs A) {
+  light_body<NN>(A, (long long)blockIdx.x * kLightThreads + threadIdx.x, blockIdx.x, gridDim.x);
+}
+
+// Grouped launches over problems with blocks of 15 or 21 functions (the fused
+// iteration of a batch), CTA c working on problem work[c].x as block
+// work[c].w of that problem's reduction (over probs[].red_count blocks): the
+// light apply of the 256 points from work[c].y * 256, and the fused update of
+// tiles [work[c].y, work[c].z).
+__global__ void __launch_bounds__(kLightThreads) k_vapply_light_group(const StreamArgs* __restrict__ probs,
+                                                                      const int4* __restrict__ work) {
+  const int4 w = work[blockIdx.x];
+  const StreamArgs A = probs[w.x];
+  const long long p = (long long)w.y * kLightThreads + threadIdx.x;
+  if (A.nn == 21)
+    light_body<21>(A, p, (unsigned)w.w, (unsigned)A.red_count);
+  else
+    light_body<15>(A, p, (unsigned)w.w, (unsigned)A.red_count);
+}
+
 __global__ void __launch_bounds__(kTilePts, 3) k_vstream_group(const StreamArgs* __restrict__ probs,
                                                                const int4* __restrict__ work) {
   const int4 w = work[blockIdx.x];
   const StreamArgs A = probs[w.x];
   if (A.vformat == BSL_VFMT_GAUNT) {
     if (A.nn == 21)
-      vstream_body<21, 2>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
+      vstream_body<21, 2, 1>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
     else
-      vstream_body<15, 2>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
+      vstream_body<15, 2, 1>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
   } else {
     if (A.nn == 21)
-      vstream_body<21, 0>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
+      vstream_body<21, 0, 1>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
     else
-      vstream_body<15, 0>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
+      vstream_body<15, 0, 1>(A, w.y, w.z, (unsigned)w.w, (unsigned)A.red_count);
   }
 }
 
@@ -544,7 +563,6 @@ struct UpdArgs {
   int hist_stride;
   int* jdev;
   int* status;
-  int red_count;  // grouped launch: blocks that reduce this problem's beta
   int defer;      // alpha from the stream's block totals here, beta's block totals left for the next kinetic
 };
 
@@ -683,15 +701,6 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream(const UpdArgs 
   update_body(a, u0, u0 + units_per_cta, blockIdx.x, gridDim.x, j_arg);
 }
 
-// Grouped launch: CTA c updates units [work[c].y, work[c].z) of problem
-// work[c].x, block work[c].w of that problem's beta reduction; j from the
-// problems' device counters.
-__global__ void __launch_bounds__(kUpdThreads, 2) k_update_stream_group(const UpdArgs* __restrict__ probs,
-                                                                        const int4* __restrict__ work) {
-  const int4 w = work[blockIdx.x];
-  const UpdArgs a = probs[w.x];
-  update_body(a, w.y, w.z, (unsigned)w.w, (unsigned)a.red_count, 0);
-}
 
 }  // namespace
 
@@ -711,23 +720,14 @@ int launch_update_stream(const float2* V, float2* R, long long L, double* partia
   const long long L2 = L / 2;
   const long long per = (L2 + grid - 1) / grid;
   const UpdArgs a{reinterpret_cast<const float4*>(V), reinterpret_cast<float4*>(R), L, partials, counter, scalars,
-                  hist, hist_stride, jdev, status, 0, defer};
+                  hist, hist_stride, jdev, status, defer};
   BSL_CUDA(launch_pdl(k_update_stream, dim3((unsigned)grid), dim3(kUpdThreads), smem, s, a, per, j));
   return BSL_OK;
 }
 
-// ---- grouped launches of the potential stream and the update ---------------
+// ---- grouped launches of the fused iteration ---------------------------------
 size_t vstream_group_arg_size() { return sizeof(StreamArgs); }
-size_t update_group_arg_size() { return sizeof(UpdArgs); }
-
-long long update_units(long long L) { return L / 2; }
-
-void update_group_arg(const float2* V, float2* R, long long L, double* partials, unsigned int* counter,
-                      double* scalars, double* hist, int hist_stride, int* jdev, int* status, int red_count,
-                      void* out) {
-  *static_cast<UpdArgs*>(out) = UpdArgs{reinterpret_cast<const float4*>(V), reinterpret_cast<float4*>(R), L,
-                                        partials, counter, scalars, hist, hist_stride, jdev, status, red_count, 1};
-}
+long long light_points_per_cta() { return kLightThreads; }
 
 int launch_finish_beta(double* partials, int count, double* scalars, double* hist, int hist_stride, int* jdev,
                        int* status, cudaStream_t s) {
@@ -754,11 +754,9 @@ int launch_vstream_group(const void* d_args, const int4* d_work, int nctas, cuda
   return BSL_OK;
 }
 
-int launch_update_group(const void* d_args, const int4* d_work, int nctas, cudaStream_t s) {
-  const size_t smem = (size_t)kUpdStages * 2 * kUpdUnits * sizeof(float4);
-  cudaFuncSetAttribute(k_update_stream_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  BSL_CUDA(launch_pdl(k_update_stream_group, dim3(nctas), dim3(kUpdThreads), smem, s,
-                      static_cast<const UpdArgs*>(d_args), d_work));
+int launch_light_group(const void* d_args, const int4* d_work, int nctas, cudaStream_t s) {
+  BSL_CUDA(launch_pdl(k_vapply_light_group, dim3(nctas), dim3(kLightThreads), 0, s,
+                      static_cast<const StreamArgs*>(d_args), d_work));
   return BSL_OK;
 }
 
