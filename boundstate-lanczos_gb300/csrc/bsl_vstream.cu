@@ -19,6 +19,13 @@
 //   u(s) = ukin(s) + B l(l+1) v(s) + sum_s' V_ss' v(s')   (FP32 block product, FP32-pair sums)
 //   mode 0: out = u (FP64);   mode 1: R += c u (FP64), partial alpha = V . R (deterministic grid reduction);
 //   mode 2: mode 1 with V and R as double-float pairs
+//
+// The iterations of a Lanczos run (graph-replayed, the fused iteration) split
+// this differently: the update streams the potential and forms the block
+// product of the next v while that v is in registers (role 1 of vstream_body),
+// and the next iteration's H v apply is element-wise (k_vapply_light).  The
+// double-float Lanczos update of the four-kernel iteration (k_update_stream)
+// and the closing kernel of the deferred beta are here too.
 #include <cuda_bf16.h>
 
 #include <type_traits>
