@@ -608,8 +608,20 @@ int bsl_autotune(bsl_handle** hs, int n, int iters, int* vs_per_sm, int* upd_per
       pb[b] = bb.data() + (size_t)b * (wv + 1);
       pb2[b] = b2.data() + (size_t)b * (wv + 1);
     }
+    // the update's shape matters only where a problem runs the streamed update
+    // (the fused iteration and the grouped batch do not use it): there it is
+    // timed too, elsewhere it stays at the default 2
+    bool upd_matters = false;
+    if (!(n > 1 && groupable(hs, n)))
+      for (int b = 0; b < n; ++b) {
+        const bsl_handle* h = hs[b];
+        if (!(h->precision == BSL_PREC_MIXED && h->kinetic_engine == BSL_KIN_TENSOR &&
+              fused_update_supported(h->vformat, h->t.nn)))
+          upd_matters = true;
+      }
+    const int up_lo = upd_matters ? 1 : 2, up_hi = upd_matters ? 3 : 2;
     for (int vs = 1; vs <= 3; ++vs)
-      for (int up = 1; up <= 3; ++up) {
+      for (int up = up_lo; up <= up_hi; ++up) {
         for (int b = 0; b < n; ++b) {
           hs[b]->tune_vs = vs;
           hs[b]->tune_upd = up;

@@ -404,7 +404,8 @@ int bsl_stage_times(bsl_handle* h, int iters, double* ms, const char** names);
    `iters` Lanczos iterations of the problem (n = 1, bsl_lanczos_run) or of the
    batch (n > 1, bsl_lanczos_run_batch) for each launch shape that the
    problem's size does not fix -- resident CTAs per SM of the potential stream
-   (1-3, capped by its occupancy) and of the update (1-3) -- and keeps the
+   or the fused update (1-3, capped by its occupancy) and, where a problem runs
+   the streamed update, of that update (1-3; else it stays 2) -- and keeps the
    fastest in the handles for later runs.  The choice is cached per problem
    set (block sizes, grids, precision, kinetic engine, block format, slices),
    so a later call with the same sizes reuses it without timing.  Outputs (any
