@@ -291,6 +291,13 @@ def stage_bytes(cfg, D, N, nn, mixed, rows=None, names=()):
             3 * (D + 1) * 8]        # r -= alpha v, beta^2: read v, r; write r (scales fold the swap)
 
 
+def run_extra_launches(names):
+    """Launches of a device-counted Lanczos run besides its iterations: the
+    counter reset and the closing kernel of the deferred beta, and with the
+    fused iteration the block product of the start vector."""
+    return 3 if any("k_vapply_light" in n for n in names) else 2
+
+
 def levels_of(bsl, a, b, b2, count):
     ev, _ = bsl.good_eigenvalues(a, b, b2, -1.0e3, 1.0e3)
     return ev
@@ -653,7 +660,7 @@ def main():
                              reference_vs_port_note="compiled reference vs this port, H v ms, 8 threads, x86 "
                                                     "build container; the port is faster, so the baseline is "
                                                     "conservative"),
-        "clocks": clocks, "gpu_launches": nst * args.steps, "prep_seconds": prep_s,
+        "clocks": clocks, "gpu_launches": nst * args.steps + run_extra_launches(stage_names), "prep_seconds": prep_s,
         "launch_shapes": {"potential_stream_ctas_per_sm": tune[0], "update_ctas_per_sm": tune[1],
                           "autotune_ms_per_iter": tune[2], "by": "bsl_autotune"},
         "wall_ms_per_step": 1000.0 * wall / args.steps,
