@@ -405,9 +405,9 @@ def batched_workload(bsl, tmp, device, fp64_check=True, nlev=10):
            "edges": [pr["n"] for pr in probs], "blocks": [h.nn for h in hs],
            "batched_iter_s": total / (batch_ms * 1e-3), "batched_ms": batch_ms,
            "path": "bsl_lanczos_run_batch: four grouped launches per iteration of all the problems "
-                   "(each CTA on one problem), 8-iteration graph",
+                   "(each CTA on one problem), 32-iteration graph",
            "streams_iter_s": total / (streams_ms * 1e-3), "streams_ms": streams_ms,
-           "streams_path": "bsl_lanczos_run_batch_streams: one stream per problem, 8-iteration graphs "
+           "streams_path": "bsl_lanczos_run_batch_streams: one stream per problem, 32-iteration graphs "
                            "interleaved",
            "sequential_iter_s": total / (sep_ms * 1e-3), "sequential_ms": sep_ms,
            "prep_seconds": prep_s,

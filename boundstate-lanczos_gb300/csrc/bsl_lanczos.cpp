@@ -159,7 +159,7 @@ int check_status(bsl_handle* h) {
 // The graph is kept with the handle until the precision, the kinetic engine
 // or the history buffer changes.  The remainder, and every other
 // configuration, is launched directly.
-constexpr int kGraphIters = 8;
+constexpr int kGraphIters = 32;
 
 // capture kGraphIters device-counted iterations of h on its stream (nothing
 // runs) unless the cached graph already matches the current configuration

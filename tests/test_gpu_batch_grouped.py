@@ -9,7 +9,7 @@ bsl_lanczos_run calls with the same start vector:
   1e-10 (alpha and beta are reduced over each problem's own CTAs, a different
   split of the same sums, whose last-bit differences the recurrence amplifies:
   2e-12 at alpha_10 measured);
-* after 801 iterations (100 graph blocks of 8 and a remainder of 1), every
+* after 801 iterations (25 graph blocks of 32 and a remainder of 1), every
   level the separate run has converged (unchanged to 1e-9 kJ/mol over its
   last 200 iterations, at least 2 per problem) within 1e-6 kJ/mol of a level
   of the grouped run (after 301 iterations levels that had moved by less than

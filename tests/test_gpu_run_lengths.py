@@ -1,5 +1,5 @@
 """Runs of every length on the graph-replayed fused iteration: a Lanczos run of
-n iterations launches n // 8 replays of the 8-iteration graph and n % 8
+n iterations launches n // 32 replays of the 32-iteration graph and n % 32
 direct iterations, each run starts with the block product of the start
 vector, and the beta that the last iteration leaves pending is finished by a
 closing kernel.  The kernels are deterministic, so the alpha/beta of an
@@ -26,14 +26,14 @@ def test_every_run_length_is_a_prefix_of_a_longer_run():
     finally:
         os.chdir(cwd)
     try:
-        a64, b64, _ = h.lanczos(24, start="normal", seed=5)
+        a64, b64, _ = h.lanczos(72, start="normal", seed=5)
         h.set_precision("mixed")
         assert h.kinetic_engine() == "tensor"
-        A, B, B2 = h.lanczos(24, start="normal", seed=5)
+        A, B, B2 = h.lanczos(72, start="normal", seed=5)
         scale = np.max(np.abs(a64))
         assert np.max(np.abs(A[:6] - a64[:6])) <= 1e-6 * scale
         assert np.max(np.abs(B[1:7] - b64[1:7])) <= 1e-6 * scale
-        for n in (1, 2, 7, 8, 9, 16, 17, 23):
+        for n in (1, 2, 31, 32, 33, 40, 64, 65, 71):
             a, b, b2 = h.lanczos(n, start="normal", seed=5)
             assert np.array_equal(a, A[:n]), n
             assert np.array_equal(b, B[:n + 1]) and np.array_equal(b2, B2[:n + 1]), n
